@@ -1,0 +1,482 @@
+"""Benchmark: forward + adjoint samples/s of the ray marcher.
+
+Workload (TF reconstruction): 256^3 volume of 32 seeded Gaussian blobs plus
+0.02 uniform noise, 64-entry RGBA texture TF initialised U(0,1), 8 views at
+256x256 on a Fibonacci sphere at radius 3 (FOV 45 deg), Beer-Lambert, step
+0.25 voxel, trilinear.  One step = forward render of the 8 views (with
+transmittance checkpoints) + L2-loss gradient against a target image + adjoint
+render accumulating the TF gradient.  Samples per step S = sum of the forward
+termination indices.  Synthetic data (seeded), as the reference has no public
+dataset for this path.
+
+Arms:
+  default          the optimized kernels, volume stored in BF16, all 8 views
+                   in one launch per pass, the step captured in a CUDA graph
+                   (`value`, device-resident); `e2e` runs the same step
+                   through pyrenderer.Renderer with the inputs copied from
+                   pinned host memory every step and the loss and TF gradient
+                   read back.  The plain FP32 kernels are timed beside it.
+  --impl reference the reference's CPU implementation of the path on the host
+                   cores (the reference's own CPU marcher where it was built
+                   here, else the oracle port), on a bounded sample of rays.
+
+Multi-GPU: rays and views shard without any exchange in a TF-only step except
+the TF-gradient sum, so N GPUs run N replicas ("scaling": "weak").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "fwd+adjoint samples/sec: batched-BF16 vs plain FP32, grad rel err ≤1e-3"
+WORKLOAD = "tf_reconstruction_256: 256^3 blobs+noise, texture TF R=64, 8 views 256x256, step 0.25 voxel, TF grad"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--res", type=int, default=256)
+    ap.add_argument("--views", type=int, default=8)
+    ap.add_argument("--image", type=int, default=256)
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP32 comparison arm")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline budget")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ workload
+def make_workload(args):
+    from diffdvr_gb300 import scenes
+    w = scenes.tf_reconstruction_256(seed=1, res=args.res, views=args.views, image=args.image)
+    return w
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "roofline_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return None
+
+
+# ------------------------------------------------------------------ GPU arm
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+    from diffdvr_gb300 import _abi, pyrenderer as pr
+
+    rank, world, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    _abi.load()
+
+    w = make_workload(args)
+    B, H, W = args.views, args.image, args.image
+    vol32 = torch.from_numpy(w.volume).to(dev)
+    vol16 = vol32.to(torch.bfloat16)
+    tf = torch.from_numpy(w.tf).to(dev)
+    viewport = torch.from_numpy(w.viewport.astype(np.float32)).to(dev)
+
+    def inputs(volume, tf_t, vp):
+        inp = pr.RendererInputs()
+        inp.screen_size = pr.int2(W, H)
+        inp.volume = volume
+        inp.volume_filter_mode = pr.VolumeFilterMode.Trilinear
+        inp.box_min = pr.real3(*w.box_min)
+        inp.box_size = pr.real3(*w.box_size)
+        inp.camera_mode = pr.CameraMode.ReferenceFrame
+        inp.camera = pr.CameraReferenceFrame(vp, float(w.fov_y))
+        inp.step_size = float(w.step_size)
+        inp.tf_mode = pr.TFMode.Texture
+        inp.tf = tf_t
+        inp.blend_mode = pr.BlendMode.BeerLambert
+        return inp
+
+    inp16 = inputs(vol16, tf, viewport)
+    slots = pr.Renderer.checkpoint_slots(inp16, 32)
+    color = torch.empty(B, H, W, 4, device=dev)
+    term = torch.empty(B, H, W, dtype=torch.int32, device=dev)
+    ckpt = torch.empty(B, H, W, slots, device=dev)
+    out = pr.RendererOutputs(color, term, ckpt, 32)
+    adj_tf = torch.zeros_like(tf)
+    adj = pr.AdjointOutputs()
+    adj.has_tf_derivatives = True
+    adj.tf_delayed_accumulation = True
+    adj.adj_tf = adj_tf
+    adj_color = torch.empty_like(color)
+
+    # target image: the same views rendered with the TF perturbed
+    g = torch.Generator(device="cpu").manual_seed(3)
+    tf_target = (tf.cpu() + 0.05 * torch.randn(tf.shape, generator=g)).clamp_min(0).to(dev)
+    target = torch.empty_like(color)
+    pr.set_kernel_family("optimized")
+    pr.Renderer.render_forward(inputs(vol16, tf_target, viewport), pr.RendererOutputs(target, torch.empty_like(term)))
+    torch.cuda.synchronize()
+    inv_n = 1.0 / color.numel()
+
+    stream = torch.cuda.Stream(device=dev)
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    fwd_ev, adj_ev = [], []
+
+    def step(record=False):
+        # forward + L2-loss gradient + adjoint of the TF
+        if record:
+            e = (ev(), ev(), ev(), ev())
+            e[0].record()
+        pr.Renderer.render_forward(inp16, out)
+        if record:
+            e[1].record()
+        torch.sub(color, target, out=adj_color)
+        adj_color.mul_(2 * inv_n)
+        adj_tf.zero_()
+        if record:
+            e[2].record()
+        pr.Renderer.render_adjoint(inp16, out, adj_color, adj)
+        if record:
+            e[3].record()
+            fwd_ev.append((e[0], e[1]))
+            adj_ev.append((e[2], e[3]))
+
+    with torch.cuda.stream(stream):
+        step()
+    torch.cuda.synchronize()
+    samples = int(term.to(torch.int64).sum().item())
+    rays_hit = int((term > 0).sum().item())
+
+    # capture the step in a CUDA graph
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(stream):
+        step()
+        torch.cuda.synchronize()
+        with torch.cuda.graph(graph, stream=stream):
+            step()
+    torch.cuda.synchronize()
+
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
+
+    def timed(fn, steps, warmup, pre=None):
+        for _ in range(warmup):
+            if pre:
+                pre()
+            fn()
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        starts = [ev() for _ in range(steps)]
+        stops = [ev() for _ in range(steps)]
+        cur = torch.cuda.current_stream()
+        for i in range(steps):
+            flush.zero_()
+            if pre:
+                pre()
+            starts[i].record(cur)
+            fn()
+            stops[i].record(cur)
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        return sum(a.elapsed_time(b) for a, b in zip(starts, stops)) / steps
+
+    # ---- value: device-resident, graph replay
+    with torch.cuda.stream(stream):
+        with ClockSampler(local) as clocks:
+            ms_graph = timed(lambda: graph.replay(), args.steps, args.warmup)
+    clock_summary = clocks.summary()
+
+    # ---- kernel durations for the roofline (same stream, events around launches)
+    fwd_ev.clear()
+    adj_ev.clear()
+    with torch.cuda.stream(stream):
+        for _ in range(max(3, args.steps // 2)):
+            flush.zero_()
+            step(record=True)
+        torch.cuda.synchronize()
+    fwd_ms = float(np.mean([a.elapsed_time(b) for a, b in fwd_ev]))
+    adj_ms = float(np.mean([a.elapsed_time(b) for a, b in adj_ev]))
+
+    # ---- e2e: public API with host buffers
+    vol_host = vol16.cpu().pin_memory()
+    tf_host = tf.cpu().pin_memory()
+    vp_host = viewport.cpu().pin_memory()
+    target_host = target.cpu().pin_memory()
+    loss_host = torch.empty(1, pin_memory=True)
+    grad_host = torch.empty_like(tf_host).pin_memory()
+    vol_d, tf_d, vp_d, tgt_d = torch.empty_like(vol16), torch.empty_like(tf), torch.empty_like(viewport), \
+        torch.empty_like(target)
+    inp_e2e = inputs(vol_d, tf_d, vp_d)
+    loss_d = torch.empty(1, device=dev)
+
+    def e2e_step():
+        vol_d.copy_(vol_host, non_blocking=True)
+        tf_d.copy_(tf_host, non_blocking=True)
+        vp_d.copy_(vp_host, non_blocking=True)
+        tgt_d.copy_(target_host, non_blocking=True)
+        pr.Renderer.render_forward(inp_e2e, out)
+        torch.sub(color, tgt_d, out=adj_color)
+        loss_d.copy_((adj_color * adj_color).sum().view(1))
+        adj_color.mul_(2 * inv_n)
+        adj_tf.zero_()
+        pr.Renderer.render_adjoint(inp_e2e, out, adj_color, adj)
+        loss_host.copy_(loss_d, non_blocking=True)
+        grad_host.copy_(adj_tf, non_blocking=True)
+
+    with torch.cuda.stream(stream):
+        ms_e2e = timed(e2e_step, args.steps, args.warmup)
+    h2d = vol_host.numel() * vol_host.element_size() + tf_host.numel() * 4 + vp_host.numel() * 4 + \
+        target_host.numel() * 4
+    d2h = 4 + grad_host.numel() * 4
+
+    # ---- plain FP32 arm (same workload, the reference's GPU algorithm)
+    plain = None
+    if not args.no_plain:
+        inp32 = inputs(vol32, tf, viewport)
+        out32 = pr.RendererOutputs(torch.empty_like(color), torch.empty_like(term))
+        adj32 = pr.AdjointOutputs()
+        adj32.has_tf_derivatives = True
+        adj32.tf_delayed_accumulation = True
+        adj32.adj_tf = torch.zeros_like(tf)
+
+        def plain_step():
+            pr.Renderer.render_forward(inp32, out32)
+            torch.sub(out32.color, target, out=adj_color)
+            adj_color.mul_(2 * inv_n)
+            adj32.adj_tf.zero_()
+            pr.Renderer.render_adjoint(inp32, out32, adj_color, adj32)
+
+        pr.set_kernel_family("plain")
+        with torch.cuda.stream(stream):
+            ms_plain = timed(plain_step, max(2, args.steps // 4), 2)
+        pr.set_kernel_family("optimized")
+        samples32 = int(out32.terminationIndex.to(torch.int64).sum().item())
+        plain = {"samples_per_s": samples32 / (ms_plain / 1e3), "ms_per_step": ms_plain,
+                 "kernels": "plain FP32 (one thread per ray, blend inversion)"}
+
+    # ---- aggregate over ranks (max time)
+    t = torch.tensor([ms_graph, ms_e2e], device=dev, dtype=torch.float64)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_graph, ms_e2e = float(t[0]), float(t[1])
+    value = samples * world / (ms_graph / 1e3)
+    e2e_value = samples * world / (ms_e2e / 1e3)
+
+    # ---- roofline of the dominant kernel (compulsory HBM bytes per launch)
+    peak, peak_kind = measured_peaks()
+    V = args.res ** 3
+    P = B * H * W
+    ck_written = int(torch.clamp((term.to(torch.int64) - 1) // 32, min=0).clamp_max(slots).sum().item())
+    fwd_bytes = V * 2 + P * (16 + 4) + ck_written * 4
+    adj_bytes = V * 2 + P * (4 + 16) + ck_written * 4 + tf.numel() * 4 * 2
+    dominant = ("adjoint", adj_bytes, adj_ms) if adj_ms >= fwd_ms else ("forward", fwd_bytes, fwd_ms)
+    achieved = dominant[1] / (dominant[2] / 1e3) / 1e9
+    tr = profiled_traffic()
+    traffic = None
+    if tr and tr.get("kernel") == dominant[0]:
+        traffic = tr.get("dram_bytes_per_launch")
+    gather_bytes = samples * 8 * 2 * 2  # 8 BF16 corner reads per sample, forward and adjoint
+
+    result = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "samples/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_graph,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "bf16-storage/f32-compute",
+        "data": "synthetic (seeded blobs + noise, random TF, Fibonacci views)",
+        "config": {"workload": WORKLOAD, "volume_storage": "bf16", "tf_storage": "f32", "views": B,
+                   "image": [H, W], "volume": [args.res] * 3, "samples_per_step": samples, "rays_hit": rays_hit,
+                   "checkpoint_interval": 32, "l2": "flushed (256 MB write) before every timed step",
+                   "graph": "forward+loss+adjoint captured in one CUDA graph",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": e2e_value, "unit": "samples/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": ms_e2e,
+                "path": "pyrenderer.Renderer.render_forward/render_adjoint, pinned host inputs"},
+        "gpu_launches": 2 * args.steps,
+        "kernel_ms": {"forward": fwd_ms, "adjoint": adj_ms},
+        "roofline": {"bound": "hbm", "kernel": dominant[0], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_launch": int(dominant[1]),
+                     "gather_model_GBps": gather_bytes / ((fwd_ms + adj_ms) / 1e3) / 1e9},
+        "plain_fp32": plain,
+        "speedup_vs_plain_fp32": (value / plain["samples_per_s"]) if plain else None,
+        "clocks": clock_summary,
+    }
+    if rank == 0:
+        result["cpu_baseline"] = cpu_baseline(w, args, samples / P)
+        print(json.dumps(result))
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+# ------------------------------------------------------------------ CPU (reference) arm
+def cpu_sample_scene(w, n_rays: int, seed: int = 0):
+    """A bounded sample of the workload: n_rays rays of the 8 views, chosen
+    among rays that hit the volume, as one 1 x n_rays 'image'."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(seed)
+    rs = w.ray_start.reshape(-1, 3)
+    rd = w.ray_dir.reshape(-1, 3)
+    # rays whose line passes within the box's circumsphere
+    t = -(rs * rd).sum(1)
+    closest = rs + t[:, None] * rd
+    hit = np.nonzero(np.linalg.norm(closest, axis=1) < 0.866)[0]
+    idx = rng.choice(hit, size=min(n_rays, hit.size), replace=False)
+    sc = O.Scene(width=idx.size, height=1, volume=w.volume, tf=w.tf, step_size=np.full((1, 1, 1), w.step_size),
+                 box_min=np.array([w.box_min]), box_size=np.array([w.box_size]), filter_mode=1, camera_mode=0,
+                 tf_mode=1, blend_mode=0, ray_start=rs[idx][None, None], ray_dir=rd[idx][None, None])
+    return sc
+
+
+def time_cpu(w, budget_s: float, kind: str):
+    """Forward + TF adjoint of a ray sample on the host cores; returns
+    (samples/s, description)."""
+    from oracle import oracle as O
+    n = 512
+    while True:
+        sc = cpu_sample_scene(w, n)
+        t0 = time.perf_counter()
+        c, term = O.forward(sc, kind, "f32")
+        adj = np.full(c.shape, 1e-3, np.float32)
+        O.adjoint(sc, c, term, adj, O.AdjointRequest(tf=True), kind, "f32")
+        dt = time.perf_counter() - t0
+        if dt > budget_s / 6 or n >= 65536:
+            break
+        n *= 2
+    reps, total, samples = 0, 0.0, 0
+    while total < budget_s * 0.7 or reps < 2:
+        t0 = time.perf_counter()
+        c, term = O.forward(sc, kind, "f32")
+        O.adjoint(sc, c, term, np.full(c.shape, 1e-3, np.float32), O.AdjointRequest(tf=True), kind, "f32")
+        total += time.perf_counter() - t0
+        samples += int(term.sum())
+        reps += 1
+    return samples / total, f"{sc.width} rays of the workload (hitting the volume), {reps} fwd+adj passes"
+
+
+def cpu_baseline(w, args, _samples_per_ray):
+    from oracle import oracle as O
+    O.build(reference=True)
+    kind = "reference" if O.reference_available() else "port"
+    value, sample = time_cpu(w, args.cpu_seconds, kind)
+    return {"value": value, "unit": "samples/s", "cores": os.cpu_count(), "kind": kind, "sample": sample}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.build(reference=True)
+    kind = "reference" if O.reference_available() else "port"
+    w = make_workload(args)
+    for _ in range(args.warmup):
+        time_cpu(w, 1.0, kind)
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        v, sample = time_cpu(w, max(1.0, args.cpu_seconds / max(args.steps, 1)), kind)
+        vals.append(v)
+    wall = time.perf_counter() - t0
+    value = float(np.median(vals))
+    res = {"metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": wall * 1e3 / max(args.steps, 1), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": WORKLOAD, "sample": sample}, "impl": "reference",
+           "cpu_baseline": {"value": value, "unit": "samples/s", "cores": os.cpu_count(), "kind": kind,
+                            "sample": sample},
+           "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(res))
+
+
+if __name__ == "__main__":
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_gpu(a)

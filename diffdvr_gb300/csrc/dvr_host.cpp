@@ -1,0 +1,657 @@
+// Host layer of the C ABI: validates the descriptors the way the reference's
+// renderer::Renderer does (renderer/renderer.cpp:49-391 checkInputs /
+// checkOutput / checkAdjointOutput, renderer/renderer.cpp:660-742 for the
+// adjoint), flattens them into kernel parameter blocks and dispatches to the
+// kernel families.  C++ internally, plain C at the boundary: nothing throws
+// across it.
+#include "../../include/diffdvr_gb300.h"
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "dvr_kernels.h"
+#include "dvr_batch.h"
+
+namespace dvr {
+namespace {
+
+thread_local std::string g_last_error;
+std::atomic<int> g_family{DVR_KERNELS_OPTIMIZED};
+std::atomic<int> g_sync{0};
+
+struct DvrError : std::runtime_error {
+  int code;
+  DvrError(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+[[noreturn]] void fail(int code, const std::string& msg) { throw DvrError(code, msg); }
+
+std::string shape_str(const DvrTensor& t) {
+  std::ostringstream os;
+  os << "[";
+  for (int i = 0; i < t.ndim; ++i) os << (i ? ", " : "") << t.sizes[i];
+  os << "]";
+  return os.str();
+}
+
+const char* dtype_name(int d) {
+  switch (d) {
+    case DVR_FLOAT32: return "float32";
+    case DVR_FLOAT64: return "float64";
+    case DVR_FLOAT16: return "float16";
+    case DVR_BFLOAT16: return "bfloat16";
+    case DVR_INT32: return "int32";
+    default: return "unknown";
+  }
+}
+
+// ---- the reference's CHECK_* macros (renderer/pytorch_utils.h:5-20) ----
+void check_dim(const DvrTensor& t, const char* name, int d) {
+  if (t.ndim < 0) fail(DVR_E_INVALID_ARGUMENT, std::string(name) + " is not defined!");
+  if (t.ndim != d) {
+    std::ostringstream os;
+    os << name << " must be a tensor with " << d << " dimensions, but has shape " << shape_str(t);
+    fail(DVR_E_INVALID_ARGUMENT, os.str());
+  }
+}
+void check_size(const DvrTensor& t, const char* name, int d, int64_t s) {
+  if (t.sizes[d] != s) {
+    std::ostringstream os;
+    os << name << " must have " << s << " entries at dimension " << d << ", but has " << t.sizes[d] << " entries";
+    fail(DVR_E_INVALID_ARGUMENT, os.str());
+  }
+}
+void check_dtype(const DvrTensor& t, const char* name, int dtype) {
+  if (t.dtype != dtype) {
+    std::ostringstream os;
+    os << name << " must be of type " << dtype_name(dtype) << ", but is " << dtype_name(t.dtype);
+    fail(DVR_E_INVALID_ARGUMENT, os.str());
+  }
+}
+void check_device(const DvrTensor& t, const char* name, int device_index) {
+  if (t.device_type != DVR_DEVICE_CUDA) {
+    fail(DVR_E_INVALID_ARGUMENT, std::string(name) +
+                                     " is a CPU tensor: diffdvr_gb300 renders on CUDA devices only, and all "
+                                     "tensors must be on the same device");
+  }
+  if (t.device_index != device_index) {
+    std::ostringstream os;
+    os << "All tensors must be on the same device, but " << name << " is on cuda:" << t.device_index
+       << " instead of cuda:" << device_index;
+    fail(DVR_E_INVALID_ARGUMENT, os.str());
+  }
+}
+int check_batch(const DvrTensor& t, const char* name, int B1, int batch_index = 0) {
+  const int B2 = int(t.sizes[batch_index]);
+  if (B2 == 1) return B1;
+  if (B1 == 1) return B2;
+  if (B1 != B2) {
+    std::ostringstream os;
+    os << name << " must be have the same batch size as other tensors, if batch>1. actual=" << B2
+       << ", expected=" << B1;
+    fail(DVR_E_INVALID_ARGUMENT, os.str());
+  }
+  return B1;
+}
+
+// broadcast-aware view: a dimension of size 1 gets stride 0
+InView in_view(const DvrTensor& t) {
+  InView v{};
+  v.p = t.data;
+  for (int i = 0; i < 4 && i < t.ndim; ++i) v.s[i] = t.sizes[i] == 1 ? 0 : t.strides[i];
+  return v;
+}
+OutView out_view(const DvrTensor& t, bool broadcast) {
+  OutView v{};
+  v.p = t.data;
+  for (int i = 0; i < 4 && i < t.ndim; ++i) v.s[i] = (broadcast && t.sizes[i] == 1) ? 0 : t.strides[i];
+  return v;
+}
+
+struct DeviceInfo {
+  bool valid = false;
+  LaunchInfo li{};
+};
+std::mutex g_dev_mutex;
+DeviceInfo g_dev[64];
+
+LaunchInfo launch_info(int device) {
+  std::lock_guard<std::mutex> lock(g_dev_mutex);
+  if (device < 0 || device >= 64) fail(DVR_E_INVALID_ARGUMENT, "device index out of range");
+  DeviceInfo& d = g_dev[device];
+  if (!d.valid) {
+    int sms = 0, smem = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, device) != cudaSuccess) {
+      cudaGetLastError();
+      fail(DVR_E_CUDA, "cannot query CUDA device " + std::to_string(device));
+    }
+    d.li.num_sms = sms;
+    d.li.max_smem_optin = smem;
+    d.valid = true;
+  }
+  return d.li;
+}
+
+// Restores the caller's current device on scope exit.
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int device) {
+    if (cudaGetDevice(&prev) != cudaSuccess) {
+      cudaGetLastError();
+      fail(DVR_E_CUDA, "no CUDA device available");
+    }
+    if (prev != device && cudaSetDevice(device) != cudaSuccess) {
+      cudaGetLastError();
+      fail(DVR_E_CUDA, "cannot select CUDA device " + std::to_string(device));
+    }
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    if (cudaGetDevice(&cur) == cudaSuccess && cur != prev && prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+// Resolved inputs of one render call.
+struct Checked {
+  RenderParams p{};
+  int filter = 1, tf_mode = 1, blend = 0;
+  int device = 0;
+};
+
+bool real_storage_ok(int dtype) { return dtype == DVR_FLOAT32 || dtype == DVR_FLOAT16 || dtype == DVR_BFLOAT16; }
+
+// renderer::Renderer::checkInputs (renderer/renderer.cpp:49-263)
+Checked check_inputs(const DvrRendererInputs& in) {
+  Checked c;
+  RenderParams& p = c.p;
+  p.W = in.screen_width;
+  p.H = in.screen_height;
+  if (p.W < 0 || p.H < 0) fail(DVR_E_INVALID_ARGUMENT, "screen size must be non-negative");
+
+  const DvrTensor& volume = in.volume;
+  check_dim(volume, "volume", 4);
+  c.device = volume.device_index;
+  check_device(volume, "volume", c.device);
+  if (!real_storage_ok(volume.dtype))
+    fail(DVR_E_INVALID_ARGUMENT, std::string("volume must be of type float32 (or float16/bfloat16), but is ") +
+                                     dtype_name(volume.dtype));
+  int B = int(volume.sizes[0]);
+  p.X = int(volume.sizes[1]);
+  p.Y = int(volume.sizes[2]);
+  p.Z = int(volume.sizes[3]);
+  if (in.volume_filter_mode == DVR_FILTER_PRESHADED || in.tf_mode == DVR_TF_PRESHADED)
+    fail(DVR_E_UNSUPPORTED, "pre-shaded volumes are not supported by diffdvr_gb300");
+  if (in.volume_filter_mode != DVR_FILTER_NEAREST && in.volume_filter_mode != DVR_FILTER_TRILINEAR)
+    fail(DVR_E_INVALID_ARGUMENT, "unknown volume filter enum value");
+  if (p.X < 1 || p.Y < 1 || p.Z < 1) fail(DVR_E_INVALID_ARGUMENT, "volume must have at least one voxel per axis");
+  {
+    // offsets inside one batch entry are 32-bit, as the reference's accessors
+    const double span = double(p.X - 1) * std::fabs(double(volume.strides[1])) +
+                        double(p.Y - 1) * std::fabs(double(volume.strides[2])) +
+                        double(p.Z - 1) * std::fabs(double(volume.strides[3]));
+    if (span >= 2147483647.0) fail(DVR_E_INVALID_ARGUMENT, "volume is too large: one batch entry must hold < 2^31 elements");
+  }
+  p.vol_storage = volume.dtype;
+  p.volume = in_view(volume);
+  c.filter = in.volume_filter_mode;
+
+  auto vec3_input = [&](int kind, const DvrTensor& t, const double* val, const char* name, InView& out) {
+    if (kind == DVR_KIND_TENSOR) {
+      check_dim(t, name, 2);
+      check_device(t, name, c.device);
+      check_size(t, name, 1, 3);
+      B = check_batch(t, name, B);
+      check_dtype(t, name, DVR_FLOAT32);
+      out = in_view(t);
+    } else if (kind == DVR_KIND_VALUE) {
+      out = InView{};
+      out.p = nullptr;
+      for (int i = 0; i < 3; ++i) out.val[i] = float(val[i]);
+    } else {
+      fail(DVR_E_INVALID_ARGUMENT, std::string("unknown kind for ") + name);
+    }
+  };
+  vec3_input(in.box_min_kind, in.box_min, in.box_min_value, "boxMin", p.box_min);
+  vec3_input(in.box_size_kind, in.box_size, in.box_size_value, "boxSize", p.box_size);
+
+  p.camera_mode = in.camera_mode;
+  switch (in.camera_mode) {
+    case DVR_CAMERA_RAY_START_DIR: {
+      if (in.camera_kind != DVR_CAMERA_PER_PIXEL_RAYS)
+        fail(DVR_E_INVALID_ARGUMENT,
+             "'CameraRayStartDir' specified in 'cameraMode', but 'camera' does not hold the first variant "
+             "'CameraPerPixelRays'");
+      const DvrTensor& rs = in.camera_ray_start;
+      const DvrTensor& rd = in.camera_ray_dir;
+      check_dim(rs, "cameraRayStart", 4);
+      check_device(rs, "cameraRayStart", c.device);
+      check_size(rs, "cameraRayStart", 1, p.H);
+      check_size(rs, "cameraRayStart", 2, p.W);
+      check_size(rs, "cameraRayStart", 3, 3);
+      B = check_batch(rs, "cameraRayStart", B);
+      check_dtype(rs, "cameraRayStart", DVR_FLOAT32);
+      check_dim(rd, "cameraRayDir", 4);
+      check_device(rd, "cameraRayDir", c.device);
+      check_size(rd, "cameraRayDir", 1, p.H);
+      check_size(rd, "cameraRayDir", 2, p.W);
+      check_size(rd, "cameraRayDir", 3, 3);
+      B = check_batch(rd, "cameraRayDir", B);
+      check_dtype(rd, "cameraRayDir", DVR_FLOAT32);
+      p.ray_start = in_view(rs);
+      p.ray_dir = in_view(rd);
+    } break;
+    case DVR_CAMERA_INVERSE_VIEW_MATRIX: {
+      if (in.camera_kind == DVR_CAMERA_INVERSE_VIEW_TENSOR) {
+        const DvrTensor& m = in.camera_matrix;
+        check_dim(m, "cameraMatrix", 3);
+        check_device(m, "cameraMatrix", c.device);
+        check_size(m, "cameraMatrix", 1, 4);
+        check_size(m, "cameraMatrix", 2, 4);
+        B = check_batch(m, "cameraMatrix", B);
+        check_dtype(m, "cameraMatrix", DVR_FLOAT32);
+        p.cam = in_view(m);
+      } else if (in.camera_kind == DVR_CAMERA_INVERSE_VIEW_VALUE) {
+        p.cam = InView{};
+        for (int i = 0; i < 16; ++i) p.cam_value[i] = in.camera_matrix_value[i];
+      } else {
+        fail(DVR_E_INVALID_ARGUMENT,
+             "'CameraInverseViewMatrix' specified in 'cameraMode', but 'camera' holds neither a B*4*4 tensor nor "
+             "a mat4");
+      }
+    } break;
+    case DVR_CAMERA_REFERENCE_FRAME: {
+      if (in.camera_kind != DVR_CAMERA_REFERENCE_FRAME_KIND)
+        fail(DVR_E_INVALID_ARGUMENT,
+             "'CameraReferenceFrame' specified in 'cameraMode', but 'camera' does not hold the fourth variant "
+             "'CameraReferenceFrame'");
+      const DvrTensor& m = in.camera_matrix;
+      check_dim(m, "cameraMatrix", 3);
+      check_device(m, "cameraMatrix", c.device);
+      check_size(m, "cameraMatrix", 1, 3);
+      check_size(m, "cameraMatrix", 2, 3);
+      B = check_batch(m, "cameraMatrix", B);
+      check_dtype(m, "cameraMatrix", DVR_FLOAT32);
+      p.cam = in_view(m);
+      p.fov_y = float(in.camera_fov_y_radians);
+    } break;
+    default:
+      fail(DVR_E_INVALID_ARGUMENT, "unknown camera enum value");
+  }
+
+  if (in.step_size_kind == DVR_KIND_TENSOR) {
+    const DvrTensor& s = in.step_size;
+    check_dim(s, "stepSize", 3);
+    check_device(s, "stepSize", c.device);
+    B = check_batch(s, "stepSize", B);
+    check_batch(s, "stepSize-Height", p.H, 1);
+    check_batch(s, "stepSize-Width", p.W, 2);
+    check_dtype(s, "stepSize", DVR_FLOAT32);
+    p.step = in_view(s);
+  } else if (in.step_size_kind == DVR_KIND_VALUE) {
+    p.step = InView{};
+    p.step.val[0] = float(in.step_size_value);
+  } else {
+    fail(DVR_E_INVALID_ARGUMENT, "unknown kind for stepSize");
+  }
+
+  const DvrTensor& tf = in.tf;
+  check_dim(tf, "tf", 3);
+  check_device(tf, "tf", c.device);
+  B = check_batch(tf, "tf", B);
+  switch (in.tf_mode) {
+    case DVR_TF_IDENTITY:
+      check_size(tf, "tf", 1, 1);
+      check_size(tf, "tf", 2, 2);
+      break;
+    case DVR_TF_TEXTURE:
+      check_size(tf, "tf", 2, 4);
+      break;
+    case DVR_TF_LINEAR:
+      check_size(tf, "tf", 2, 5);
+      if (tf.sizes[1] <= 1) fail(DVR_E_INVALID_ARGUMENT, "tensor 'tf' must have at least two control points in TFLinear-mode");
+      break;
+    case DVR_TF_GAUSSIAN:
+      check_size(tf, "tf", 2, 6);
+      break;
+    case DVR_TF_GAUSSIAN_LOG:
+      fail(DVR_E_UNSUPPORTED, "TFGaussianLog is not supported by diffdvr_gb300");
+    default:
+      fail(DVR_E_INVALID_ARGUMENT, "unknown tf enum value");
+  }
+  if (tf.sizes[1] < 1) fail(DVR_E_INVALID_ARGUMENT, "tensor 'tf' must have at least one control point");
+  if (!real_storage_ok(tf.dtype))
+    fail(DVR_E_INVALID_ARGUMENT, std::string("tf must be of type float32 (or float16/bfloat16), but is ") +
+                                     dtype_name(tf.dtype));
+  p.tf = in_view(tf);
+  p.tf_storage = tf.dtype;
+  p.R = int(tf.sizes[1]);
+  p.C = int(tf.sizes[2]);
+  c.tf_mode = in.tf_mode;
+
+  if (in.blend_mode != DVR_BLEND_BEER_LAMBERT && in.blend_mode != DVR_BLEND_ALPHA)
+    fail(DVR_E_INVALID_ARGUMENT, "unknown blend enum value");
+  c.blend = in.blend_mode;
+  p.early_out = float(in.blending_early_out);
+  p.B = B;
+  return c;
+}
+
+// renderer::Renderer::checkOutput (renderer/renderer.cpp:367-391)
+void check_outputs(const DvrRendererOutputs& out, Checked& c, bool forward) {
+  RenderParams& p = c.p;
+  const DvrTensor& color = out.color;
+  const char* cname = forward ? "color" : "output_color";
+  check_dim(color, cname, 4);
+  check_device(color, cname, c.device);
+  check_size(color, cname, 0, p.B);
+  check_size(color, cname, 1, p.H);
+  check_size(color, cname, 2, p.W);
+  check_size(color, cname, 3, 4);
+  check_dtype(color, cname, DVR_FLOAT32);
+  const DvrTensor& term = out.termination_index;
+  check_dim(term, "terminationIndex", 3);
+  check_device(term, "terminationIndex", c.device);
+  check_size(term, "terminationIndex", 0, p.B);
+  check_size(term, "terminationIndex", 1, p.H);
+  check_size(term, "terminationIndex", 2, p.W);
+  check_dtype(term, "terminationIndex", DVR_INT32);
+  p.color = out_view(color, false);
+  p.term = out_view(term, false);
+  p.ckpt = OutView{};
+  p.ckpt_slots = 0;
+  p.ckpt_interval = out.checkpoint_interval > 0 ? out.checkpoint_interval : 32;
+  if (out.checkpoints.ndim >= 0 && out.checkpoints.data != nullptr) {
+    const DvrTensor& ck = out.checkpoints;
+    check_dim(ck, "checkpoints", 4);
+    check_device(ck, "checkpoints", c.device);
+    check_size(ck, "checkpoints", 0, p.B);
+    check_size(ck, "checkpoints", 1, p.H);
+    check_size(ck, "checkpoints", 2, p.W);
+    check_dtype(ck, "checkpoints", DVR_FLOAT32);
+    if (ck.sizes[3] < 1) fail(DVR_E_INVALID_ARGUMENT, "checkpoints must hold at least one slot per ray");
+    if (p.ckpt_interval < 1 || p.ckpt_interval > 64)
+      fail(DVR_E_INVALID_ARGUMENT, "checkpoint_interval must be in [1, 64]");
+    p.ckpt = out_view(ck, false);
+    p.ckpt_slots = int(ck.sizes[3]);
+  }
+}
+
+// checkAdjointOutput (renderer/renderer.cpp:265-365) plus the forward-output
+// and adj_color checks of renderAdjoint (renderer/renderer.cpp:670-717)
+AdjointParams check_adjoint(const DvrTensor& adj_color, const DvrAdjointOutputs& o, const Checked& c) {
+  const RenderParams& p = c.p;
+  AdjointParams a{};
+  check_dim(adj_color, "adj_color", 4);
+  check_device(adj_color, "adj_color", c.device);
+  check_size(adj_color, "adj_color", 0, p.B);
+  check_size(adj_color, "adj_color", 1, p.H);
+  check_size(adj_color, "adj_color", 2, p.W);
+  check_size(adj_color, "adj_color", 3, 4);
+  check_dtype(adj_color, "adj_color", DVR_FLOAT32);
+  a.adj_color = in_view(adj_color);
+  a.fwd_color = InView{p.color.p, {p.color.s[0], p.color.s[1], p.color.s[2], p.color.s[3]}, {0, 0, 0}, 0};
+  a.fwd_term = InView{p.term.p, {p.term.s[0], p.term.s[1], p.term.s[2], 0}, {0, 0, 0}, 0};
+
+  a.has_volume = o.has_volume_derivatives != 0;
+  if (a.has_volume) {
+    const DvrTensor& t = o.adj_volume;
+    check_dim(t, "adj_volume", 4);
+    check_device(t, "adj_volume", c.device);
+    check_batch(t, "adj_volume", p.B);
+    check_size(t, "adj_volume", 1, p.X);
+    check_size(t, "adj_volume", 2, p.Y);
+    check_size(t, "adj_volume", 3, p.Z);
+    check_dtype(t, "adj_volume", DVR_FLOAT32);
+    a.adj_volume = out_view(t, true);
+  }
+  a.has_stepsize = o.has_stepsize_derivatives != 0;
+  if (a.has_stepsize) {
+    const DvrTensor& t = o.adj_stepsize;
+    check_dim(t, "adj_stepSize", 3);
+    check_device(t, "adj_stepSize", c.device);
+    check_batch(t, "adj_stepSize", p.B);
+    check_batch(t, "adj_stepSize", p.H, 1);
+    check_batch(t, "adj_stepSize", p.W, 2);
+    check_dtype(t, "adj_stepSize", DVR_FLOAT32);
+    a.adj_step = out_view(t, true);
+    a.stepsize_broadcast = p.B != t.sizes[0] || p.H != t.sizes[1] || p.W != t.sizes[2];
+  }
+  a.has_camera = o.has_camera_derivatives != 0;
+  if (a.has_camera) {
+    const DvrTensor& ts = o.adj_camera_ray_start;
+    check_dim(ts, "adj_cameraRayStart", 4);
+    check_device(ts, "adj_cameraRayStart", c.device);
+    check_batch(ts, "adj_cameraRayStart", p.B);
+    check_size(ts, "adj_cameraRayStart", 1, p.H);
+    check_size(ts, "adj_cameraRayStart", 2, p.W);
+    check_size(ts, "adj_cameraRayStart", 3, 3);
+    check_dtype(ts, "adj_cameraRayStart", DVR_FLOAT32);
+    const DvrTensor& td = o.adj_camera_ray_dir;
+    check_dim(td, "adj_cameraRayDir", 4);
+    check_device(td, "adj_cameraRayDir", c.device);
+    check_batch(td, "adj_cameraRayDir", p.B);
+    check_size(td, "adj_cameraRayDir", 1, p.H);
+    check_size(td, "adj_cameraRayDir", 2, p.W);
+    check_size(td, "adj_cameraRayDir", 3, 3);
+    check_dtype(td, "adj_cameraRayDir", DVR_FLOAT32);
+    a.adj_start = out_view(ts, true);
+    a.adj_dir = out_view(td, true);
+    a.camera_broadcast = p.B != ts.sizes[0] || p.B != td.sizes[0];
+    if (p.camera_mode != DVR_CAMERA_RAY_START_DIR)
+      fail(DVR_E_INVALID_ARGUMENT, "camera derivatives require cameraMode == RayStartDir (per-pixel rays)");
+  }
+  a.has_tf = o.has_tf_derivatives != 0;
+  a.tf_delayed = o.tf_delayed_accumulation != 0;
+  if (a.has_tf) {
+    const DvrTensor& t = o.adj_tf;
+    check_dim(t, "adj_tf", 3);
+    check_device(t, "adj_tf", c.device);
+    check_batch(t, "adj_tf", p.B);
+    check_size(t, "adj_tf", 1, p.R);
+    check_size(t, "adj_tf", 2, p.C);
+    check_dtype(t, "adj_tf", DVR_FLOAT32);
+    a.adj_tf = out_view(t, true);
+  }
+  if (!a.has_volume && !a.has_stepsize && !a.has_camera && !a.has_tf)
+    fail(DVR_E_NO_GRADIENT, "At least one adjoint variable must be activated!");
+  return a;
+}
+
+void after_launch(cudaError_t e, cudaStream_t s, const char* what) {
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    fail(DVR_E_CUDA, std::string(what) + " launch failed: " + cudaGetErrorString(e));
+  }
+  if (g_sync.load()) {
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) fail(DVR_E_CUDA, std::string(what) + " failed: " + cudaGetErrorString(e));
+  }
+}
+
+bool use_plain(const Checked& c) {
+  if (g_family.load() == DVR_KERNELS_PLAIN) {
+    if (c.p.vol_storage != DVR_FLOAT32 || c.p.tf_storage != DVR_FLOAT32)
+      fail(DVR_E_UNSUPPORTED, "the plain kernel family renders float32 volumes and TFs only");
+    return true;
+  }
+  return false;
+}
+
+template <typename F>
+int guarded(F&& fn) {
+  try {
+    fn();
+    g_last_error.clear();
+    return DVR_OK;
+  } catch (const DvrError& e) {
+    g_last_error = e.what();
+    return e.code;
+  } catch (const std::exception& e) {
+    g_last_error = e.what();
+    return DVR_E_INVALID_ARGUMENT;
+  }
+}
+
+cudaError_t dispatch_forward(const Checked& c, bool plain, const LaunchInfo& li, cudaStream_t s) {
+  switch (c.tf_mode) {
+    case DVR_TF_IDENTITY:
+      return plain ? launch_plain_forward<0>(c.p, c.filter, c.blend, li, s)
+                   : launch_fast_forward<0>(c.p, c.filter, c.blend, li, s);
+    case DVR_TF_TEXTURE:
+      return plain ? launch_plain_forward<1>(c.p, c.filter, c.blend, li, s)
+                   : launch_fast_forward<1>(c.p, c.filter, c.blend, li, s);
+    case DVR_TF_LINEAR:
+      return plain ? launch_plain_forward<2>(c.p, c.filter, c.blend, li, s)
+                   : launch_fast_forward<2>(c.p, c.filter, c.blend, li, s);
+    default:
+      return plain ? launch_plain_forward<3>(c.p, c.filter, c.blend, li, s)
+                   : launch_fast_forward<3>(c.p, c.filter, c.blend, li, s);
+  }
+}
+
+cudaError_t dispatch_adjoint(const Checked& c, const AdjointParams& a, bool plain, const LaunchInfo& li,
+                             cudaStream_t s) {
+  switch (c.tf_mode) {
+    case DVR_TF_IDENTITY:
+      return plain ? launch_plain_adjoint<0>(c.p, a, c.filter, c.blend, li, s)
+                   : launch_fast_adjoint<0>(c.p, a, c.filter, c.blend, li, s);
+    case DVR_TF_TEXTURE:
+      return plain ? launch_plain_adjoint<1>(c.p, a, c.filter, c.blend, li, s)
+                   : launch_fast_adjoint<1>(c.p, a, c.filter, c.blend, li, s);
+    case DVR_TF_LINEAR:
+      return plain ? launch_plain_adjoint<2>(c.p, a, c.filter, c.blend, li, s)
+                   : launch_fast_adjoint<2>(c.p, a, c.filter, c.blend, li, s);
+    default:
+      return plain ? launch_plain_adjoint<3>(c.p, a, c.filter, c.blend, li, s)
+                   : launch_fast_adjoint<3>(c.p, a, c.filter, c.blend, li, s);
+  }
+}
+
+}  // namespace
+}  // namespace dvr
+
+using namespace dvr;
+
+extern "C" int dvr_render_forward(const DvrRendererInputs* inputs, const DvrRendererOutputs* outputs,
+                                  void* cuda_stream) {
+  return guarded([&] {
+    if (!inputs || !outputs) fail(DVR_E_INVALID_ARGUMENT, "inputs and outputs must not be NULL");
+    Checked c = check_inputs(*inputs);
+    check_outputs(*outputs, c, true);
+    DeviceGuard guard(c.device);
+    const LaunchInfo li = launch_info(c.device);
+    const bool plain = use_plain(c);
+    cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+    after_launch(dispatch_forward(c, plain, li, s), s, "forward");
+  });
+}
+
+extern "C" int dvr_render_adjoint(const DvrRendererInputs* inputs, const DvrRendererOutputs* outputs_from_forward,
+                                  const DvrTensor* adj_color, const DvrAdjointOutputs* adj_outputs,
+                                  void* cuda_stream) {
+  return guarded([&] {
+    if (!inputs || !outputs_from_forward || !adj_color || !adj_outputs)
+      fail(DVR_E_INVALID_ARGUMENT, "arguments must not be NULL");
+    Checked c = check_inputs(*inputs);
+    check_outputs(*outputs_from_forward, c, false);
+    const AdjointParams a = check_adjoint(*adj_color, *adj_outputs, c);
+    DeviceGuard guard(c.device);
+    const LaunchInfo li = launch_info(c.device);
+    const bool plain = use_plain(c);
+    cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+    after_launch(dispatch_adjoint(c, a, plain, li, s), s, "adjoint");
+  });
+}
+
+extern "C" int dvr_render_forward_batched(const DvrRendererInputs* inputs, const DvrRendererOutputs* outputs,
+                                          int32_t n, void* cuda_stream) {
+  return guarded([&] {
+    if (n < 0 || (n > 0 && (!inputs || !outputs))) fail(DVR_E_INVALID_ARGUMENT, "invalid instance list");
+    if (n == 0) return;
+    std::vector<Checked> cs(n);
+    for (int i = 0; i < n; ++i) {
+      cs[i] = check_inputs(inputs[i]);
+      check_outputs(outputs[i], cs[i], true);
+      if (i > 0 && (cs[i].filter != cs[0].filter || cs[i].tf_mode != cs[0].tf_mode || cs[i].blend != cs[0].blend ||
+                    cs[i].p.vol_storage != cs[0].p.vol_storage || cs[i].p.tf_storage != cs[0].p.tf_storage ||
+                    cs[i].device != cs[0].device))
+        fail(DVR_E_INVALID_ARGUMENT,
+             "all instances of a batched call must share filter, TF and blend modes, storage types and device");
+    }
+    DeviceGuard guard(cs[0].device);
+    const LaunchInfo li = launch_info(cs[0].device);
+    std::vector<RenderParams> ps(n);
+    for (int i = 0; i < n; ++i) ps[i] = cs[i].p;
+    cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+    after_launch(launch_batched_forward(ps.data(), n, cs[0].filter, cs[0].tf_mode, cs[0].blend, cs[0].device, li, s),
+                 s, "batched forward");
+  });
+}
+
+extern "C" int dvr_render_adjoint_batched(const DvrRendererInputs* inputs,
+                                          const DvrRendererOutputs* outputs_from_forward, const DvrTensor* adj_colors,
+                                          const DvrAdjointOutputs* adj_outputs, int32_t n, void* cuda_stream) {
+  return guarded([&] {
+    if (n < 0 || (n > 0 && (!inputs || !outputs_from_forward || !adj_colors || !adj_outputs)))
+      fail(DVR_E_INVALID_ARGUMENT, "invalid instance list");
+    if (n == 0) return;
+    std::vector<Checked> cs(n);
+    std::vector<AdjointParams> as(n);
+    for (int i = 0; i < n; ++i) {
+      cs[i] = check_inputs(inputs[i]);
+      check_outputs(outputs_from_forward[i], cs[i], false);
+      as[i] = check_adjoint(adj_colors[i], adj_outputs[i], cs[i]);
+      if (i > 0 && (cs[i].filter != cs[0].filter || cs[i].tf_mode != cs[0].tf_mode || cs[i].blend != cs[0].blend ||
+                    cs[i].p.vol_storage != cs[0].p.vol_storage || cs[i].p.tf_storage != cs[0].p.tf_storage ||
+                    cs[i].device != cs[0].device || as[i].has_volume != as[0].has_volume ||
+                    as[i].has_tf != as[0].has_tf))
+        fail(DVR_E_INVALID_ARGUMENT,
+             "all instances of a batched call must share modes, storage types, device and gradient selection");
+    }
+    DeviceGuard guard(cs[0].device);
+    const LaunchInfo li = launch_info(cs[0].device);
+    std::vector<RenderParams> ps(n);
+    for (int i = 0; i < n; ++i) ps[i] = cs[i].p;
+    cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+    after_launch(launch_batched_adjoint(ps.data(), as.data(), n, cs[0].filter, cs[0].tf_mode, cs[0].blend,
+                                        cs[0].device, li, s),
+                 s, "batched adjoint");
+  });
+}
+
+extern "C" int64_t dvr_checkpoint_slots(double max_ray_length, double min_step_size, int32_t checkpoint_interval) {
+  const int K = checkpoint_interval > 0 ? checkpoint_interval : 32;
+  if (!(max_ray_length >= 0) || !(min_step_size > 0) || K > 64) {
+    g_last_error = "dvr_checkpoint_slots: need max_ray_length >= 0, min_step_size > 0 and interval <= 64";
+    return DVR_E_INVALID_ARGUMENT;
+  }
+  // samples k = 0..n-1 with t = tmin + k*step <= tmax: n <= floor(len/step) + 1
+  const double n = std::floor(max_ray_length / min_step_size) + 2.0;
+  const double slots = std::ceil(n / K);
+  return slots < 1 ? 1 : int64_t(slots);
+}
+
+extern "C" const char* dvr_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" int dvr_set_kernel_family(int32_t family) {
+  if (family != DVR_KERNELS_PLAIN && family != DVR_KERNELS_OPTIMIZED) {
+    g_last_error = "unknown kernel family";
+    return DVR_E_INVALID_ARGUMENT;
+  }
+  return g_family.exchange(family);
+}
+extern "C" int dvr_get_kernel_family(void) { return g_family.load(); }
+extern "C" int dvr_set_sync_mode(int32_t sync) { return g_sync.exchange(sync ? 1 : 0); }
+extern "C" int dvr_get_sync_mode(void) { return g_sync.load(); }
+extern "C" int dvr_abi_version(void) { return DVR_ABI_VERSION; }

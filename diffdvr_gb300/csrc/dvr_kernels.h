@@ -1,0 +1,29 @@
+// Launchers of the ray-marcher kernel families (host-callable, no torch).
+// Each TF mode's kernels live in their own translation unit so the build
+// compiles them in parallel; dvr_host.cu dispatches on the TF mode.
+#pragma once
+#include <cuda_runtime.h>
+#include "dvr_params.h"
+
+namespace dvr {
+
+struct LaunchInfo {
+  int num_sms;
+  int max_smem_optin;  // cudaDevAttrMaxSharedMemoryPerBlockOptin
+};
+
+// Plain family (reference semantics).
+template <int TF>
+cudaError_t launch_plain_forward(const RenderParams& p, int filter, int blend, const LaunchInfo& li, cudaStream_t s);
+template <int TF>
+cudaError_t launch_plain_adjoint(const RenderParams& p, const AdjointParams& a, int filter, int blend,
+                                 const LaunchInfo& li, cudaStream_t s);
+
+// Optimized family.
+template <int TF>
+cudaError_t launch_fast_forward(const RenderParams& p, int filter, int blend, const LaunchInfo& li, cudaStream_t s);
+template <int TF>
+cudaError_t launch_fast_adjoint(const RenderParams& p, const AdjointParams& a, int filter, int blend,
+                                const LaunchInfo& li, cudaStream_t s);
+
+}  // namespace dvr

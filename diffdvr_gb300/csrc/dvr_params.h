@@ -1,0 +1,66 @@
+// Kernel-side parameter blocks of the ray marcher (host and device).
+//
+// The host layer (dvr_host.cu) validates the C-ABI descriptors and flattens
+// them into these PODs: element strides with the broadcast rule already
+// applied (a dimension of size 1 gets stride 0, as the reference's
+// BroadcastingTensorAccessor32 does, renderer/renderer_tensor.cuh:140-144),
+// and scalar settings carried by value instead of as temporary tensors.
+#pragma once
+#include <stdint.h>
+
+namespace dvr {
+
+enum StorageType : int32_t { kF32 = 0, kF16 = 2, kBF16 = 3 };
+
+// A (B) * ... real-valued input.  p == nullptr means "use val" (a setting
+// given by value, broadcast over everything).
+struct InView {
+  const void* p;
+  int64_t s[4];
+  float val[3];
+  int32_t pad_;
+};
+
+struct OutView {
+  void* p;
+  int64_t s[4];
+};
+
+struct RenderParams {
+  int32_t W, H, B;              // screen size and resolved batch
+  int32_t camera_mode;          // 0 rays, 1 inverse view matrix, 2 reference frame
+  int32_t X, Y, Z;              // volume resolution
+  int32_t R, C;                 // TF control points and channels
+  int32_t vol_storage, tf_storage;
+  float fov_y;                  // camera_mode 2
+  float early_out;              // blendingEarlyOut
+  int32_t pad0_;
+  float cam_value[16];          // camera_mode 1 given by value: rows of the 4x4 matrix
+  InView volume;                // [b][x][y][z]
+  InView box_min, box_size;     // [b][i]
+  InView ray_start, ray_dir;    // [b][y][x][i]
+  InView cam;                   // [b][r][c]
+  InView step;                  // [b][y][x]
+  InView tf;                    // [b][r][c]
+  OutView color;                // [b][y][x][c]
+  OutView term;                 // [b][y][x] int32
+  // checkpointed adjoint (optimized kernels); ckpt.p == nullptr when absent
+  OutView ckpt;                 // [b][y][x][j] float, transmittance before sample (j+1)*K
+  int32_t ckpt_slots;           // C slots per ray
+  int32_t ckpt_interval;        // K
+};
+
+struct AdjointParams {
+  InView fwd_color;             // [b][y][x][c]
+  InView fwd_term;              // [b][y][x] int32 (read as int)
+  InView adj_color;             // [b][y][x][c]
+  int32_t has_volume, has_stepsize, has_camera, has_tf;
+  int32_t stepsize_broadcast, camera_broadcast, tf_delayed;
+  int32_t pad_;
+  OutView adj_volume;           // [b][x][y][z]  (broadcast strides allowed)
+  OutView adj_step;             // [b][y][x]
+  OutView adj_start, adj_dir;   // [b][y][x][i]
+  OutView adj_tf;               // [b][r][c]
+};
+
+}  // namespace dvr

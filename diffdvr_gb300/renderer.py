@@ -1,0 +1,202 @@
+"""Drop-in for the reference's ``diffdvr.Renderer`` module and its autograd
+function (pytests/diffdvr/renderer.py:61-359), adjoint method.
+
+``forward`` renders with ``pyrenderer.Renderer.render_forward`` and saves the
+outputs; ``backward`` zero-initialises the enabled gradients and calls
+``render_adjoint``.  When gradients are required, the forward pass also
+fills a transmittance-checkpoint buffer so the adjoint re-marches segments
+instead of inverting the blend.
+
+The reference's forward-mode differentiation (``gradient_method="forward"``)
+is not part of this renderer; requesting it raises ``NotImplementedError``.
+"""
+from __future__ import annotations
+
+import time
+from typing import Optional
+
+import torch
+import torch.nn as nn
+
+from . import pyrenderer
+from .camera import Camera
+
+
+class ProfileRenderer:
+    def __init__(self):
+        self.forward_ms = 0.0
+        self.forward_bytes = 0
+        self.backward_ms = 0.0
+
+
+class _Timer:
+    def __init__(self, enable: bool):
+        self._enable = enable
+        self._elapsed_ms = None
+
+    def elapsed_ms(self):
+        return self._elapsed_ms
+
+    def __enter__(self):
+        if self._enable:
+            self._t = pyrenderer.GpuTimer()
+            torch.cuda.synchronize()
+            self._t.start()
+        return self
+
+    def __exit__(self, *exc):
+        if self._enable:
+            self._t.stop()
+            self._elapsed_ms = self._t.elapsed_ms()
+
+
+def _size_of(*ts) -> int:
+    return sum(t.element_size() * t.numel() for t in ts if t is not None)
+
+
+def _implies(a, b) -> bool:
+    return (not a) or b
+
+
+class _RendererFunction(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, camera_matrix, camera_ray_start, camera_ray_dir, tf, volume,
+                inputs: pyrenderer.RendererInputs, fov_y_radians,
+                optimize_camera, optimize_tf, optimize_volume, tf_delayed_accumulation,
+                checkpoint_interval, profiling: Optional[ProfileRenderer]):
+        ctx.inputs = inputs
+        ctx.fov_y_radians = fov_y_radians
+        ctx.optimize = (optimize_camera, optimize_tf, optimize_volume)
+        ctx.tf_delayed_accumulation = tf_delayed_accumulation
+        ctx.profiling = profiling
+        assert _implies(optimize_camera, inputs.camera_mode == pyrenderer.CameraMode.RayStartDir)
+        if inputs.camera_mode == pyrenderer.CameraMode.RayStartDir:
+            inputs.camera = pyrenderer.CameraPerPixelRays(camera_ray_start, camera_ray_dir)
+        else:
+            inputs.camera = pyrenderer.CameraReferenceFrame(camera_matrix, fov_y_radians)
+        inputs.tf = tf
+        inputs.volume = volume
+
+        B = max([(1 if t is None else t.shape[0]) for t in (camera_matrix, camera_ray_start, camera_ray_dir, tf,
+                                                            volume)])
+        W, H = inputs.screen_size.x, inputs.screen_size.y
+        color = torch.empty(B, H, W, 4, dtype=torch.float32, device=volume.device)
+        term = torch.empty(B, H, W, dtype=torch.int32, device=volume.device)
+        needs_grad = any(ctx.needs_input_grad[:5])
+        ckpt = None
+        if needs_grad and checkpoint_interval > 0:
+            slots = pyrenderer.Renderer.checkpoint_slots(inputs, checkpoint_interval)
+            ckpt = torch.empty(B, H, W, slots, dtype=torch.float32, device=volume.device)
+        outputs = pyrenderer.RendererOutputs(color, term, ckpt, checkpoint_interval)
+        with _Timer(profiling is not None) as timer:
+            pyrenderer.Renderer.render_forward(inputs, outputs)
+        if profiling is not None:
+            profiling.forward_ms += timer.elapsed_ms()
+            profiling.forward_bytes += _size_of(camera_matrix, camera_ray_start, camera_ray_dir, tf, volume, color,
+                                                term, ckpt)
+        ctx.save_for_backward(camera_matrix, camera_ray_start, camera_ray_dir, tf, volume, color, term, ckpt)
+        ctx.checkpoint_interval = checkpoint_interval
+        return color
+
+    @staticmethod
+    def backward(ctx, grad_color):
+        camera_matrix, ray_start, ray_dir, tf, volume, color, term, ckpt = ctx.saved_tensors
+        optimize_camera, optimize_tf, optimize_volume = ctx.optimize
+        inputs = ctx.inputs
+        if inputs.camera_mode == pyrenderer.CameraMode.RayStartDir:
+            inputs.camera = pyrenderer.CameraPerPixelRays(ray_start, ray_dir)
+        else:
+            inputs.camera = pyrenderer.CameraReferenceFrame(camera_matrix, ctx.fov_y_radians)
+        inputs.tf = tf
+        inputs.volume = volume
+        g_start = g_dir = g_tf = g_volume = None
+        adj = pyrenderer.AdjointOutputs()
+        if optimize_camera:
+            g_start = torch.zeros_like(ray_start)
+            g_dir = torch.zeros_like(ray_dir)
+            adj.has_camera_derivatives = True
+            adj.adj_camera_ray_start = g_start
+            adj.adj_camera_ray_dir = g_dir
+        if optimize_tf:
+            g_tf = torch.zeros(tf.shape, dtype=torch.float32, device=tf.device)
+            adj.has_tf_derivatives = True
+            adj.tf_delayed_accumulation = ctx.tf_delayed_accumulation
+            adj.adj_tf = g_tf
+        if optimize_volume:
+            g_volume = torch.zeros(volume.shape, dtype=torch.float32, device=volume.device)
+            adj.has_volume_derivatives = True
+            adj.adj_volume = g_volume
+        fwd = pyrenderer.RendererOutputs(color, term, ckpt, ctx.checkpoint_interval)
+        with _Timer(ctx.profiling is not None) as timer:
+            pyrenderer.Renderer.render_adjoint(inputs, fwd, grad_color.contiguous().float(), adj)
+        if ctx.profiling is not None:
+            ctx.profiling.backward_ms += timer.elapsed_ms()
+        if g_tf is not None and tf.dtype != torch.float32:
+            g_tf = g_tf.to(tf.dtype)
+        if g_volume is not None and volume.dtype != torch.float32:
+            g_volume = g_volume.to(volume.dtype)
+        return None, g_start, g_dir, g_tf, g_volume, None, None, None, None, None, None, None, None
+
+
+class Renderer(nn.Module):
+    """Mirrors diffdvr.Renderer (pytests/diffdvr/renderer.py:264-359)."""
+
+    def __init__(self, settings: Optional[pyrenderer.RendererInputs] = None, optimize_camera=False,
+                 optimize_tf=False, optimize_volume=False, gradient_method="adjoint",
+                 forward_delayed_gradients=False, tf_delayed_accumulation=True, checkpoint_interval: int = 32):
+        super().__init__()
+        self._settings = settings if settings is not None else pyrenderer.RendererInputs()
+        self._optimize_camera = optimize_camera
+        self._optimize_tf = optimize_tf
+        self._optimize_volume = optimize_volume
+        self._has_parameters_to_optimize = optimize_camera or optimize_tf or optimize_volume
+        assert gradient_method in ["adjoint", "forward"]
+        if gradient_method != "adjoint":
+            raise NotImplementedError("forward-mode differentiation is not provided by diffdvr_gb300; "
+                                      "use gradient_method='adjoint'")
+        self._tf_delayed_accumulation = tf_delayed_accumulation
+        self._checkpoint_interval = int(checkpoint_interval)
+        self._renderer_function = _RendererFunction.apply
+
+    def get_settings(self):
+        return self._settings
+
+    def set_settings(self, settings: pyrenderer.RendererInputs):
+        assert settings is not None
+        self._settings = settings
+
+    settings = property(get_settings, set_settings)
+
+    def train(self, mode: bool = True):
+        if mode is True and not self._has_parameters_to_optimize:
+            raise ValueError("requested training mode, but no parameters were specified to be optimized")
+        return super().train(mode)
+
+    def forward(self, *, camera: torch.Tensor = None, fov_y_radians: float = None, tf: torch.Tensor = None,
+                volume: torch.Tensor = None, profiling: ProfileRenderer = None):
+        """Renders the volume; returns the B*H*W*4 colour image."""
+        assert _implies(self._optimize_camera, camera is not None)
+        assert _implies(self._optimize_camera, fov_y_radians is not None)
+        assert _implies(self._optimize_tf, tf is not None)
+        assert _implies(self._optimize_volume, volume is not None)
+        inputs = self._settings.clone()
+        camera_matrix = ray_start = ray_dir = None
+        if camera is not None:
+            if self._optimize_camera:
+                ray_start, ray_dir = Camera.generate_rays(camera, fov_y_radians, self._settings.screen_size.x,
+                                                          self._settings.screen_size.y)
+                inputs.camera_mode = pyrenderer.CameraMode.RayStartDir
+            else:
+                camera_matrix = camera
+                inputs.camera_mode = pyrenderer.CameraMode.ReferenceFrame
+        elif isinstance(inputs.camera, pyrenderer.CameraPerPixelRays):
+            ray_start, ray_dir = inputs.camera.ray_start, inputs.camera.ray_dir
+        elif isinstance(inputs.camera, pyrenderer.CameraReferenceFrame):
+            camera_matrix, fov_y_radians = inputs.camera.viewport, inputs.camera.fov_y_radians
+        if tf is None:
+            tf = inputs.tf
+        if volume is None:
+            volume = inputs.volume
+        return self._renderer_function(camera_matrix, ray_start, ray_dir, tf, volume, inputs, fov_y_radians,
+                                       self._optimize_camera, self._optimize_tf, self._optimize_volume,
+                                       self._tf_delayed_accumulation, self._checkpoint_interval, profiling)

@@ -1,0 +1,199 @@
+/*
+ * diffdvr_gb300 — C ABI of the GB300 (sm_103a) differentiable volume ray marcher.
+ *
+ * Plain C: raw pointers, sizes and element strides; no torch types.  Every
+ * entry point returns DVR_OK (0) or a negative DVR_E* code and never throws;
+ * the message of the last failure on the calling thread is returned by
+ * dvr_last_error().  Launches are asynchronous on the given CUDA stream
+ * (NULL = legacy default stream), like the reference, which launches on the
+ * PyTorch current stream (renderer/renderer_cuda.cpp:105, :304).
+ *
+ * Layout contract (renderer/renderer_settings.cuh:8-45); a bracketed leading
+ * dimension may be 1 and is then broadcast over the batch:
+ *   volume            (B) X Y Z            density
+ *   box_min, box_size (B) 3
+ *   camera            (B) H W 3 ray start + (B) H W 3 ray direction, or
+ *                     (B) 4 4 inverse view-projection, or
+ *                     (B) 3 3 reference frame (eye, right, up) + fovY
+ *   step_size         (B) (H) (W)
+ *   tf                (B) R C, C = 2 identity, 4 texture, 5 linear, 6 Gaussian
+ *   color             B H W 4              output (r, g, b, alpha)
+ *   termination_index B H W int32          output
+ * Gradient outputs are accumulated with atomics and must be zero-initialised
+ * by the caller (renderer/renderer_settings.cuh:227-229).
+ *
+ * Storage types: every real-valued tensor is float32, except that the volume
+ * and the TF may also be float16 or bfloat16 (sampled and blended in FP32);
+ * gradients are always float32.  All tensors must live on the same CUDA device.
+ */
+#ifndef DIFFDVR_GB300_H
+#define DIFFDVR_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DVR_ABI_VERSION 1
+
+/* ---- status codes ---- */
+#define DVR_OK 0
+#define DVR_E_INVALID_ARGUMENT (-1) /* a shape, dtype, device or mode check failed (TORCH_CHECK in the reference) */
+#define DVR_E_NO_GRADIENT (-2)      /* adjoint with no gradient enabled (renderer/renderer.cpp:712-717) */
+#define DVR_E_UNSUPPORTED (-3)      /* mode or dtype this build does not implement */
+#define DVR_E_CUDA (-4)             /* a CUDA runtime call or launch failed */
+
+/* ---- enums: values equal to the reference's (renderer/renderer_settings.cuh:81-146) ---- */
+enum DvrVolumeFilterMode { DVR_FILTER_NEAREST = 0, DVR_FILTER_TRILINEAR = 1, DVR_FILTER_PRESHADED = 3 };
+enum DvrCameraMode { DVR_CAMERA_RAY_START_DIR = 0, DVR_CAMERA_INVERSE_VIEW_MATRIX = 1, DVR_CAMERA_REFERENCE_FRAME = 2 };
+enum DvrTFMode {
+  DVR_TF_IDENTITY = 0, DVR_TF_TEXTURE = 1, DVR_TF_LINEAR = 2, DVR_TF_GAUSSIAN = 3,
+  DVR_TF_PRESHADED = 5, DVR_TF_GAUSSIAN_LOG = 6
+};
+enum DvrBlendMode { DVR_BLEND_BEER_LAMBERT = 0, DVR_BLEND_ALPHA = 1 };
+
+enum DvrDType { DVR_FLOAT32 = 0, DVR_FLOAT64 = 1, DVR_FLOAT16 = 2, DVR_BFLOAT16 = 3, DVR_INT32 = 4 };
+enum DvrDeviceType { DVR_DEVICE_CPU = 0, DVR_DEVICE_CUDA = 1 };
+
+/* Kernel family used by dvr_render_forward / dvr_render_adjoint.
+ *  DVR_KERNELS_PLAIN:     one thread per ray, reference semantics throughout
+ *                         (adjoint recovers the accumulator by inverting the
+ *                         blend, renderer/renderer_blending.cuh:75-77).
+ *  DVR_KERNELS_OPTIMIZED: tiled ray order, FP16/BF16 volume storage, TF in
+ *                         shared memory, pre-aggregated gradient scatters and,
+ *                         when the forward pass was given a checkpoint buffer,
+ *                         a checkpointed adjoint that recomputes each segment
+ *                         instead of inverting the blend.  Default. */
+enum DvrKernelFamily { DVR_KERNELS_PLAIN = 0, DVR_KERNELS_OPTIMIZED = 1 };
+
+/* A strided tensor view.  ndim < 0 marks an absent (undefined) tensor.
+ * strides are in elements. */
+typedef struct DvrTensor {
+  void* data;
+  int32_t ndim;
+  int32_t dtype;         /* DvrDType */
+  int32_t device_type;   /* DvrDeviceType */
+  int32_t device_index;
+  int64_t sizes[5];
+  int64_t strides[5];
+} DvrTensor;
+
+/* Which alternative a host-side variant field holds. */
+enum DvrValueKind { DVR_KIND_TENSOR = 0, DVR_KIND_VALUE = 1 };
+enum DvrCameraKind {
+  DVR_CAMERA_PER_PIXEL_RAYS = 0,           /* CameraPerPixelRays{ray_start, ray_dir} */
+  DVR_CAMERA_INVERSE_VIEW_TENSOR = 1,      /* B*4*4 tensor */
+  DVR_CAMERA_INVERSE_VIEW_VALUE = 2,       /* one 4x4 matrix by value (glm::mat4) */
+  DVR_CAMERA_REFERENCE_FRAME_KIND = 3      /* CameraReferenceFrame{viewport B*3*3, fovY} */
+};
+
+/* Mirrors renderer::RendererInputsHost (renderer/renderer.h:20-64).  Each
+ * std::variant of the reference becomes a kind tag plus both alternatives. */
+typedef struct DvrRendererInputs {
+  int32_t screen_width;          /* screenSize.x = W */
+  int32_t screen_height;         /* screenSize.y = H */
+  int32_t volume_filter_mode;    /* DvrVolumeFilterMode */
+  int32_t camera_mode;           /* DvrCameraMode */
+  int32_t tf_mode;               /* DvrTFMode */
+  int32_t blend_mode;            /* DvrBlendMode */
+  DvrTensor volume;
+  int32_t box_min_kind;          /* DvrValueKind */
+  int32_t box_size_kind;
+  DvrTensor box_min;
+  DvrTensor box_size;
+  double box_min_value[3];
+  double box_size_value[3];
+  int32_t camera_kind;           /* DvrCameraKind */
+  int32_t step_size_kind;        /* DvrValueKind */
+  DvrTensor camera_ray_start;
+  DvrTensor camera_ray_dir;
+  DvrTensor camera_matrix;       /* B*4*4 or B*3*3 */
+  float camera_matrix_value[16]; /* rows of the 4x4 matrix as the kernel reads them
+                                    (= the column-major storage of a glm::mat4) */
+  double camera_fov_y_radians;
+  DvrTensor step_size;
+  double step_size_value;
+  DvrTensor tf;
+  double blending_early_out;     /* default 1 - 1e-5 */
+} DvrRendererInputs;
+
+/* Mirrors renderer::RendererOutputsHost (renderer/renderer.h:67-71), plus an
+ * optional transmittance-checkpoint buffer (B*H*W*C float32, ndim < 0 when
+ * absent) that the forward pass fills every `checkpoint_interval` samples for
+ * the optimized adjoint.  C >= ceil(max samples per ray / interval) - 1. */
+typedef struct DvrRendererOutputs {
+  DvrTensor color;
+  DvrTensor termination_index;
+  DvrTensor checkpoints;
+  int32_t checkpoint_interval;   /* samples between checkpoints; 0 = default (32) */
+  int32_t pad_;
+} DvrRendererOutputs;
+
+/* Mirrors renderer::AdjointOutputsHost (renderer/renderer.h:95-111). */
+typedef struct DvrAdjointOutputs {
+  int32_t has_volume_derivatives;
+  int32_t has_stepsize_derivatives;
+  int32_t has_camera_derivatives;
+  int32_t has_tf_derivatives;
+  int32_t tf_delayed_accumulation;
+  int32_t pad_;
+  DvrTensor adj_volume;          /* (B) X Y Z */
+  DvrTensor adj_stepsize;        /* (B) (H) (W) */
+  DvrTensor adj_camera_ray_start;/* (B) H W 3 */
+  DvrTensor adj_camera_ray_dir;  /* (B) H W 3 */
+  DvrTensor adj_tf;              /* (B) R C */
+} DvrAdjointOutputs;
+
+/* Forward rendering without gradients.
+ * Replaces renderer::Renderer::renderForward (renderer/renderer.h:159-161,
+ * renderer/renderer.cpp:393-417). */
+int dvr_render_forward(const DvrRendererInputs* inputs, const DvrRendererOutputs* outputs, void* cuda_stream);
+
+/* Adjoint (backward) rendering: traces adj_color (B*H*W*4) back through the
+ * march and accumulates into the enabled gradient outputs.
+ * Replaces renderer::Renderer::renderAdjoint (renderer/renderer.h:264-268,
+ * renderer/renderer.cpp:660-742). */
+int dvr_render_adjoint(const DvrRendererInputs* inputs, const DvrRendererOutputs* outputs_from_forward,
+                       const DvrTensor* adj_color, const DvrAdjointOutputs* adj_outputs, void* cuda_stream);
+
+/* Batched rendering of n independent instances, each with its own volume
+ * size, image size, camera and TF, in ONE persistent launch over a work list
+ * of (instance, view, tile) items.  All instances share the filter, TF and
+ * blend modes and the volume storage dtype.  Extends the reference, whose
+ * batches must share the volume and image sizes (renderer/renderer.cpp:59-70).
+ * The per-instance descriptors are copied to a device workspace owned by the
+ * library (grown on demand, reused across calls) on the same stream. */
+int dvr_render_forward_batched(const DvrRendererInputs* inputs, const DvrRendererOutputs* outputs, int32_t n,
+                               void* cuda_stream);
+int dvr_render_adjoint_batched(const DvrRendererInputs* inputs, const DvrRendererOutputs* outputs_from_forward,
+                               const DvrTensor* adj_colors, const DvrAdjointOutputs* adj_outputs, int32_t n,
+                               void* cuda_stream);
+
+/* Number of checkpoint slots per ray (the C of DvrRendererOutputs.checkpoints)
+ * for rays of at most max_ray_length world units inside the box (the box
+ * diagonal bounds it) marched with steps of at least min_step_size, at the
+ * given interval (0 = default).  Host-only; returns a negative DVR_E* code for
+ * invalid arguments. */
+int64_t dvr_checkpoint_slots(double max_ray_length, double min_step_size, int32_t checkpoint_interval);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* dvr_last_error(void);
+
+/* Kernel family selection (process-wide).  Returns the previous value. */
+int dvr_set_kernel_family(int32_t family);
+int dvr_get_kernel_family(void);
+
+/* In sync mode every launch is followed by cudaStreamSynchronize and a launch
+ * error check, for debugging (renderer::Renderer::setCudaSyncMode,
+ * renderer/renderer.h:147-149).  Returns the previous value. */
+int dvr_set_sync_mode(int32_t sync);
+int dvr_get_sync_mode(void);
+
+/* ABI version of the loaded library (DVR_ABI_VERSION). */
+int dvr_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DIFFDVR_GB300_H */

@@ -1,0 +1,83 @@
+/*
+ * Oracle interface — TEST INFRASTRUCTURE ONLY.
+ *
+ * CPU restatement of DiffDVR's forward and adjoint volume ray marcher, used
+ * as the checker for the CUDA kernels of diffdvr_gb300.  Nothing in the
+ * product links, imports or executes code from this directory; only tests/,
+ * __graft_entry__.smoke() and bench.py's CPU-baseline leg do.
+ *
+ * Two libraries implement this interface:
+ *   libdvr_oracle_{f32,f64}.so  our plain-C restatement (dvr_oracle.c), builds
+ *                               anywhere (x86 container and the Arm GPU host);
+ *   _ref/libdvr_ref_{f32,f64}.so  the reference's own DvrKernel*Host templates
+ *                               compiled from its headers (ref_harness.cpp),
+ *                               only where the reference sources are present.
+ * Both take identical arguments so the Python wrapper (oracle.py) can call
+ * either one and the tests can pin the restatement to the reference.
+ *
+ * All real-valued buffers hold `real_t` = float (f32 build) or double (f64
+ * build).  Tensors follow the reference memory layout
+ * (renderer/renderer_settings.cuh:8-45); a dimension of size 1 is broadcast
+ * (stride treated as 0), as BroadcastingTensorAccessor32 does
+ * (renderer/renderer_tensor.cuh:140-144).
+ */
+#ifndef DVR_ORACLE_H
+#define DVR_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct OracleTensor {
+  void* data;          /* real_t* (or int32_t* for termination indices) */
+  int32_t ndim;
+  int32_t pad_;
+  int64_t sizes[5];
+  int64_t strides[5];  /* in elements */
+} OracleTensor;
+
+/* Enum values are those of renderer/renderer_settings.cuh:81-146. */
+typedef struct OracleInputs {
+  int32_t width, height;
+  int32_t filter_mode;   /* 0 nearest, 1 trilinear */
+  int32_t camera_mode;   /* 0 ray start/dir, 1 inverse view matrix, 2 reference frame */
+  int32_t tf_mode;       /* 0 identity, 1 texture, 2 linear, 3 gaussian */
+  int32_t blend_mode;    /* 0 Beer-Lambert, 1 alpha */
+  OracleTensor volume;        /* (B) X Y Z */
+  OracleTensor box_min;       /* (B) 3 */
+  OracleTensor box_size;      /* (B) 3 */
+  OracleTensor ray_start;     /* (B) H W 3   (camera_mode 0) */
+  OracleTensor ray_dir;       /* (B) H W 3   (camera_mode 0) */
+  OracleTensor camera_matrix; /* (B) 4 4 (mode 1) or (B) 3 3 (mode 2) */
+  double fov_y_radians;       /* camera_mode 2 */
+  OracleTensor step_size;     /* (B) (H) (W) */
+  OracleTensor tf;            /* (B) R C */
+  double blending_early_out;
+  int32_t batch;              /* resolved broadcast batch size B */
+  int32_t pad_;
+} OracleInputs;
+
+typedef struct OracleAdjointOutputs {
+  int32_t has_volume, has_stepsize, has_camera, has_tf;
+  int32_t stepsize_broadcast, camera_broadcast;
+  OracleTensor adj_volume;     /* (B) X Y Z */
+  OracleTensor adj_stepsize;   /* (B) (H) (W) */
+  OracleTensor adj_ray_start;  /* (B) H W 3 */
+  OracleTensor adj_ray_dir;    /* (B) H W 3 */
+  OracleTensor adj_tf;         /* (B) R C */
+} OracleAdjointOutputs;
+
+/* Returns 0 on success, nonzero for an unsupported mode combination. */
+int oracle_forward(const OracleInputs* in, OracleTensor* color, OracleTensor* termination);
+int oracle_adjoint(const OracleInputs* in, const OracleTensor* color,
+                   const OracleTensor* termination, const OracleTensor* adj_color,
+                   OracleAdjointOutputs* out);
+/* Size of real_t in this build (4 or 8). */
+int oracle_real_size(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

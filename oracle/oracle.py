@@ -1,0 +1,250 @@
+"""Oracle wrapper — TEST INFRASTRUCTURE ONLY.
+
+ctypes front end for the CPU ray-marcher oracle libraries declared in
+``oracle/dvr_oracle.h``:
+
+* ``kind="port"``: our plain-C restatement (``oracle/_build/libdvr_oracle_*.so``),
+  built on any machine by ``build()`` below;
+* ``kind="reference"``: the reference's own CPU templates
+  (``oracle/_ref/libdvr_ref_*.so``), built only where the reference sources are
+  present.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg
+use this module; the ``diffdvr_gb300`` package never imports it.
+
+Inputs are numpy arrays in the reference layout (renderer/renderer_settings.cuh:8-45):
+volume (B)XYZ, box_min/box_size (B)3, ray_start/ray_dir (B)HW3, camera_matrix
+(B)44 or (B)33, step_size (B)(H)(W), tf (B)RC.  Size-1 leading dimensions
+broadcast, as in the reference.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from dataclasses import dataclass, field
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+REF_DIR = os.path.join(HERE, "_ref")
+REFERENCE_SOURCES = "/root/reference/renderer"
+
+
+class OracleTensor(ctypes.Structure):
+    _fields_ = [
+        ("data", ctypes.c_void_p),
+        ("ndim", ctypes.c_int32),
+        ("pad_", ctypes.c_int32),
+        ("sizes", ctypes.c_int64 * 5),
+        ("strides", ctypes.c_int64 * 5),
+    ]
+
+
+class OracleInputs(ctypes.Structure):
+    _fields_ = [
+        ("width", ctypes.c_int32), ("height", ctypes.c_int32),
+        ("filter_mode", ctypes.c_int32), ("camera_mode", ctypes.c_int32),
+        ("tf_mode", ctypes.c_int32), ("blend_mode", ctypes.c_int32),
+        ("volume", OracleTensor), ("box_min", OracleTensor), ("box_size", OracleTensor),
+        ("ray_start", OracleTensor), ("ray_dir", OracleTensor), ("camera_matrix", OracleTensor),
+        ("fov_y_radians", ctypes.c_double), ("step_size", OracleTensor), ("tf", OracleTensor),
+        ("blending_early_out", ctypes.c_double), ("batch", ctypes.c_int32), ("pad_", ctypes.c_int32),
+    ]
+
+
+class OracleAdjointOutputs(ctypes.Structure):
+    _fields_ = [
+        ("has_volume", ctypes.c_int32), ("has_stepsize", ctypes.c_int32),
+        ("has_camera", ctypes.c_int32), ("has_tf", ctypes.c_int32),
+        ("stepsize_broadcast", ctypes.c_int32), ("camera_broadcast", ctypes.c_int32),
+        ("adj_volume", OracleTensor), ("adj_stepsize", OracleTensor),
+        ("adj_ray_start", OracleTensor), ("adj_ray_dir", OracleTensor), ("adj_tf", OracleTensor),
+    ]
+
+
+def build(reference: bool = True, quiet: bool = True) -> None:
+    """Builds the port libraries (and the reference harness when its sources exist)."""
+    out = subprocess.DEVNULL if quiet else None
+    subprocess.run(["make", "-C", HERE, "-j2", "all"], check=True, stdout=out)
+    if reference and os.path.isdir(REFERENCE_SOURCES):
+        subprocess.run(["make", "-C", HERE, "-j2", "ref", f"REF_DIR={REFERENCE_SOURCES}"],
+                       check=True, stdout=out)
+
+
+def reference_available() -> bool:
+    return os.path.exists(os.path.join(REF_DIR, "libdvr_ref_f32.so"))
+
+
+_LIBS: dict = {}
+
+
+def load(kind: str = "port", precision: str = "f64") -> ctypes.CDLL:
+    key = (kind, precision)
+    if key not in _LIBS:
+        if kind == "port":
+            path = os.path.join(BUILD_DIR, f"libdvr_oracle_{precision}.so")
+        elif kind == "reference":
+            path = os.path.join(REF_DIR, f"libdvr_ref_{precision}.so")
+        else:
+            raise ValueError(kind)
+        if not os.path.exists(path):
+            raise FileNotFoundError(f"oracle library {path} not built (run oracle.oracle.build())")
+        lib = ctypes.CDLL(path)
+        lib.oracle_forward.argtypes = [ctypes.POINTER(OracleInputs), ctypes.POINTER(OracleTensor),
+                                       ctypes.POINTER(OracleTensor)]
+        lib.oracle_adjoint.argtypes = [ctypes.POINTER(OracleInputs), ctypes.POINTER(OracleTensor),
+                                       ctypes.POINTER(OracleTensor), ctypes.POINTER(OracleTensor),
+                                       ctypes.POINTER(OracleAdjointOutputs)]
+        lib.oracle_forward.restype = ctypes.c_int
+        lib.oracle_adjoint.restype = ctypes.c_int
+        lib.oracle_real_size.restype = ctypes.c_int
+        _LIBS[key] = lib
+    return _LIBS[key]
+
+
+def _tensor(arr: Optional[np.ndarray], keep: list) -> OracleTensor:
+    t = OracleTensor()
+    if arr is None:
+        t.data = None
+        t.ndim = 0
+        return t
+    arr = np.ascontiguousarray(arr)
+    keep.append(arr)
+    t.data = arr.ctypes.data
+    t.ndim = arr.ndim
+    for d in range(arr.ndim):
+        t.sizes[d] = arr.shape[d]
+        t.strides[d] = arr.strides[d] // arr.itemsize
+    return t
+
+
+@dataclass
+class Scene:
+    """Renderer inputs in the reference layout (numpy, any float dtype)."""
+    width: int
+    height: int
+    volume: np.ndarray
+    tf: np.ndarray
+    step_size: np.ndarray            # (B)(H)(W)
+    box_min: np.ndarray              # (B)3
+    box_size: np.ndarray             # (B)3
+    filter_mode: int = 1
+    camera_mode: int = 0
+    tf_mode: int = 1
+    blend_mode: int = 0
+    ray_start: Optional[np.ndarray] = None
+    ray_dir: Optional[np.ndarray] = None
+    camera_matrix: Optional[np.ndarray] = None
+    fov_y_radians: float = 0.0
+    blending_early_out: float = 1.0 - 1e-5
+
+    def batch(self) -> int:
+        arrs = [self.volume, self.tf, self.step_size, self.box_min, self.box_size]
+        if self.camera_mode == 0:
+            arrs += [self.ray_start, self.ray_dir]
+        else:
+            arrs += [self.camera_matrix]
+        return max(int(a.shape[0]) for a in arrs)
+
+
+def _inputs(scene: Scene, dtype, keep: list) -> OracleInputs:
+    cast = lambda a: None if a is None else np.asarray(a, dtype=dtype)
+    i = OracleInputs()
+    i.width, i.height = scene.width, scene.height
+    i.filter_mode, i.camera_mode = scene.filter_mode, scene.camera_mode
+    i.tf_mode, i.blend_mode = scene.tf_mode, scene.blend_mode
+    i.volume = _tensor(cast(scene.volume), keep)
+    i.box_min = _tensor(cast(scene.box_min), keep)
+    i.box_size = _tensor(cast(scene.box_size), keep)
+    empty4 = np.zeros((1, 1, 1, 3), dtype=dtype)
+    i.ray_start = _tensor(cast(scene.ray_start) if scene.ray_start is not None else empty4, keep)
+    i.ray_dir = _tensor(cast(scene.ray_dir) if scene.ray_dir is not None else empty4, keep)
+    empty3 = np.zeros((1, 4, 4), dtype=dtype)
+    i.camera_matrix = _tensor(cast(scene.camera_matrix) if scene.camera_matrix is not None else empty3, keep)
+    i.fov_y_radians = float(scene.fov_y_radians)
+    i.step_size = _tensor(cast(scene.step_size), keep)
+    i.tf = _tensor(cast(scene.tf), keep)
+    i.blending_early_out = float(scene.blending_early_out)
+    i.batch = scene.batch()
+    return i
+
+
+def _dtype(lib) -> type:
+    return np.float64 if lib.oracle_real_size() == 8 else np.float32
+
+
+def forward(scene: Scene, kind: str = "port", precision: str = "f64"):
+    """Returns (color B*H*W*4, termination_index B*H*W int32)."""
+    lib = load(kind, precision)
+    dt = _dtype(lib)
+    keep: list = []
+    inp = _inputs(scene, dt, keep)
+    B = inp.batch
+    color = np.zeros((B, scene.height, scene.width, 4), dtype=dt)
+    term = np.zeros((B, scene.height, scene.width), dtype=np.int32)
+    tc, tt = _tensor(color, keep), _tensor(term, keep)
+    rc = lib.oracle_forward(ctypes.byref(inp), ctypes.byref(tc), ctypes.byref(tt))
+    if rc != 0:
+        raise RuntimeError(f"oracle_forward failed with code {rc}")
+    return color, term
+
+
+@dataclass
+class AdjointRequest:
+    volume: bool = False
+    tf: bool = False
+    camera: bool = False
+    stepsize: bool = False
+    # shapes of the gradient outputs (broadcast dims allowed); None = full shape
+    stepsize_shape: Optional[tuple] = None
+    camera_batch: Optional[int] = None
+    volume_batch: Optional[int] = None
+    tf_batch: Optional[int] = None
+    results: dict = field(default_factory=dict)
+
+
+def adjoint(scene: Scene, color: np.ndarray, term: np.ndarray, adj_color: np.ndarray,
+            req: AdjointRequest, kind: str = "port", precision: str = "f64") -> dict:
+    """Runs the adjoint march; returns a dict of gradient arrays (zero-initialised)."""
+    lib = load(kind, precision)
+    dt = _dtype(lib)
+    keep: list = []
+    inp = _inputs(scene, dt, keep)
+    B, H, W = inp.batch, scene.height, scene.width
+    out = OracleAdjointOutputs()
+    res = {}
+    if req.volume:
+        vb = req.volume_batch or int(scene.volume.shape[0])
+        res["adj_volume"] = np.zeros((vb,) + tuple(scene.volume.shape[1:]), dtype=dt)
+        out.has_volume = 1
+        out.adj_volume = _tensor(res["adj_volume"], keep)
+    if req.tf:
+        tb = req.tf_batch or int(scene.tf.shape[0])
+        res["adj_tf"] = np.zeros((tb,) + tuple(scene.tf.shape[1:]), dtype=dt)
+        out.has_tf = 1
+        out.adj_tf = _tensor(res["adj_tf"], keep)
+    if req.camera:
+        cb = req.camera_batch or B
+        res["adj_ray_start"] = np.zeros((cb, H, W, 3), dtype=dt)
+        res["adj_ray_dir"] = np.zeros((cb, H, W, 3), dtype=dt)
+        out.has_camera = 1
+        out.camera_broadcast = int(cb != B)
+        out.adj_ray_start = _tensor(res["adj_ray_start"], keep)
+        out.adj_ray_dir = _tensor(res["adj_ray_dir"], keep)
+    if req.stepsize:
+        shp = req.stepsize_shape or (B, H, W)
+        res["adj_stepsize"] = np.zeros(shp, dtype=dt)
+        out.has_stepsize = 1
+        out.stepsize_broadcast = int(tuple(shp) != (B, H, W))
+        out.adj_stepsize = _tensor(res["adj_stepsize"], keep)
+    tc =_tensor(np.asarray(color, dtype=dt), keep)
+    tt = _tensor(np.asarray(term, dtype=np.int32), keep)
+    ta = _tensor(np.asarray(adj_color, dtype=dt), keep)
+    rc = lib.oracle_adjoint(ctypes.byref(inp), ctypes.byref(tc), ctypes.byref(tt), ctypes.byref(ta),
+                            ctypes.byref(out))
+    if rc != 0:
+        raise RuntimeError(f"oracle_adjoint failed with code {rc}")
+    return res

@@ -1,0 +1,187 @@
+"""C ABI and host logic without a GPU: the library loads and exports every
+symbol of include/diffdvr_gb300.h; argument validation mirrors the reference's
+checks (renderer/renderer.cpp:49-391, :660-742) and fails before any CUDA call."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from diffdvr_gb300 import _abi
+from diffdvr_gb300 import pyrenderer as pr
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "diffdvr_gb300.h")
+
+
+def header_functions():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\*?\s+\*?(dvr_\w+)\(", text, re.M)))
+
+
+def test_library_exports_every_header_symbol(dvr_lib):
+    names = header_functions()
+    assert len(names) >= 10
+    for n in names:
+        assert hasattr(dvr_lib, n), n
+    assert set(names) == set(_abi.SIGNATURES)
+    assert dvr_lib.dvr_abi_version() == 1
+
+
+def _fake(shape, dtype=_abi.DVR_FLOAT32, cuda=True, ptr=0x100000):
+    t = _abi.DvrTensor()
+    t.data = ptr
+    t.ndim = len(shape)
+    t.dtype = dtype
+    t.device_type = _abi.DVR_DEVICE_CUDA if cuda else _abi.DVR_DEVICE_CPU
+    t.device_index = 0 if cuda else -1
+    st = 1
+    for i in reversed(range(len(shape))):
+        t.sizes[i] = shape[i]
+        t.strides[i] = st
+        st *= shape[i]
+    return t
+
+
+def _inputs(B=1, X=4, Y=5, Z=6, W=8, H=7, tf_mode=1, R=8):
+    c = _abi.DvrRendererInputs()
+    c.screen_width, c.screen_height = W, H
+    c.volume_filter_mode, c.camera_mode, c.tf_mode, c.blend_mode = 1, 0, tf_mode, 0
+    c.volume = _fake((B, X, Y, Z))
+    c.box_min_kind = c.box_size_kind = _abi.DVR_KIND_VALUE
+    c.box_min = _fake(())
+    c.box_min.ndim = -1
+    c.box_size = _fake(())
+    c.box_size.ndim = -1
+    for i in range(3):
+        c.box_min_value[i], c.box_size_value[i] = -0.5, 1.0
+    c.camera_kind = _abi.DVR_CAMERA_PER_PIXEL_RAYS
+    c.camera_ray_start = _fake((B, H, W, 3))
+    c.camera_ray_dir = _fake((B, H, W, 3))
+    c.camera_matrix = _fake(())
+    c.camera_matrix.ndim = -1
+    c.step_size_kind = _abi.DVR_KIND_VALUE
+    c.step_size = _fake(())
+    c.step_size.ndim = -1
+    c.step_size_value = 0.01
+    C = {0: 2, 1: 4, 2: 5, 3: 6}[tf_mode]
+    c.tf = _fake((B, 1 if tf_mode == 0 else R, C))
+    c.blending_early_out = 1 - 1e-5
+    return c
+
+
+def _outputs(B=1, W=8, H=7):
+    o = _abi.DvrRendererOutputs()
+    o.color = _fake((B, H, W, 4))
+    o.termination_index = _fake((B, H, W), _abi.DVR_INT32)
+    o.checkpoints = _fake(())
+    o.checkpoints.ndim = -1
+    o.checkpoint_interval = 32
+    return o
+
+
+def _forward(lib, i, o):
+    code = lib.dvr_render_forward(ctypes.byref(i), ctypes.byref(o), None)
+    return code, lib.dvr_last_error().decode()
+
+
+@pytest.mark.parametrize("mutate,expect", [
+    (lambda i, o: setattr(i, "volume", _fake((4, 5, 6))), "volume must be a tensor with 4 dimensions"),
+    (lambda i, o: setattr(i, "volume", _fake((1, 4, 5, 6), cuda=False)), "CPU tensor"),
+    (lambda i, o: setattr(i, "volume", _fake((1, 4, 5, 6), _abi.DVR_FLOAT64)), "volume must be of type float32"),
+    (lambda i, o: setattr(i, "tf", _fake((1, 8, 3))), "tf must have 4 entries at dimension 2"),
+    (lambda i, o: setattr(i, "tf_mode", 6), "TFGaussianLog is not supported"),
+    (lambda i, o: setattr(i, "volume_filter_mode", 3), "pre-shaded volumes are not supported"),
+    (lambda i, o: setattr(i, "camera_ray_start", _fake((1, 7, 9, 3))), "cameraRayStart must have 8 entries at dimension 2"),
+    (lambda i, o: setattr(i, "camera_ray_dir", _fake((3, 7, 8, 3))), None),  # batch 3 vs 1 broadcasts; passes checks
+    (lambda i, o: setattr(i, "camera_mode", 2), "'CameraReferenceFrame' specified in 'cameraMode'"),
+    (lambda i, o: setattr(o, "color", _fake((1, 7, 8, 3))), "color must have 4 entries at dimension 3"),
+    (lambda i, o: setattr(o, "termination_index", _fake((1, 7, 8))), "terminationIndex must be of type int32"),
+])
+def test_forward_validation_messages(dvr_lib, mutate, expect):
+    i, o = _inputs(), _outputs()
+    mutate(i, o)
+    code, msg = _forward(dvr_lib, i, o)
+    if expect is None:
+        # all checks pass for broadcasting, the output batch (1) is then wrong
+        assert code == _abi.DVR_E_INVALID_ARGUMENT and "color must have 3 entries at dimension 0" in msg
+    else:
+        assert code in (_abi.DVR_E_INVALID_ARGUMENT, _abi.DVR_E_UNSUPPORTED)
+        assert expect in msg, msg
+
+
+def test_linear_tf_needs_two_points(dvr_lib):
+    i, o = _inputs(tf_mode=2, R=1), _outputs()
+    code, msg = _forward(dvr_lib, i, o)
+    assert code == _abi.DVR_E_INVALID_ARGUMENT and "at least two control points" in msg
+
+
+def test_batch_mismatch(dvr_lib):
+    i, o = _inputs(B=2), _outputs(B=2)
+    i.tf = _fake((3, 8, 4))
+    code, msg = _forward(dvr_lib, i, o)
+    assert "tf must be have the same batch size as other tensors" in msg
+
+
+def test_adjoint_without_gradients_is_rejected(dvr_lib):
+    i, o = _inputs(), _outputs()
+    a = _abi.DvrAdjointOutputs()
+    for n in ("adj_volume", "adj_stepsize", "adj_camera_ray_start", "adj_camera_ray_dir", "adj_tf"):
+        getattr(a, n).ndim = -1
+    adj = _fake((1, 7, 8, 4))
+    code = dvr_lib.dvr_render_adjoint(ctypes.byref(i), ctypes.byref(o), ctypes.byref(adj), ctypes.byref(a), None)
+    assert code == _abi.DVR_E_NO_GRADIENT
+    assert "At least one adjoint variable must be activated" in dvr_lib.dvr_last_error().decode()
+
+
+def test_adjoint_output_shape_checks(dvr_lib):
+    i, o = _inputs(), _outputs()
+    a = _abi.DvrAdjointOutputs()
+    a.has_tf_derivatives = 1
+    a.adj_tf = _fake((1, 7, 4))
+    adj = _fake((1, 7, 8, 4))
+    code = dvr_lib.dvr_render_adjoint(ctypes.byref(i), ctypes.byref(o), ctypes.byref(adj), ctypes.byref(a), None)
+    assert code == _abi.DVR_E_INVALID_ARGUMENT
+    assert "adj_tf must have 8 entries at dimension 1" in dvr_lib.dvr_last_error().decode()
+
+
+def test_checkpoint_slots(dvr_lib):
+    # 256^3 box diagonal sqrt(3), step 0.25 voxel: at most 1768 samples -> 56 slots of 32
+    n = dvr_lib.dvr_checkpoint_slots(np.sqrt(3.0), 0.25 / 255, 32)
+    assert n == int(np.ceil((np.floor(np.sqrt(3.0) / (0.25 / 255)) + 2) / 32))
+    assert dvr_lib.dvr_checkpoint_slots(1.0, 0.0, 32) < 0
+    assert dvr_lib.dvr_checkpoint_slots(1.0, 0.1, 100) < 0
+
+
+def test_kernel_family_and_sync_mode(dvr_lib):
+    prev = pr.set_kernel_family("plain")
+    assert pr.get_kernel_family() == "plain"
+    pr.set_kernel_family(prev)
+    pr.set_cuda_sync_mode(True)
+    assert pr.get_cuda_sync_mode()
+    pr.set_cuda_sync_mode(False)
+    assert dvr_lib.dvr_set_kernel_family(7) == _abi.DVR_E_INVALID_ARGUMENT
+
+
+def test_python_api_mirrors_reference_names():
+    inp = pr.RendererInputs()
+    for f in ("screen_size", "volume", "volume_filter_mode", "box_min", "box_size", "camera_mode", "camera",
+              "step_size", "tf_mode", "tf", "blend_mode", "blending_early_out"):
+        assert hasattr(inp, f), f
+    c = inp.clone()
+    assert c is not inp and c.camera is inp.camera  # shallow
+    a = pr.AdjointOutputs()
+    for f in ("has_volume_derivatives", "adj_volume", "has_stepsize_derivatives", "adj_stepsize",
+              "has_camera_derivatives", "adj_camera_ray_start", "adj_camera_ray_dir", "has_tf_derivatives",
+              "tf_delayed_accumulation", "adj_tf"):
+        assert hasattr(a, f), f
+    assert pr.TFMode.Gaussian == 3 and pr.BlendMode.Alpha == 1 and pr.CameraMode.ReferenceFrame == 2
+    assert pr.VolumeFilterMode.Trilinear == 1
+    assert abs(inp.blending_early_out - (1 - 1e-5)) < 1e-12
+
+
+def test_forward_mode_differentiation_is_reported_missing():
+    from diffdvr_gb300 import Renderer
+    with pytest.raises(NotImplementedError):
+        Renderer(optimize_tf=True, gradient_method="forward")

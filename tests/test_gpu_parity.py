@@ -1,0 +1,422 @@
+"""GPU parity: the CUDA kernels (through the C ABI) against the oracle and
+the reference fixtures, for every mode combination and both kernel families.
+
+Tolerances (stated per check):
+* forward colour: the reference's symmetric metric |a-b|/max(1,|a|+|b|)
+  against the FP64 oracle <= tol = max(1e-5, 3 * e32), where e32 is the
+  same metric between the reference's own FP32 and FP64 computations of the
+  case (the inverse-view-matrix camera is ill-conditioned in FP32: e32 reaches
+  2e-5); against the FP32 oracle <= tol + e32.  Compared on pixels whose
+  sample count agrees; the count may differ by one on rays whose last sample
+  sits on the box exit or the early-out threshold up to rounding (<= 2% of
+  pixels).  With nearest filtering a sample within rounding of a voxel
+  boundary may pick the neighbouring voxel, so up to 2% of pixels may exceed
+  tol there.
+* gradients: relative L2 error against the FP64 oracle (forward + adjoint in
+  FP64) <= max(1e-3, 3 * r32), r32 the reference FP32 build's own relative
+  error, and at most 1% of entries off by more than 1e-3 of the largest
+  reference entry.  Test volumes
+  keep densities inside (0, 1) and repeat the outermost layers, so the
+  derivatives of the identity TF and of the trilinear position are continuous
+  at the box faces (rays entering through a face at the maximum coordinate
+  have their first sample on the face, where the reference's derivative is
+  one-sided).  Adjoint scenes keep rays short of opaque, where the reference's
+  blend inversion (used by the plain family) is ill-conditioned in FP32; the
+  checkpointed adjoint is checked on opaque rays separately.
+"""
+import numpy as np
+import pytest
+import torch
+
+from dvr_cases import (all_mode_combos, golden, golden_case, golden_prefixes, gpu_adjoint, gpu_forward, make_case,
+                       rel_l2, symmetric_error)
+
+pytestmark = pytest.mark.gpu
+
+FAMILIES = ["plain", "optimized"]
+
+
+def _pixel_errors(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return np.max(np.abs(a - b) / np.maximum(1.0, np.abs(a) + np.abs(b)), axis=-1)
+
+
+def _forward_errors(case, color, term, O, max_mismatch=0.02):
+    """List of failed checks (empty when the forward output matches)."""
+    sc = case.oracle_scene()
+    c32, t32 = O.forward(sc, "port", "f32")
+    c64, t64 = O.forward(sc, "port", "f64")
+    agree = t32 == t64
+    e32 = symmetric_error(c32[agree], c64[agree])
+    tol64 = max(1e-5, 3 * e32)
+    outliers = 0.02 if case.filter_mode == 0 else 0.0
+    bad = []
+    for prec, oc, ot, tol in (("f64", c64, t64, tol64), ("f32", c32, t32, tol64 + e32)):
+        same = term == ot
+        if np.mean(~same) > max_mismatch:
+            bad.append(f"{prec}: termination mismatch on {np.mean(~same):.3f} of pixels")
+        if not np.all(np.abs(term[~same] - ot[~same]) <= 1):
+            bad.append(f"{prec}: termination index off by more than one")
+        pe = _pixel_errors(color[same], oc[same])
+        if pe.size and np.mean(pe > tol) > outliers:
+            bad.append(f"{prec}: colour error {pe.max():.2e} > {tol:.1e} on {np.mean(pe > tol):.3f} of pixels")
+    return bad
+
+
+def _compare_forward(case, color, term, O):
+    bad = _forward_errors(case, color, term, O)
+    assert not bad, bad
+
+
+@pytest.mark.parametrize("family", FAMILIES)
+def test_forward_all_modes(family, oracle_built, cuda_device):
+    O = oracle_built
+    failures = {}
+    for i, (tfm, filt, blend, cam) in enumerate(all_mode_combos()):
+        case = make_case(200 + i, tf_mode=tfm, filter_mode=filt, blend_mode=blend, camera_mode=cam)
+        _, out = gpu_forward(case, family)
+        bad = _forward_errors(case, out.color.cpu().numpy(), out.terminationIndex.cpu().numpy(), O)
+        if bad:
+            failures[(tfm, filt, blend, cam)] = bad
+    assert not failures, failures
+
+
+@pytest.mark.parametrize("family", FAMILIES)
+def test_forward_matches_reference_fixtures(family, oracle_built, cuda_device):
+    """Against the reference's own FP64 and FP32 CPU renders (fixtures), with
+    the tolerances of _forward_errors (e32 taken from the two fixtures)."""
+    g = golden("modes.npz")
+    failures = {}
+    for p in golden_prefixes(g):
+        case = golden_case(g, p)
+        _, out = gpu_forward(case, family)
+        color, term = out.color.cpu().numpy(), out.terminationIndex.cpu().numpy()
+        agree = g[p + "term_f32"] == g[p + "term_f64"]
+        e32 = symmetric_error(g[p + "color_f32"][agree], g[p + "color_f64"][agree])
+        tol64 = max(1e-5, 3 * e32)
+        outliers = 0.02 if case.filter_mode == 0 else 0.0
+        for prec, tol in (("f64", tol64), ("f32", tol64 + e32)):
+            same = term == g[p + "term_" + prec]
+            pe = _pixel_errors(color[same], g[p + "color_" + prec][same])
+            if np.mean(~same) > 0.05 or (pe.size and np.mean(pe > tol) > outliers):
+                failures[(p, prec)] = (float(np.mean(~same)), float(pe.max()), tol)
+    assert not failures, failures
+
+
+def _grad_errors(got, ref, r32=None):
+    bad = {}
+    for k in got:
+        r = rel_l2(got[k], ref[k])
+        tol = max(1e-3, 3 * r32[k]) if r32 else 1e-3
+        scale = max(float(np.max(np.abs(ref[k]))), 1e-30)
+        pe = np.abs(np.asarray(got[k], np.float64) - ref[k]) / scale
+        frac = float(np.mean(pe > 1e-3))
+        if r > tol or frac > 0.01:
+            bad[k] = (r, tol, frac)
+    return bad
+
+
+def reference_adjoint(case, O, gpu_term, adj, req, oracle_case=None):
+    """FP64 oracle forward + adjoint of the same scene.  Pixels whose sample
+    count differs from the GPU's get a zero output adjoint, in the returned
+    adj as well, so both sides sum the same rays.  (Inverting the blend from
+    the GPU's FP32 colour instead would amplify its rounding by 1/(1-alpha)
+    on near-opaque rays.)"""
+    sc = (oracle_case or case).oracle_scene()
+    c64, t64 = O.forward(sc, "port", "f64")
+    adj = np.where((gpu_term == t64)[..., None], adj, 0.0).astype(np.float32)
+    return O.adjoint(sc, c64, t64, adj, req, "port", "f64"), adj
+
+
+def _adjoint_case(case, family, O, checkpoints, stepsize):
+    cam = case.camera_mode == 0
+    inp, out = gpu_forward(case, family, checkpoints=checkpoints)
+    term = out.terminationIndex.cpu().numpy()
+    adj = np.random.default_rng(7).normal(size=out.color.shape).astype(np.float32)
+    req = O.AdjointRequest(volume=True, tf=True, camera=cam, stepsize=stepsize)
+    ref, adj = reference_adjoint(case, O, term, adj, req)
+    got = gpu_adjoint(case, inp, out, adj, volume=True, tf=True, camera=cam, stepsize=stepsize, family=family)
+    # the reference FP32 build's own error on the same rays, as a yardstick
+    sc = case.oracle_scene()
+    c32, t32 = O.forward(sc, "port", "f32")
+    g32 = O.adjoint(sc, c32, t32, np.where((t32 == term)[..., None], adj, 0.0), req, "port", "f32")
+    r32 = {k: rel_l2(g32[k], ref[k]) for k in g32}
+    return got, ref, r32
+
+
+@pytest.mark.parametrize("family,checkpoints", [("plain", False), ("optimized", False), ("optimized", True)])
+def test_adjoint_all_modes(family, checkpoints, oracle_built, cuda_device):
+    O = oracle_built
+    failures = {}
+    for i, (tfm, filt, blend, cam) in enumerate(all_mode_combos()):
+        case = make_case(300 + i, tf_mode=tfm, filter_mode=filt, blend_mode=blend, camera_mode=cam, opacity=0.25,
+                         pad_faces=True)
+        # the optimized family returns the full step-size derivative, the
+        # reference (and the oracle) only the last blend term; checked by FD below
+        got, ref, r32 = _adjoint_case(case, family, O, checkpoints, stepsize=(family == "plain"))
+        bad = _grad_errors(got, ref, r32)
+        if bad:
+            failures[(tfm, filt, blend, cam)] = bad
+    assert not failures, failures
+
+
+@pytest.mark.parametrize("family", FAMILIES)
+def test_broadcasting_matches_reference_fixture(family, oracle_built, cuda_device):
+    """Volume B=1 with TF B=2, per-pixel step sizes, box tensors; gradients of
+    broadcast inputs accumulate over the batch (atomics into stride-0 outputs)."""
+    g = golden("broadcast.npz")
+    case = golden_case(g, "b_")
+    inp, out = gpu_forward(case, family, checkpoints=(family == "optimized"))
+    term = out.terminationIndex.cpu().numpy()
+    same = term == g["b_term_f64"]
+    assert np.mean(~same) <= 0.02
+    assert symmetric_error(out.color.cpu().numpy()[same], g["b_color_f64"][same]) <= 1e-5
+    if np.all(same):
+        # volume and TF gradients against the reference's FP64 adjoint; the
+        # plain family inverts the blend in FP32, which loses accuracy on the
+        # opaque rays of this scene, so it is held to 1e-2
+        tol = 1e-3 if family == "optimized" else 1e-2
+        got = gpu_adjoint(case, inp, out, g["b_adj_color"], volume=True, tf=True, family=family, volume_batch=1)
+        for k in got:
+            assert rel_l2(got[k], g["b_" + k + "_f64"]) <= tol, (k, rel_l2(got[k], g["b_" + k + "_f64"]))
+    # broadcast camera / step-size gradients equal the per-batch gradients summed
+    adj = g["b_adj_color"]
+    full = gpu_adjoint(case, inp, out, adj, camera=True, stepsize=True, family=family)
+    bc = gpu_adjoint(case, inp, out, adj, camera=True, stepsize=True, family=family, stepsize_shape=(1, 1, 1),
+                     camera_batch=1)
+    for k in ("adj_ray_start", "adj_ray_dir"):
+        assert np.allclose(bc[k][0], full[k].sum(0), rtol=1e-5, atol=1e-6), k
+    assert np.allclose(bc["adj_stepsize"].item(), full["adj_stepsize"].sum(), rtol=1e-5, atol=1e-6)
+
+
+def test_plain_adjoint_immediate_and_delayed_tf_accumulation_agree(cuda_device, oracle_built):
+    case = make_case(41, tf_mode=3, R=6)
+    inp, out = gpu_forward(case, "plain")
+    adj = np.random.default_rng(3).normal(size=(case.batch(), case.height, case.width, 4))
+    a = gpu_adjoint(case, inp, out, adj, tf=True, family="plain", delayed=True)
+    b = gpu_adjoint(case, inp, out, adj, tf=True, family="plain", delayed=False)
+    assert rel_l2(a["adj_tf"], b["adj_tf"]) <= 1e-5
+
+
+def _nonconvex_case(d1: float):
+    from dvr_cases import Case
+    vol = np.zeros((1, 2, 2, 2), np.float32)
+    vol[0, 0], vol[0, 1] = -1.0, d1
+    return Case(width=1, height=1, volume=vol, tf=np.array([[[1, 0, 0, 1, 0, 0.5]]], np.float32), tf_mode=3,
+                filter_mode=1, blend_mode=0, camera_mode=0, step=1 / 32, box_min=(0.0, 0.0, 0.0),
+                box_size=(1.0, 1.0, 1.0), ray_start=np.array([[[[-1.0, 0.5, 0.5]]]], np.float32),
+                ray_dir=np.array([[[[1.0, 0.0, 0.0]]]], np.float32))
+
+
+@pytest.mark.parametrize("family", FAMILIES)
+def test_nonconvex_density_table_on_gpu(family, cuda_device):
+    """The reference's known-answer table (unittests/NonConvexDensity.tsv)
+    through the CUDA kernels: colour, loss and d(loss)/d(d1)."""
+    t = golden("nonconvex_density.npz")
+    _, o = gpu_forward(_nonconvex_case(-1.0), family)
+    gt = o.color.cpu().numpy()[0, 0, 0].astype(np.float64)
+    for d1, red, alpha, loss, grad in t["table"]:
+        case = _nonconvex_case(d1)
+        inp, out = gpu_forward(case, family, checkpoints=(family == "optimized"))
+        c = out.color.cpu().numpy()[0, 0, 0].astype(np.float64)
+        assert int(out.terminationIndex.item()) == 33
+        diff = c - gt
+        l = float(np.linalg.norm(diff))
+        adj = (diff / l if l > 0 else np.zeros(4))[None, None, None, :]
+        g = gpu_adjoint(case, inp, out, adj, volume=True, family=family)
+        gr = float(g["adj_volume"][0, 1].sum())
+        tol = 2e-5 if abs(d1) < 100 else 1e-4
+        assert abs(c[0] - red) <= tol and abs(c[3] - alpha) <= tol, d1
+        assert abs(l - loss) <= tol, d1
+        assert abs(gr - grad) <= 3e-5 + 2e-3 * abs(grad), (d1, gr, grad)
+
+
+@pytest.mark.parametrize("dtype", [torch.bfloat16, torch.float16])
+def test_reduced_precision_storage(dtype, oracle_built, cuda_device):
+    """Volume and TF stored in BF16/FP16, sampled and blended in FP32: against
+    the FP64 oracle on the same rounded values (forward 1e-5, gradients 1e-3)."""
+    O = oracle_built
+    case = make_case(51, tf_mode=1, shape=(17, 19, 21), W=24, H=20, B=2, R=16, pad_faces=True)
+    rounded = lambda a: torch.from_numpy(a).to(dtype).float().numpy()
+    case_r = make_case(51, tf_mode=1, shape=(17, 19, 21), W=24, H=20, B=2, R=16, pad_faces=True)
+    case_r.volume, case_r.tf = rounded(case.volume), rounded(case.tf)
+    inp, out = gpu_forward(case, "optimized", volume_dtype=dtype, tf_dtype=dtype, checkpoints=True)
+    color, term = out.color.cpu().numpy(), out.terminationIndex.cpu().numpy()
+    _compare_forward(case_r, color, term, O)
+    adj = np.random.default_rng(9).normal(size=color.shape)
+    ref, adj = reference_adjoint(case, O, term, adj, O.AdjointRequest(volume=True, tf=True, camera=True),
+                                 oracle_case=case_r)
+    got = gpu_adjoint(case, inp, out, adj, volume=True, tf=True, camera=True)
+    bad = _grad_errors(got, ref)
+    assert not bad, bad
+
+
+def test_batched_uneven_matches_single_instances(cuda_device):
+    from diffdvr_gb300 import pyrenderer as pr
+    cases = [make_case(61, tf_mode=3, shape=(9, 10, 11), W=20, H=12, B=1),
+             make_case(62, tf_mode=3, shape=(17, 13, 15), W=33, H=17, B=2),
+             make_case(63, tf_mode=3, shape=(5, 6, 7), W=8, H=8, B=1)]
+    singles = [gpu_forward(c, "optimized", checkpoints=True) for c in cases]
+    ins, outs = [], []
+    for c in cases:
+        inp = c.inputs("cuda")
+        B = c.batch()
+        ck = torch.empty(B, c.height, c.width, pr.Renderer.checkpoint_slots(inp), device="cuda")
+        ins.append(inp)
+        outs.append(pr.RendererOutputs(torch.empty(B, c.height, c.width, 4, device="cuda"),
+                                       torch.empty(B, c.height, c.width, dtype=torch.int32, device="cuda"), ck, 32))
+    pr.Renderer.render_forward_batched(ins, outs)
+    torch.cuda.synchronize()
+    for (si, so), o in zip(singles, outs):
+        assert torch.equal(so.terminationIndex, o.terminationIndex)
+        assert torch.equal(so.color, o.color)
+    adjs = [torch.randn_like(o.color) for o in outs]
+    single_g, batch_g = [], []
+    for c, (si, so), a in zip(cases, singles, adjs):
+        single_g.append(gpu_adjoint(c, si, so, a.cpu().numpy(), volume=True, tf=True))
+    aos = []
+    for c in cases:
+        ao = pr.AdjointOutputs()
+        ao.has_volume_derivatives = True
+        ao.adj_volume = torch.zeros(c.volume.shape, device="cuda")
+        ao.has_tf_derivatives = True
+        ao.adj_tf = torch.zeros(c.tf.shape, device="cuda")
+        aos.append(ao)
+    pr.Renderer.render_adjoint_batched(ins, outs, adjs, aos)
+    torch.cuda.synchronize()
+    for sg, ao in zip(single_g, aos):
+        assert rel_l2(ao.adj_volume.cpu().numpy(), sg["adj_volume"]) <= 1e-5
+        assert rel_l2(ao.adj_tf.cpu().numpy(), sg["adj_tf"]) <= 1e-5
+
+
+def test_checkpointed_adjoint_is_exact_for_opaque_rays(oracle_built, cuda_device):
+    """With high absorption the reference's blend inversion loses accuracy in
+    FP32 (it divides by alpha - 1); the checkpointed adjoint does not."""
+    O = oracle_built
+    case = make_case(71, tf_mode=0, shape=(12, 12, 12), W=16, H=16, B=1)
+    case.tf = np.array([[[60.0, 1.0]]], np.float32)
+    inp, out = gpu_forward(case, "optimized", checkpoints=True)
+    term = out.terminationIndex.cpu().numpy()
+    assert np.mean(out.color[..., 3].cpu().numpy() > 0.999) > 0.2  # many rays are opaque
+    adj = np.random.default_rng(2).normal(size=out.color.shape)
+    ref, adj = reference_adjoint(case, O, term, adj, O.AdjointRequest(volume=True, tf=True))
+    got = gpu_adjoint(case, inp, out, adj, volume=True, tf=True)
+    for k in got:
+        assert rel_l2(got[k], ref[k]) <= 1e-3, (k, rel_l2(got[k], ref[k]))
+
+
+def test_full_stepsize_gradient_matches_finite_differences(oracle_built, cuda_device):
+    """The optimized family's step-size gradient against central differences
+    of the FP64 forward (interior blobs, so no sample crosses the box exit)."""
+    O = oracle_built
+    case = make_case(81, tf_mode=2, shape=(16, 16, 16), W=12, H=12, B=1)
+    g = np.zeros((1, 16, 16, 16), np.float32)
+    g[0, 3:13, 3:13, 3:13] = case.volume[0, 3:13, 3:13, 3:13]
+    case.volume = g
+    case.tf[..., 3] *= 0.2
+    inp, out = gpu_forward(case, "optimized", checkpoints=True)
+    color = out.color.cpu().numpy()
+    w = np.random.default_rng(4).normal(size=color.shape)
+    got = gpu_adjoint(case, inp, out, w, stepsize=True, stepsize_shape=(1, 1, 1))
+    sc = case.oracle_scene()
+    s0 = float(case.step)
+    h = 1e-4 * s0
+
+    def loss(step):
+        sc.step_size = np.full((1, 1, 1), step)
+        c, _ = O.forward(sc, "port", "f64")
+        return float((c * w).sum())
+
+    fd = (loss(s0 + h) - loss(s0 - h)) / (2 * h)
+    assert abs(got["adj_stepsize"].item() - fd) <= 1e-3 * max(1.0, abs(fd)), (got["adj_stepsize"].item(), fd)
+
+
+def test_tf_gradient_finite_differences_16_entries(oracle_built, cuda_device):
+    """TF-reconstruction setting at test size: texture TF R=64, Beer-Lambert,
+    step 0.25 voxel; GPU TF gradient vs central FD in FP64 on 16 random entries."""
+    from diffdvr_gb300 import scenes
+    O = oracle_built
+    rng = np.random.default_rng(11)
+    vol = scenes.blob_volume(32, 8, rng, noise=0.02)
+    tf = scenes.tf_texture(64, rng)
+    lat, lon = scenes.fibonacci_sphere(2)
+    vp = scenes.viewport_from_sphere(lat, lon, 3.0)
+    rs, rd = scenes.generate_rays(vp, np.radians(45.0), 24, 24)
+    from dvr_cases import Case
+    case = Case(width=24, height=24, volume=vol, tf=tf, tf_mode=1, filter_mode=1, blend_mode=0, camera_mode=0,
+                step=0.25 / 31, ray_start=rs, ray_dir=rd)
+    inp, out = gpu_forward(case, "optimized", checkpoints=True)
+    w = rng.normal(size=out.color.shape)
+    got = gpu_adjoint(case, inp, out, w, tf=True)["adj_tf"]
+    sc = case.oracle_scene()
+    sc.tf = tf.astype(np.float64)
+    sc.volume = vol.astype(np.float64)
+
+    def loss(t):
+        sc.tf = t
+        c, _ = O.forward(sc, "port", "f64")
+        return float((c * w).sum())
+
+    base = tf.astype(np.float64)
+    for e in rng.choice(64 * 4, 16, replace=False):
+        r, c = divmod(int(e), 4)
+        h = 1e-6
+        tp, tm = base.copy(), base.copy()
+        tp[0, r, c] += h
+        tm[0, r, c] -= h
+        fd = (loss(tp) - loss(tm)) / (2 * h)
+        assert abs(got[0, r, c] - fd) <= 1e-3 * max(abs(fd), 1e-2), (r, c, got[0, r, c], fd)
+
+
+def test_autograd_module_matches_direct_calls(cuda_device):
+    from diffdvr_gb300 import Renderer, pyrenderer as pr
+    case = make_case(91, tf_mode=1, B=2)
+    inp = case.inputs("cuda")
+    tf = inp.tf.clone().requires_grad_(True)
+    vol = inp.volume.clone().requires_grad_(True)
+    r = Renderer(inp, optimize_tf=True, optimize_volume=True)
+    img = r(tf=tf, volume=vol)
+    w = torch.randn_like(img)
+    (img * w).sum().backward()
+    inp2, out2 = gpu_forward(case, "optimized", checkpoints=True)
+    assert torch.allclose(img.detach(), out2.color)
+    g = gpu_adjoint(case, inp2, out2, w.cpu().numpy(), volume=True, tf=True)
+    assert rel_l2(tf.grad.cpu().numpy(), g["adj_tf"]) <= 1e-5
+    assert rel_l2(vol.grad.cpu().numpy(), g["adj_volume"]) <= 1e-5
+
+
+def test_camera_gradient_through_generate_rays(cuda_device):
+    """optimize_camera: the module generates per-pixel rays from the viewport
+    with differentiable torch ops and the adjoint returns ray gradients."""
+    from diffdvr_gb300 import Renderer, pyrenderer as pr, scenes
+    case = make_case(95, tf_mode=1, B=1)
+    inp = case.inputs("cuda")
+    vp = torch.from_numpy(scenes.viewport_from_sphere(0.3, 1.0, 2.0).astype(np.float32)).cuda().requires_grad_(True)
+    r = Renderer(inp, optimize_camera=True)
+    img = r(camera=vp, fov_y_radians=0.7)
+    img.sum().backward()
+    assert vp.grad is not None and torch.isfinite(vp.grad).all() and vp.grad.abs().sum() > 0
+
+
+def test_invalid_inputs_raise(cuda_device):
+    from diffdvr_gb300 import pyrenderer as pr
+    case = make_case(99)
+    inp, out = gpu_forward(case, "optimized")
+    bad = inp.clone()
+    bad.volume = inp.volume[0]
+    with pytest.raises(RuntimeError, match="volume must be a tensor with 4 dimensions"):
+        pr.Renderer.render_forward(bad, out)
+    bad = inp.clone()
+    bad.tf = inp.tf[:, :, :3]
+    with pytest.raises(RuntimeError, match="tf must have 4 entries at dimension 2"):
+        pr.Renderer.render_forward(bad, out)
+    bad = inp.clone()
+    bad.tf = inp.tf.cpu()
+    with pytest.raises(RuntimeError, match="CPU tensor"):
+        pr.Renderer.render_forward(bad, out)
+    with pytest.raises(RuntimeError, match="At least one adjoint variable must be activated"):
+        pr.Renderer.render_adjoint(inp, out, torch.zeros_like(out.color), pr.AdjointOutputs())
+    wrong = pr.RendererOutputs(out.color[:, :, :-1], out.terminationIndex)
+    with pytest.raises(RuntimeError, match="color must have"):
+        pr.Renderer.render_forward(inp, wrong)

@@ -1,0 +1,156 @@
+"""The oracle (C restatement) pinned to the reference: golden fixtures made by
+the reference's own CPU code, the reference's known-answer table, and (where
+the reference sources exist) a direct comparison over all mode combinations."""
+import numpy as np
+import pytest
+
+from dvr_cases import (all_mode_combos, golden, golden_case, golden_prefixes, make_case, rel_l2,
+                       symmetric_error)
+
+
+@pytest.fixture(scope="module")
+def modes(oracle_built):
+    return golden("modes.npz")
+
+
+def test_port_forward_matches_reference_fixtures(oracle_built, modes):
+    O = oracle_built
+    for p in golden_prefixes(modes):
+        case = golden_case(modes, p)
+        sc = case.oracle_scene()
+        c32, t32 = O.forward(sc, "port", "f32")
+        c64, t64 = O.forward(sc, "port", "f64")
+        assert np.array_equal(t32, modes[p + "term_f32"]), p
+        assert np.array_equal(t64, modes[p + "term_f64"]), p
+        assert symmetric_error(c32, modes[p + "color_f32"]) <= 2e-6, p
+        assert symmetric_error(c64, modes[p + "color_f64"]) <= 1e-12, p
+
+
+def test_port_adjoint_matches_reference_fixtures(oracle_built, modes):
+    O = oracle_built
+    for p in golden_prefixes(modes):
+        case = golden_case(modes, p)
+        sc = case.oracle_scene()
+        req = O.AdjointRequest(volume=True, tf=True, camera=case.camera_mode == 0, stepsize=True)
+        adj = modes[p + "adj_color"]
+        g64 = O.adjoint(sc, modes[p + "color_f64"], modes[p + "term_f64"], adj, req, "port", "f64")
+        g32 = O.adjoint(sc, modes[p + "color_f32"], modes[p + "term_f32"], adj, req, "port", "f32")
+        for k in g64:
+            assert symmetric_error(g64[k], modes[p + k + "_f64"]) <= 1e-11, (p, k)
+            # multi-threaded atomics sum in a different order than the fixture
+            assert symmetric_error(g32[k], modes[p + k + "_f32"]) <= 2e-5, (p, k)
+
+
+def test_port_broadcasting_matches_reference_fixture(oracle_built):
+    O = oracle_built
+    g = golden("broadcast.npz")
+    case = golden_case(g, "b_")
+    sc = case.oracle_scene()
+    c64, t64 = O.forward(sc, "port", "f64")
+    assert np.array_equal(t64, g["b_term_f64"])
+    assert symmetric_error(c64, g["b_color_f64"]) <= 1e-12
+    req = O.AdjointRequest(volume=True, tf=True, camera=True, stepsize=True, stepsize_shape=(1, 1, 1),
+                           camera_batch=1, volume_batch=1)
+    gr = O.adjoint(sc, c64, t64, g["b_adj_color"], req, "port", "f64")
+    for k in gr:
+        assert symmetric_error(gr[k], g["b_" + k + "_f64"]) <= 1e-11, k
+
+
+def nonconvex_scene(d1: float, O):
+    """A 2x2x2 volume with density d0=-1 at x=0 and d1 at x=1, one ray along
+    +x through the box [0,1]^3 with step 1/32: 33 samples on the density ramp
+    (1-f)*d0 + f*d1 of unittests/testNonConvexDensity.cpp:25-42."""
+    vol = np.zeros((1, 2, 2, 2))
+    vol[0, 0], vol[0, 1] = -1.0, d1
+    return O.Scene(width=1, height=1, volume=vol, tf=np.array([[[1, 0, 0, 1, 0, 0.5]]], float),
+                   step_size=np.full((1, 1, 1), 1 / 32), box_min=np.zeros((1, 3)), box_size=np.ones((1, 3)),
+                   filter_mode=1, camera_mode=0, tf_mode=3, blend_mode=0,
+                   ray_start=np.array([[[[-1.0, 0.5, 0.5]]]]), ray_dir=np.array([[[[1.0, 0.0, 0.0]]]]))
+
+
+def nonconvex_row(d1: float, gt, O, precision="f64"):
+    sc = nonconvex_scene(d1, O)
+    color, term = O.forward(sc, "port", precision)
+    diff = color[0, 0, 0] - gt
+    loss = float(np.linalg.norm(diff))
+    # d|diff|/d(color); at the minimum (loss 0) the table lists a zero gradient
+    adj_color = (diff / loss if loss > 0 else np.zeros_like(diff))[None, None, None, :]
+    g = O.adjoint(sc, color, term, adj_color, O.AdjointRequest(volume=True), "port", precision)
+    grad = float(g["adj_volume"][0, 1].sum())
+    return color[0, 0, 0], int(term[0, 0, 0]), loss, grad
+
+
+def test_oracle_reproduces_nonconvex_density_table(oracle_built):
+    """The reference's known-answer table (unittests/NonConvexDensity.tsv):
+    red, alpha, loss and d(loss)/d(d1), printed with 5 decimals."""
+    O = oracle_built
+    t = golden("nonconvex_density.npz")
+    gt_color, _ = O.forward(nonconvex_scene(-1.0, O), "port", "f64")
+    gt = gt_color[0, 0, 0]
+    assert abs(gt[0] - t["ground_truth_red_alpha"][0]) <= 6e-4
+    assert abs(gt[3] - t["ground_truth_red_alpha"][1]) <= 6e-4
+    for d1, red, alpha, loss, grad in t["table"]:
+        color, n, l, gr = nonconvex_row(d1, gt, O)
+        assert n == 33
+        assert abs(color[0] - red) <= 6e-6, d1
+        assert abs(color[3] - alpha) <= 6e-6, d1
+        assert abs(l - loss) <= 6e-6, d1
+        assert abs(gr - grad) <= 6e-6 + 1e-4 * abs(grad), d1
+
+
+@pytest.mark.parametrize("tf_mode", [0, 1, 2, 3])
+def test_port_gradients_match_central_differences(oracle_built, tf_mode):
+    """FP64 oracle adjoint against central finite differences of the FP64
+    forward, for TF entries and voxels (the reference's checkAdjoint idea,
+    unittests/check_adjoint.h:35-84, with central differences)."""
+    O = oracle_built
+    case = make_case(31 + tf_mode, tf_mode=tf_mode, shape=(5, 6, 7), W=6, H=5, B=1)
+    sc = case.oracle_scene()
+    sc.volume = sc.volume.astype(np.float64)
+    sc.tf = sc.tf.astype(np.float64)
+    rng = np.random.default_rng(tf_mode)
+    color, term = O.forward(sc, "port", "f64")
+    w = rng.normal(size=color.shape)
+    g = O.adjoint(sc, color, term, w, O.AdjointRequest(volume=True, tf=True), "port", "f64")
+
+    def loss(s):
+        c, _ = O.forward(s, "port", "f64")
+        return float((c * w).sum())
+
+    flat_tf = [(r, c) for r in range(sc.tf.shape[1]) for c in range(sc.tf.shape[2])]
+    for (r, c) in [flat_tf[i] for i in rng.choice(len(flat_tf), min(6, len(flat_tf)), replace=False)]:
+        h = 1e-6 * max(1.0, abs(sc.tf[0, r, c]))
+        tp, tm = sc.tf.copy(), sc.tf.copy()
+        tp[0, r, c] += h
+        tm[0, r, c] -= h
+        sp, sm = O.Scene(**{**sc.__dict__, "tf": tp}), O.Scene(**{**sc.__dict__, "tf": tm})
+        fd = (loss(sp) - loss(sm)) / (2 * h)
+        assert abs(fd - g["adj_tf"][0, r, c]) <= 1e-5 * max(1.0, abs(fd)), (r, c)
+    for _ in range(6):
+        x, y, z = (int(rng.integers(0, n)) for n in sc.volume.shape[1:])
+        h = 1e-6
+        vp, vm = sc.volume.copy(), sc.volume.copy()
+        vp[0, x, y, z] += h
+        vm[0, x, y, z] -= h
+        fd = (loss(O.Scene(**{**sc.__dict__, "volume": vp})) - loss(O.Scene(**{**sc.__dict__, "volume": vm}))) / (2 * h)
+        assert abs(fd - g["adj_volume"][0, x, y, z]) <= 1e-5 * max(1.0, abs(fd)), (x, y, z)
+
+
+def test_port_matches_reference_all_modes(oracle_built):
+    """Direct restatement-vs-reference comparison (needs the reference sources)."""
+    O = oracle_built
+    if not O.reference_available():
+        pytest.skip("reference sources not present: the golden fixtures pin the oracle instead")
+    for i, (tfm, filt, blend, cam) in enumerate(all_mode_combos()):
+        case = make_case(500 + i, tf_mode=tfm, filter_mode=filt, blend_mode=blend, camera_mode=cam)
+        sc = case.oracle_scene()
+        c1, t1 = O.forward(sc, "port", "f64")
+        c2, t2 = O.forward(sc, "reference", "f64")
+        assert np.array_equal(t1, t2)
+        assert symmetric_error(c1, c2) <= 1e-12
+        adj = np.random.default_rng(i).normal(size=c1.shape)
+        req = O.AdjointRequest(volume=True, tf=True, camera=cam == 0, stepsize=True)
+        g1 = O.adjoint(sc, c2, t2, adj, req, "port", "f64")
+        g2 = O.adjoint(sc, c2, t2, adj, req, "reference", "f64")
+        for k in g1:
+            assert rel_l2(g1[k], g2[k]) <= 1e-12 or symmetric_error(g1[k], g2[k]) <= 1e-12, k
