@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--image", type=int, default=256)
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP32 comparison arm")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline budget")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
+    ap.add_argument("--interval", type=int, default=16, help="transmittance checkpoint interval (samples)")
     return ap.parse_args()
 
 
@@ -174,11 +176,12 @@ def run_gpu(args):
         return inp
 
     inp16 = inputs(vol16, tf, viewport)
-    slots = pr.Renderer.checkpoint_slots(inp16, 32)
+    K = args.interval
+    slots = pr.Renderer.checkpoint_slots(inp16, K)
     color = torch.empty(B, H, W, 4, device=dev)
     term = torch.empty(B, H, W, dtype=torch.int32, device=dev)
     ckpt = torch.empty(B, H, W, slots, device=dev)
-    out = pr.RendererOutputs(color, term, ckpt, 32)
+    out = pr.RendererOutputs(color, term, ckpt, K)
     adj_tf = torch.zeros_like(tf)
     adj = pr.AdjointOutputs()
     adj.has_tf_derivatives = True
@@ -344,7 +347,7 @@ def run_gpu(args):
     peak, peak_kind = measured_peaks()
     V = args.res ** 3
     P = B * H * W
-    ck_written = int(torch.clamp((term.to(torch.int64) - 1) // 32, min=0).clamp_max(slots).sum().item())
+    ck_written = int(torch.clamp((term.to(torch.int64) - 1) // K, min=0).clamp_max(slots).sum().item())
     fwd_bytes = V * 2 + P * (16 + 4) + ck_written * 4
     adj_bytes = V * 2 + P * (4 + 16) + ck_written * 4 + tf.numel() * 4 * 2
     dominant = ("adjoint", adj_bytes, adj_ms) if adj_ms >= fwd_ms else ("forward", fwd_bytes, fwd_ms)
@@ -370,7 +373,7 @@ def run_gpu(args):
         "data": "synthetic (seeded blobs + noise, random TF, Fibonacci views)",
         "config": {"workload": WORKLOAD, "volume_storage": "bf16", "tf_storage": "f32", "views": B,
                    "image": [H, W], "volume": [args.res] * 3, "samples_per_step": samples, "rays_hit": rays_hit,
-                   "checkpoint_interval": 32, "l2": "flushed (256 MB write) before every timed step",
+                   "checkpoint_interval": K, "l2": "flushed (256 MB write) before every timed step",
                    "graph": "forward+loss+adjoint captured in one CUDA graph",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": "samples/s", "h2d_bytes_per_step": int(h2d),
@@ -387,7 +390,7 @@ def run_gpu(args):
         "clocks": clock_summary,
     }
     if rank == 0:
-        result["cpu_baseline"] = cpu_baseline(w, args, samples / P)
+        result["cpu_baseline"] = None if args.no_cpu else cpu_baseline(w, args, samples / P)
         print(json.dumps(result))
     if world > 1:
         dist.barrier()

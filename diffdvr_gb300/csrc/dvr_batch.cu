@@ -184,13 +184,12 @@ cudaError_t launch_batched_adjoint(const RenderParams* ps, const AdjointParams* 
   const RenderParams* dt = reinterpret_cast<const RenderParams*>(static_cast<char*>(w.dev) + offs[0]);
   const AdjointParams* da = reinterpret_cast<const AdjointParams*>(static_cast<char*>(w.dev) + offs[1]);
   const int4* di = reinterpret_cast<const int4*>(static_cast<char*>(w.dev) + offs[2]);
-  const size_t entries = max_tf_entries(ps, n);
   const bool tg = as[0].has_tf != 0, vg = as[0].has_volume != 0;
-  bool any_ckpt = false;
-  for (int i = 0; i < n; ++i) any_ckpt |= ps[i].ckpt.p != nullptr;
-  size_t smem = entries * sizeof(float);
-  if (tg) smem += size_t(kFastThreads / 32) * entries * sizeof(float);
-  if (any_ckpt) smem += size_t(2) * kMaxSegment * kFastThreads * sizeof(float);
+  size_t smem = 0;
+  for (int i = 0; i < n; ++i) {
+    const int seg = ps[i].ckpt.p ? ps[i].ckpt_interval : 0;
+    smem = std::max(smem, fast_adjoint_smem(tf_mode, ps[i].R, ps[i].C, tg, seg));
+  }
   const int ni = int(items.size()), vst = ps[0].vol_storage;
   switch (tf_mode) {
     case 0: return adj_tf<0>(dt, da, di, ni, smem, vst, filter, blend, vg, tg, s);

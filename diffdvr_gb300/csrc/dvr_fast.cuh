@@ -18,10 +18,11 @@
 //    recovers the previous accumulator by dividing by (alpha - 1),
 //    renderer/renderer_blending.cuh:75-77, which is ill-conditioned as the
 //    opacity approaches 1);
-//  * TF gradients are accumulated per warp in shared memory and reduced into
-//    the output with one global atomic per TF entry and block; the volume
-//    gradient keeps the reference's per-cell register accumulation and issues
-//    its eight corner reductions on cell exit.
+//  * TF gradients are accumulated per thread in registers (see TfGradAccum),
+//    flushed to a per-warp copy in shared memory, and reduced into the output
+//    with one global atomic per TF entry and block; the volume gradient keeps
+//    the reference's per-cell register accumulation and issues its eight
+//    corner reductions on cell exit.
 //  * The step-size gradient is the full derivative (the reference keeps only
 //    the last blend contribution, renderer/renderer_kernels.cuh:393-395).
 #pragma once
@@ -30,7 +31,7 @@
 namespace dvr {
 
 constexpr int kTileW = 16, kTileH = 8, kFastThreads = 128;
-constexpr int kMaxSegment = 32;  // checkpoint interval capacity of the adjoint
+constexpr int kMaxSegment = 64;  // largest checkpoint interval
 
 // Maps thread -> pixel within a 16x8 tile: warp w covers an 8x4 patch.
 __device__ __forceinline__ void tile_pixel(int tid, int& px, int& py) {
@@ -198,23 +199,369 @@ __global__ void __launch_bounds__(kFastThreads) fast_forward_batched_kernel(cons
 }
 
 // ----------------------------------------------------------------- adjoint
-// Per-warp TF gradient accumulator in shared memory.
-struct TfSinkWarp {
-  float* p;
-  int C;
-  __device__ __forceinline__ void add(int r, int c, float v) { atomicAdd(p + r * C + c, v); }
-  __device__ __forceinline__ void add4(int r, f4 v) {
-    float* q = p + r * C;
-    atomicAdd(q + 0, v.x);
-    atomicAdd(q + 1, v.y);
-    atomicAdd(q + 2, v.z);
-    atomicAdd(q + 3, v.w);
+// TF-gradient accumulation.  Every adjoint sample adds to a few TF entries.
+// Adding each one to shared memory with atomics makes the 32 lanes of a warp,
+// whose rays see similar densities, collide on the same addresses, and float
+// atomics on shared memory serialise on conflicts.  So every lane owns its
+// accumulators and nothing is shared until the block ends:
+//  * identity (2 entries) and Gaussian with R <= kGaussRegs: registers, stored
+//    into the lane's shared-memory slots when the ray is done;
+//  * texture / linear (and larger Gaussian TFs): a register window over the
+//    few control points around the current density (RegWindow), flushed when
+//    the density leaves it into a private store of up to kLaneWin control
+//    points per lane in shared memory, laid out [slot][lane] so the accesses
+//    of a warp never share a bank.  For R <= kLaneWin it holds
+//    the whole TF; else it is a circular window over the control points near
+//    the current density, and a point that leaves the window (the density
+//    drifted by more than kLaneWin points along the ray) is added to the
+//    warp's shared copy.
+// At the end of the block all lane stores and warp copies are summed per
+// entry and added to the output with one global atomic per entry.
+constexpr int kLaneWin = 16;   // window of the lane stores (power of two)
+constexpr int kGaussRegs = 4;
+
+// Shared-memory layout of the adjoint block (offsets in floats), computed
+// identically on host and device.
+struct AdjointSmem {
+  int tf, warp, lane, lo, seg, total;
+  int slots;  // control points per lane store
+  __host__ __device__ static int slots_for(int tf_mode, int R) {
+    if (tf_mode == kTfIdentity) return 1;
+    return R <= kLaneWin ? R : kLaneWin;
+  }
+  __host__ __device__ AdjointSmem(int tf_mode, int R, int C, int threads, bool tfgrad, int seg_len) {
+    int o = 0;
+    tf = o;
+    o += (R * C + 3) & ~3;
+    slots = slots_for(tf_mode, R);
+    warp = o;
+    if (tfgrad) o += ((threads / 32) * R * C + 3) & ~3;
+    lane = o;
+    if (tfgrad) o += slots * C * threads;
+    lo = o;
+    if (tfgrad) o += threads;
+    seg = o;
+    o += 2 * seg_len * threads;
+    total = o;
   }
 };
-struct TfSinkNone {
-  __device__ __forceinline__ void add(int, int, float) {}
-  __device__ __forceinline__ void add4(int, f4) {}
+
+// A lane's private accumulators: C channels per control point, stored
+// [slot][lane] as float4 for channels 0-3 and [slot][k][lane] floats for the
+// extra channels (linear: position; Gaussian: mean, sigma).
+template <int C>
+struct LaneStore {
+  float* base;   // the block's lane-store region
+  int T, tid;
+  int slots;     // slots per lane
+  int R;
+  int lo = -1;   // first control point of the window; -1 = empty
+  __device__ __forceinline__ float4* q(int slot) const { return reinterpret_cast<float4*>(base) + slot * T + tid; }
+  __device__ __forceinline__ float* x(int slot, int k) const {
+    return base + 4 * slots * T + (slot * (C - 4) + k) * T + tid;
+  }
+  __device__ __forceinline__ bool windowed() const { return R > slots; }
+  __device__ __forceinline__ int slot_of(int t) const { return windowed() ? (t & (kLaneWin - 1)) : t; }
+  __device__ __forceinline__ void clear(int s) {
+    *q(s) = make_float4(0.f, 0.f, 0.f, 0.f);
+    if constexpr (C > 4) {
+#pragma unroll
+      for (int k = 0; k < C - 4; ++k) *x(s, k) = 0.f;
+    }
+  }
+  __device__ __forceinline__ void evict(int t, float* warp_copy) {
+    const int s = slot_of(t);
+    if (t >= 0 && t < R) {
+      const float4 v = *q(s);
+      float* g = warp_copy + t * C;
+      if (v.x != 0.f) atomicAdd(g + 0, v.x);
+      if (v.y != 0.f) atomicAdd(g + 1, v.y);
+      if (v.z != 0.f) atomicAdd(g + 2, v.z);
+      if (v.w != 0.f) atomicAdd(g + 3, v.w);
+      if constexpr (C > 4) {
+#pragma unroll
+        for (int k = 0; k < C - 4; ++k) {
+          const float e = *x(s, k);
+          if (e != 0.f) atomicAdd(g + 4 + k, e);
+        }
+      }
+    }
+    clear(s);
+  }
+  // makes control points [t0, t1] resident (window mode only)
+  __device__ __forceinline__ void ensure(int t0, int t1, float* warp_copy) {
+    if (!windowed()) return;
+    if (lo < 0) {
+      lo = max(0, min(t0 - kLaneWin / 2, R - kLaneWin));
+      return;
+    }
+    while (t1 >= lo + kLaneWin) {
+      evict(lo, warp_copy);
+      ++lo;
+    }
+    while (t0 < lo) {
+      --lo;
+      evict(lo + kLaneWin, warp_copy);
+    }
+  }
+  __device__ __forceinline__ void add(int t, f4 v, float e0 = 0.f, float e1 = 0.f) {
+    const int s = slot_of(t);
+    float4* p = q(s);
+    float4 a = *p;
+    a.x += v.x;
+    a.y += v.y;
+    a.z += v.z;
+    a.w += v.w;
+    *p = a;
+    if constexpr (C > 4) *x(s, 0) += e0;
+    if constexpr (C > 5) *x(s, 1) += e1;
+  }
+  __device__ __forceinline__ int window_lo() const { return windowed() ? max(lo, 0) : 0; }
 };
+
+// Register window in front of a lane store: kRegWin consecutive control
+// points around the current interval, re-centred when the density leaves it;
+// re-centring flushes the window into the lane store with independent
+// read-modify-writes (no dependency chain per sample).
+constexpr int kRegWin = 4;
+
+template <int C>
+struct RegWindow {
+  int base = -1;
+  float acc[kRegWin][C];
+  __device__ __forceinline__ void flush(LaneStore<C>& st, float* warp_copy) {
+    if (base < 0) return;
+    st.ensure(base, min(base + kRegWin - 1, st.R - 1), warp_copy);
+#pragma unroll
+    for (int w = 0; w < kRegWin; ++w) {
+      if (base + w < st.R) {
+        if constexpr (C == 4) st.add(base + w, mk4(acc[w][0], acc[w][1], acc[w][2], acc[w][3]));
+        else st.add(base + w, mk4(acc[w][0], acc[w][1], acc[w][2], acc[w][3]), acc[w][4]);
+      }
+    }
+    base = -1;
+  }
+  // adds k0 * v (+ e0 on channel 4) to point i0 and k1 * v (+ e1) to point i1
+  __device__ __forceinline__ void add(int i0, int i1, f4 v, float k0, float k1, float e0, float e1,
+                                      LaneStore<C>& st, float* warp_copy) {
+    if (base < 0 || i0 < base || i1 >= base + kRegWin) {
+      flush(st, warp_copy);
+      base = max(0, min(i0 - 1, st.R - kRegWin));
+#pragma unroll
+      for (int w = 0; w < kRegWin; ++w)
+#pragma unroll
+        for (int c = 0; c < C; ++c) acc[w][c] = 0.f;
+    }
+    const int o0 = i0 - base, o1 = i1 - base;
+#pragma unroll
+    for (int w = 0; w < kRegWin; ++w) {
+      const float k = (o0 == w ? k0 : 0.f) + (o1 == w ? k1 : 0.f);
+      acc[w][0] += v.x * k;
+      acc[w][1] += v.y * k;
+      acc[w][2] += v.z * k;
+      acc[w][3] += v.w * k;
+      if constexpr (C == 5) acc[w][4] += (o0 == w ? e0 : 0.f) + (o1 == w ? e1 : 0.f);
+    }
+  }
+};
+
+template <int TF, bool TFGRAD>
+struct TfGradAccum;
+
+template <bool TFGRAD>
+struct TfGradAccum<kTfIdentity, TFGRAD> {
+  float ga = 0.f, gc = 0.f;
+  __device__ __forceinline__ void bind(float*, int, int, int, int) {}
+  template <class A>
+  __device__ __forceinline__ float adjoint(const A& tf, float density, f4 adj, float*) {
+    const float dc = clampf(density, 0.f, 1.f);
+    const float sa = tf.at(0, 0), sc = tf.at(0, 1);
+    if constexpr (TFGRAD) {
+      ga += adj.w * dc;
+      gc += adj.x * dc + adj.y * dc + adj.z * dc;
+    }
+    const float adj_dc = (adj.x * sc + adj.y * sc + adj.z * sc) + adj.w * sa;
+    return (density > 0 && density < 1) ? adj_dc : 0.f;
+  }
+  // identity lane store: 2 floats [channel][lane]
+  __device__ __forceinline__ void finish(float* lane_base, int T, int tid, int* lo_out) {
+    if constexpr (TFGRAD) {
+      lane_base[tid] = ga;
+      lane_base[T + tid] = gc;
+      *lo_out = 0;
+    }
+  }
+};
+
+template <bool TFGRAD>
+struct TfGradAccum<kTfTexture, TFGRAD> {
+  LaneStore<4> st;
+  RegWindow<4> win;
+  float* warp_copy = nullptr;
+  __device__ __forceinline__ void bind(float* lane_base, int T, int tid, int slots, int R) {
+    st.base = lane_base;
+    st.T = T;
+    st.tid = tid;
+    st.slots = slots;
+    st.R = R;
+  }
+  template <class A>
+  __device__ __forceinline__ float adjoint(const A& tf, float density, f4 adj, float* wc) {
+    const int R = tf.R;
+    const float d = density * R - 0.5f;
+    const int di = int(floorf(d));
+    const float df = d - di;
+    const int i0 = clampi(di, 0, R - 1), i1 = clampi(di + 1, 0, R - 1);
+    const f4 a = tf.rgba(i0), c = tf.rgba(i1);
+    if constexpr (TFGRAD) {
+      warp_copy = wc;
+      win.add(i0, i1, adj, 1 - df, df, 0.f, 0.f, st, wc);
+    }
+    return dot4(adj, mk4(c.x - a.x, c.y - a.y, c.z - a.z, c.w - a.w)) * R;
+  }
+  __device__ __forceinline__ void finish(float*, int, int, int* lo_out) {
+    if constexpr (TFGRAD) {
+      win.flush(st, warp_copy);
+      *lo_out = st.window_lo();
+    }
+  }
+};
+
+template <bool TFGRAD>
+struct TfGradAccum<kTfLinear, TFGRAD> {
+  LaneStore<5> st;
+  RegWindow<5> win;
+  float* warp_copy = nullptr;
+  __device__ __forceinline__ void bind(float* lane_base, int T, int tid, int slots, int R) {
+    st.base = lane_base;
+    st.T = T;
+    st.tid = tid;
+    st.slots = slots;
+    st.R = R;
+  }
+  template <class A>
+  __device__ __forceinline__ float adjoint(const A& tf, float density, f4 adj, float* wc) {
+    const int i = linear_interval(tf, density);
+    const f4 a = tf.rgba(i), c = tf.rgba(i + 1);
+    const float p0 = tf.at(i, 4), p1 = tf.at(i + 1, 4);
+    const float d2 = clampf(density, p0, p1);
+    const float fr = (d2 - p0) / (p1 - p0);
+    const float adj_fr = dot4(adj, mk4(c.x - a.x, c.y - a.y, c.z - a.z, c.w - a.w));
+    if constexpr (TFGRAD) {
+      const float den = (p1 - p0) * (p1 - p0);
+      warp_copy = wc;
+      win.add(i, i + 1, adj, 1 - fr, fr, adj_fr * (d2 - p1) / den, adj_fr * (p0 - d2) / den, st, wc);
+    }
+    return adj_fr / (p1 - p0);
+  }
+  __device__ __forceinline__ void finish(float*, int, int, int* lo_out) {
+    if constexpr (TFGRAD) {
+      win.flush(st, warp_copy);
+      *lo_out = st.window_lo();
+    }
+  }
+};
+
+template <bool TFGRAD>
+struct TfGradAccum<kTfGaussian, TFGRAD> {
+  float acc[kGaussRegs][6];
+  LaneStore<6> st;
+  bool regs = true;
+  __device__ __forceinline__ void bind(float* lane_base, int T, int tid, int slots, int R) {
+#pragma unroll
+    for (int i = 0; i < kGaussRegs; ++i)
+#pragma unroll
+      for (int c = 0; c < 6; ++c) acc[i][c] = 0.f;
+    regs = R <= kGaussRegs;
+    st.base = lane_base;
+    st.T = T;
+    st.tid = tid;
+    st.slots = slots;
+    st.R = R;
+  }
+  template <class A>
+  __device__ __forceinline__ float adjoint(const A& tf, float density, f4 adj, float* warp_copy) {
+    float adj_density = 0;
+    for (int i = 0; i < tf.R; ++i) {
+      const f4 ci = tf.rgba(i);
+      const float mu = tf.at(i, 4), sigma = tf.at(i, 5);
+      const float s2 = sigma * sigma;
+      const float ni = gauss(density, mu, sigma);
+      const float f1 = (mu - density) / s2 * ni;
+      const float d1 = dot4(adj, mk4(ci.x * f1, ci.y * f1, ci.z * f1, ci.w * f1));
+      adj_density += d1;
+      if constexpr (TFGRAD) {
+        const float f2 = f1 * (mu - density) / sigma;
+        const float gs = dot4(adj, mk4(ci.x * f2, ci.y * f2, ci.z * f2, ci.w * f2));
+        const f4 gc = mk4(adj.x * ni, adj.y * ni, adj.z * ni, adj.w * ni);
+        if (regs) {
+#pragma unroll
+          for (int r = 0; r < kGaussRegs; ++r) {
+            if (r == i) {
+              acc[r][0] += gc.x;
+              acc[r][1] += gc.y;
+              acc[r][2] += gc.z;
+              acc[r][3] += gc.w;
+              acc[r][4] += -d1;
+              acc[r][5] += gs;
+            }
+          }
+        } else {
+          st.ensure(i, i, warp_copy);
+          st.add(i, gc, -d1, gs);
+        }
+      }
+    }
+    return adj_density;
+  }
+  __device__ __forceinline__ void finish(float*, int, int, int* lo_out) {
+    if constexpr (TFGRAD) {
+      if (regs) {
+#pragma unroll
+        for (int r = 0; r < kGaussRegs; ++r) {
+          if (r < st.R) {
+            *st.q(r) = make_float4(acc[r][0], acc[r][1], acc[r][2], acc[r][3]);
+            *st.x(r, 0) = acc[r][4];
+            *st.x(r, 1) = acc[r][5];
+          }
+        }
+      }
+      *lo_out = st.window_lo();
+    }
+  }
+};
+
+// Sums the lane stores and warp copies of the block into the output TF
+// gradient (one global atomic per entry).
+template <int TF>
+__device__ __forceinline__ void reduce_tf_grad(const AdjointSmem& L, const float* smem, int R, float* out,
+                                               int64_t sb, int64_t sr, int64_t sc, int b) {
+  constexpr int C = TfChannels<TF>::C;
+  const int T = blockDim.x;
+  const int n = R * C;
+  const float* lane = smem + L.lane;
+  const int* lo = reinterpret_cast<const int*>(smem + L.lo);
+  const float* warp = smem + L.warp;
+  const bool window = TF != kTfIdentity && R > L.slots;
+  for (int e = threadIdx.x; e < n; e += T) {
+    const int t = e / C, c = e - t * C;
+    float v = 0.f;
+    for (int w = 0; w < T / 32; ++w) v += warp[w * n + e];
+    if constexpr (TF == kTfIdentity) {
+      for (int l = 0; l < T; ++l) v += lane[c * T + l];
+    } else {
+      const int slot = window ? (t & (kLaneWin - 1)) : t;
+      for (int l = 0; l < T; ++l) {
+        if (window) {
+          const int l0 = lo[l];
+          if (t < l0 || t >= l0 + kLaneWin) continue;
+        }
+        v += c < 4 ? lane[(slot * T + l) * 4 + c] : lane[4 * L.slots * T + (slot * (C - 4) + (c - 4)) * T + l];
+      }
+    }
+    if (v != 0.f) atomicAdd(out + b * sb + t * sr + c * sc, v);
+  }
+}
 
 // Volume-gradient accumulator for the current cell (reference scheme).
 template <int FILTER, bool VOLGRAD>
@@ -251,9 +598,10 @@ struct VolGradCell {
 
 // One reverse step shared by both adjoint variants.  Returns the step's
 // position-chain contribution to d(loss)/d(step) via adj_step.
-template <int FILTER, int TF, int BLEND, bool VOLGRAD, bool TFGRAD, typename VT, class A, class Sink>
+template <int FILTER, int TF, int BLEND, bool VOLGRAD, bool TFGRAD, typename VT, class A>
 __device__ __forceinline__ void fast_reverse_step(const RenderParams& p, const AdjointParams& a, const FastRay& r,
-                                                  const VolumeFast<VT>& vol, const A& tf, Sink& sink,
+                                                  const VolumeFast<VT>& vol, const A& tf,
+                                                  TfGradAccum<TF, TFGRAD>& tacc, float* s_grad_warp,
                                                   Sampler<FILTER, VT>& smp, VolGradCell<FILTER, VOLGRAD>& vg,
                                                   float* adjv, int k, float density, float alpha_in, f4& adj_acc,
                                                   f3& adj_start, f3& adj_dir, float& adj_step, bool need_pos_grad) {
@@ -262,7 +610,7 @@ __device__ __forceinline__ void fast_reverse_step(const RenderParams& p, const A
   const float alpha = blend_alpha<BLEND>(cur.w, r.step);
   f4 adj_cur;
   adj_step += blend_adjoint_core<BLEND>(alpha_in, cur, r.step, alpha, adj_acc, adj_cur);
-  const float adj_density = tf_adjoint<TF, TFGRAD>(tf, density, adj_cur, sink);
+  const float adj_density = tacc.adjoint(tf, density, adj_cur, s_grad_warp);
   if (!VOLGRAD && !need_pos_grad) return;
   const float3 q = fast_pos(r, t);
   if constexpr (FILTER == kNearest) {
@@ -309,25 +657,35 @@ __device__ __forceinline__ void fast_reverse_step(const RenderParams& p, const A
 
 template <int FILTER, int TF, int BLEND, bool VOLGRAD, bool TFGRAD, typename VT>
 __device__ __forceinline__ void fast_adjoint_tile(const RenderParams& p, const AdjointParams& a, int b, int tx, int ty,
-                                                  float* s_tf, float* s_grad, float* s_seg) {
+                                                  float* s_tf, float* s_grad, float* s_lane, int s_lane_slots,
+                                                  int* s_lo, float* s_seg) {
   constexpr int C = TfChannels<TF>::C;
+  constexpr unsigned kFull = 0xffffffffu;
   int px, py;
   tile_pixel(threadIdx.x, px, py);
   const int x = tx * kTileW + px, y = ty * kTileH + py;
-  if (x >= p.W || y >= p.H) return;
-  FastRay r;
-  fast_setup(p, x, y, b, r);
+  // every lane stays in the loops below (pixels outside the image have no
+  // samples) so that the warp can reconverge explicitly after each step
+  const bool valid = x < p.W && y < p.H;
+  FastRay r{};
+  if (valid) fast_setup(p, x, y, b, r);
   VolumeFast<VT> vol{static_cast<const VT*>(p.volume.p) + b * p.volume.s[0], int(p.volume.s[1]), int(p.volume.s[2]),
                      int(p.volume.s[3]), p.X - 1, p.Y - 1, p.Z - 1};
   const TfShared<C> tf{s_tf, p.R};
-  TfSinkWarp sink{s_grad + (threadIdx.x >> 5) * p.R * C, C};
+  float* s_grad_warp = s_grad + (threadIdx.x >> 5) * p.R * C;
+  TfGradAccum<TF, TFGRAD> tacc;
+  tacc.bind(s_lane, int(blockDim.x), int(threadIdx.x), s_lane_slots, p.R);
   float* adjv = VOLGRAD ? static_cast<float*>(a.adj_volume.p) + b * a.adj_volume.s[0] : nullptr;
   const bool need_pos = a.has_camera || a.has_stepsize;
 
-  const int n = static_cast<const int*>(a.fwd_term.p)[b * a.fwd_term.s[0] + y * a.fwd_term.s[1] + x * a.fwd_term.s[2]];
-  const float* ac = static_cast<const float*>(a.adj_color.p) + b * a.adj_color.s[0] + y * a.adj_color.s[1] +
-                    x * a.adj_color.s[2];
-  f4 adj_acc = mk4(ac[0], ac[a.adj_color.s[3]], ac[2 * a.adj_color.s[3]], ac[3 * a.adj_color.s[3]]);
+  int n = 0;
+  f4 adj_acc = mk4(0, 0, 0, 0);
+  if (valid) {
+    n = static_cast<const int*>(a.fwd_term.p)[b * a.fwd_term.s[0] + y * a.fwd_term.s[1] + x * a.fwd_term.s[2]];
+    const float* ac = static_cast<const float*>(a.adj_color.p) + b * a.adj_color.s[0] + y * a.adj_color.s[1] +
+                      x * a.adj_color.s[2];
+    adj_acc = mk4(ac[0], ac[a.adj_color.s[3]], ac[2 * a.adj_color.s[3]], ac[3 * a.adj_color.s[3]]);
+  }
   float adj_step = 0;
   f3 adj_start = mk3(0, 0, 0), adj_dir = mk3(0, 0, 0);
   Sampler<FILTER, VT> smp;
@@ -335,64 +693,74 @@ __device__ __forceinline__ void fast_adjoint_tile(const RenderParams& p, const A
   vg.reset();
 
   const int K = p.ckpt_interval;
-  const bool ckpt_ok = p.ckpt.p != nullptr && K <= kMaxSegment && n <= (p.ckpt_slots + 1) * K;
-  if (ckpt_ok) {
-    const float* ck = static_cast<const float*>(p.ckpt.p) + b * p.ckpt.s[0] + y * p.ckpt.s[1] + x * p.ckpt.s[2];
-    float* seg_d = s_seg + threadIdx.x;                     // [j][thread]
-    float* seg_a = s_seg + kMaxSegment * blockDim.x + threadIdx.x;
-    const int nseg = (n + K - 1) / K;
-    for (int j = nseg - 1; j >= 0; --j) {
-      const int k0 = j * K, k1 = min(n, k0 + K);
-      // re-march the segment from its checkpoint
-      float alpha = j == 0 ? 0.f : ck[(j - 1) * p.ckpt.s[3]];
-      for (int k = k0; k < k1; ++k) {
+  const bool ckpt_ok = valid && p.ckpt.p != nullptr && n <= (p.ckpt_slots + 1) * K;
+  // checkpointed rays: segments [jK, (j+1)K) from last to first, all lanes on
+  // the same segment index and sample offset (predicated per lane)
+  const int nseg = ckpt_ok ? (n + K - 1) / K : 0;
+  const int nseg_max = int(__reduce_max_sync(kFull, unsigned(nseg)));
+  const float* ck = ckpt_ok ? static_cast<const float*>(p.ckpt.p) + b * p.ckpt.s[0] + y * p.ckpt.s[1] +
+                                  x * p.ckpt.s[2]
+                            : nullptr;
+  float* seg_d = s_seg + threadIdx.x;  // [offset][thread]
+  float* seg_a = s_seg + K * blockDim.x + threadIdx.x;
+  for (int j = nseg_max - 1; j >= 0; --j) {
+    const int k0 = j * K;
+    const int k1 = j < nseg ? min(n, k0 + K) : k0;
+    // re-march the segment from its checkpoint
+    float alpha = (j > 0 && j < nseg) ? ck[(j - 1) * p.ckpt.s[3]] : 0.f;
+    for (int kk = 0; kk < K; ++kk) {
+      const int k = k0 + kk;
+      if (k < k1) {
         const float t = r.tmin + k * r.step;
         const float density = smp.sample(vol, fast_pos(r, t));
         const float a_k = blend_alpha<BLEND>(tf_eval<TF>(tf, density).w, r.step);
-        seg_d[(k - k0) * blockDim.x] = density;
-        seg_a[(k - k0) * blockDim.x] = alpha;
+        seg_d[kk * blockDim.x] = density;
+        seg_a[kk * blockDim.x] = alpha;
         alpha = alpha + (1 - alpha) * a_k;
       }
-      for (int k = k1 - 1; k >= k0; --k) {
-        const float density = seg_d[(k - k0) * blockDim.x];
-        const float alpha_in = seg_a[(k - k0) * blockDim.x];
-        if constexpr (TFGRAD) {
-          fast_reverse_step<FILTER, TF, BLEND, VOLGRAD, TFGRAD, VT>(p, a, r, vol, tf, sink, smp, vg, adjv, k, density,
-                                                                    alpha_in, adj_acc, adj_start, adj_dir, adj_step,
-                                                                    need_pos);
-        } else {
-          TfSinkNone none;
-          fast_reverse_step<FILTER, TF, BLEND, VOLGRAD, TFGRAD, VT>(p, a, r, vol, tf, none, smp, vg, adjv, k, density,
-                                                                    alpha_in, adj_acc, adj_start, adj_dir, adj_step,
-                                                                    need_pos);
-        }
-      }
+      __syncwarp();
     }
-  } else {
-    // no checkpoints: recover the accumulator by inverting the blend, as the reference
-    const float* fc = static_cast<const float*>(a.fwd_color.p) + b * a.fwd_color.s[0] + y * a.fwd_color.s[1] +
-                      x * a.fwd_color.s[2];
-    float alpha_out = fc[3 * a.fwd_color.s[3]];
-    for (int k = n - 1; k >= 0; --k) {
-      const float t = r.tmin + k * r.step;
-      const float density = smp.sample(vol, fast_pos(r, t));
-      const float a_k = blend_alpha<BLEND>(tf_eval<TF>(tf, density).w, r.step);
-      const float a_inv = BLEND == kAlphaBlend ? rminf(1.0f - 1e-5f, a_k) : a_k;
-      const float alpha_in = (a_inv - alpha_out) / (a_inv - 1);
-      if constexpr (TFGRAD) {
-        fast_reverse_step<FILTER, TF, BLEND, VOLGRAD, TFGRAD, VT>(p, a, r, vol, tf, sink, smp, vg, adjv, k, density,
-                                                                  alpha_in, adj_acc, adj_start, adj_dir, adj_step,
-                                                                  need_pos);
-      } else {
-        TfSinkNone none;
-        fast_reverse_step<FILTER, TF, BLEND, VOLGRAD, TFGRAD, VT>(p, a, r, vol, tf, none, smp, vg, adjv, k, density,
-                                                                  alpha_in, adj_acc, adj_start, adj_dir, adj_step,
-                                                                  need_pos);
+    for (int kk = K - 1; kk >= 0; --kk) {
+      const int k = k0 + kk;
+      if (k < k1) {
+        const float density = seg_d[kk * blockDim.x];
+        const float alpha_in = seg_a[kk * blockDim.x];
+        fast_reverse_step<FILTER, TF, BLEND, VOLGRAD, TFGRAD, VT>(p, a, r, vol, tf, tacc, s_grad_warp, smp, vg, adjv,
+                                                                  k, density, alpha_in, adj_acc, adj_start, adj_dir,
+                                                                  adj_step, need_pos);
       }
-      alpha_out = alpha_in;
+      __syncwarp();
+    }
+  }
+  // rays without checkpoints: recover the accumulator by inverting the blend,
+  // as the reference
+  const int ninv = (valid && !ckpt_ok) ? n : 0;
+  const int ninv_max = int(__reduce_max_sync(kFull, unsigned(ninv)));
+  if (ninv_max > 0) {
+    float alpha_out = 0.f;
+    if (ninv > 0) {
+      const float* fc = static_cast<const float*>(a.fwd_color.p) + b * a.fwd_color.s[0] + y * a.fwd_color.s[1] +
+                        x * a.fwd_color.s[2];
+      alpha_out = fc[3 * a.fwd_color.s[3]];
+    }
+    for (int k = ninv_max - 1; k >= 0; --k) {
+      if (k < ninv) {
+        const float t = r.tmin + k * r.step;
+        const float density = smp.sample(vol, fast_pos(r, t));
+        const float a_k = blend_alpha<BLEND>(tf_eval<TF>(tf, density).w, r.step);
+        const float a_inv = BLEND == kAlphaBlend ? rminf(1.0f - 1e-5f, a_k) : a_k;
+        const float alpha_in = (a_inv - alpha_out) / (a_inv - 1);
+        fast_reverse_step<FILTER, TF, BLEND, VOLGRAD, TFGRAD, VT>(p, a, r, vol, tf, tacc, s_grad_warp, smp, vg, adjv,
+                                                                  k, density, alpha_in, adj_acc, adj_start, adj_dir,
+                                                                  adj_step, need_pos);
+        alpha_out = alpha_in;
+      }
+      __syncwarp();
     }
   }
   vg.flush(adjv, a.adj_volume, p.X - 1, p.Y - 1, p.Z - 1);
+  tacc.finish(s_lane, int(blockDim.x), int(threadIdx.x), s_lo + threadIdx.x);
+  if (!valid) return;
 
   if (a.has_stepsize) {
     float* ps = static_cast<float*>(a.adj_step.p) + b * a.adj_step.s[0] + y * a.adj_step.s[1] + x * a.adj_step.s[2];
@@ -417,13 +785,9 @@ __device__ __forceinline__ void fast_adjoint_tile(const RenderParams& p, const A
   }
 }
 
-// Shared memory of the adjoint block: TF (R*C) | per-warp TF gradients
-// (4 * R*C) | segment buffers (2 * kMaxSegment * threads).
-__host__ __device__ inline size_t fast_adjoint_smem(int R, int C, bool tfgrad, bool ckpt) {
-  size_t n = size_t(R) * C;
-  if (tfgrad) n += size_t(kFastThreads / 32) * R * C;
-  if (ckpt) n += size_t(2) * kMaxSegment * kFastThreads;
-  return n * sizeof(float);
+// Shared memory of the adjoint block, in bytes.
+__host__ __device__ inline size_t fast_adjoint_smem(int tf_mode, int R, int C, bool tfgrad, int seg_len) {
+  return size_t(AdjointSmem(tf_mode, R, C, kFastThreads, tfgrad, seg_len).total) * sizeof(float);
 }
 
 template <int FILTER, int TF, int BLEND, bool VOLGRAD, bool TFGRAD, typename VT>
@@ -431,26 +795,23 @@ __device__ __forceinline__ void fast_adjoint_block(const RenderParams& p, const 
                                                    int ty) {
   extern __shared__ float4 fast_smem4[];
   constexpr int C = TfChannels<TF>::C;
-  float* s_tf = reinterpret_cast<float*>(fast_smem4);
-  float* s_grad = s_tf + p.R * C;
-  float* s_seg = s_grad + (TFGRAD ? (kFastThreads / 32) * p.R * C : 0);
-  stage_tf(p, b, s_tf);
+  float* smem = reinterpret_cast<float*>(fast_smem4);
+  const int seg_len = p.ckpt.p ? p.ckpt_interval : 0;
+  const AdjointSmem L(TF, p.R, C, int(blockDim.x), TFGRAD, seg_len);
+  float* s_grad = smem + L.warp;
+  stage_tf(p, b, smem + L.tf);
   if constexpr (TFGRAD) {
-    for (int e = threadIdx.x; e < (kFastThreads / 32) * p.R * C; e += blockDim.x) s_grad[e] = 0.f;
+    // warp copies, lane stores and window bases start at zero
+    for (int e = threadIdx.x; e < L.seg - L.warp; e += blockDim.x) s_grad[e] = 0.f;
   }
   __syncthreads();
-  fast_adjoint_tile<FILTER, TF, BLEND, VOLGRAD, TFGRAD, VT>(p, a, b, tx, ty, s_tf, s_grad, s_seg);
+  fast_adjoint_tile<FILTER, TF, BLEND, VOLGRAD, TFGRAD, VT>(p, a, b, tx, ty, smem + L.tf, s_grad, smem + L.lane,
+                                                            L.slots, reinterpret_cast<int*>(smem + L.lo),
+                                                            smem + L.seg);
   if constexpr (TFGRAD) {
     __syncthreads();
-    const int n = p.R * C;
-    float* g = static_cast<float*>(a.adj_tf.p) + b * a.adj_tf.s[0];
-    for (int e = threadIdx.x; e < n; e += blockDim.x) {
-      float v = 0.f;
-#pragma unroll
-      for (int w = 0; w < kFastThreads / 32; ++w) v += s_grad[w * n + e];
-      const int rr = e / C, cc = e - rr * C;
-      if (v != 0.f) atomicAdd(g + rr * a.adj_tf.s[1] + cc * a.adj_tf.s[2], v);
-    }
+    reduce_tf_grad<TF>(L, smem, p.R, static_cast<float*>(a.adj_tf.p), a.adj_tf.s[0], a.adj_tf.s[1], a.adj_tf.s[2],
+                       b);
   }
 }
 

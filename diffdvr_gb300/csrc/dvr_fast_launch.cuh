@@ -107,7 +107,7 @@ static cudaError_t fast_adjoint_go(const RenderParams& p, const AdjointParams& a
   if (blocks > 0x7fffffff) return cudaErrorInvalidConfiguration;
   constexpr int C = TfChannels<TF>::C;
   const bool tfgrad = a.has_tf != 0, volgrad = a.has_volume != 0;
-  const size_t smem = fast_adjoint_smem(p.R, C, tfgrad, p.ckpt.p != nullptr);
+  const size_t smem = fast_adjoint_smem(TF, p.R, C, tfgrad, p.ckpt.p ? p.ckpt_interval : 0);
   auto go = [&](auto kernel) {
     if (smem > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));

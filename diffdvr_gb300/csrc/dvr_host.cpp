@@ -4,7 +4,7 @@
 // adjoint), flattens them into kernel parameter blocks and dispatches to the
 // kernel families.  C++ internally, plain C at the boundary: nothing throws
 // across it.
-#include "../../include/diffdvr_gb300.h"
+#include "diffdvr_gb300.h"
 
 #include <cuda_runtime.h>
 
@@ -382,6 +382,9 @@ void check_outputs(const DvrRendererOutputs& out, Checked& c, bool forward) {
     if (ck.sizes[3] < 1) fail(DVR_E_INVALID_ARGUMENT, "checkpoints must hold at least one slot per ray");
     if (p.ckpt_interval < 1 || p.ckpt_interval > 64)
       fail(DVR_E_INVALID_ARGUMENT, "checkpoint_interval must be in [1, 64]");
+    // the adjoint keeps one segment per thread in shared memory
+    if (p.ckpt_interval > 32 && p.R * p.C > 1024)
+      fail(DVR_E_INVALID_ARGUMENT, "checkpoint_interval above 32 needs a TF with at most 1024 entries");
     p.ckpt = out_view(ck, false);
     p.ckpt_slots = int(ck.sizes[3]);
   }

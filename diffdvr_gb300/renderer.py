@@ -143,7 +143,7 @@ class Renderer(nn.Module):
 
     def __init__(self, settings: Optional[pyrenderer.RendererInputs] = None, optimize_camera=False,
                  optimize_tf=False, optimize_volume=False, gradient_method="adjoint",
-                 forward_delayed_gradients=False, tf_delayed_accumulation=True, checkpoint_interval: int = 32):
+                 forward_delayed_gradients=False, tf_delayed_accumulation=True, checkpoint_interval: int = 16):
         super().__init__()
         self._settings = settings if settings is not None else pyrenderer.RendererInputs()
         self._optimize_camera = optimize_camera
