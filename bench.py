@@ -133,7 +133,7 @@ def measured_peaks():
 
 def profiled_traffic():
     """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "roofline_traffic.json")
+    p = os.path.join(ROOT, "profiles", "roofline_traffic.txt")
     if os.path.exists(p):
         with open(p) as f:
             return json.load(f)

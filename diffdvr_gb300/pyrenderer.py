@@ -153,7 +153,7 @@ class RendererOutputs:
     ``Renderer.checkpoint_slots``."""
 
     def __init__(self, color: Optional[torch.Tensor] = None, terminationIndex: Optional[torch.Tensor] = None,
-                 checkpoints: Optional[torch.Tensor] = None, checkpoint_interval: int = 32):
+                 checkpoints: Optional[torch.Tensor] = None, checkpoint_interval: int = 16):
         self.color = color
         self.terminationIndex = terminationIndex
         self.checkpoints = checkpoints
@@ -263,7 +263,7 @@ def _outputs(out: RendererOutputs) -> _abi.DvrRendererOutputs:
     c.color = _tensor(out.color, "color")
     c.termination_index = _tensor(out.terminationIndex, "terminationIndex")
     c.checkpoints = _tensor(getattr(out, "checkpoints", None), "checkpoints")
-    c.checkpoint_interval = int(getattr(out, "checkpoint_interval", 32) or 32)
+    c.checkpoint_interval = int(getattr(out, "checkpoint_interval", 16) or 16)
     return c
 
 
@@ -338,7 +338,7 @@ class Renderer:
         _abi.check(lib.dvr_render_adjoint_batched(ci, co, ca, cg, n, stream))
 
     @staticmethod
-    def checkpoint_slots(inputs: RendererInputs, interval: int = 32) -> int:
+    def checkpoint_slots(inputs: RendererInputs, interval: int = 16) -> int:
         """Checkpoint slots per ray for RendererOutputs.checkpoints: from the
         box diagonal and the smallest step size."""
         bs = inputs.box_size

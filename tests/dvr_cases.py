@@ -157,7 +157,7 @@ def golden_prefixes(g: dict) -> list:
 
 # ---------------------------------------------------------------- GPU runs
 def gpu_forward(case: Case, family: str = "optimized", volume_dtype=None, tf_dtype=None, checkpoints: bool = False,
-                interval: int = 32):
+                interval: int = 16):
     """Renders case on cuda:0; returns (inputs, outputs) with torch tensors."""
     import torch
     from diffdvr_gb300 import pyrenderer as pr

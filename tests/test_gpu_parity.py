@@ -129,9 +129,9 @@ def reference_adjoint(case, O, gpu_term, adj, req, oracle_case=None):
     return O.adjoint(sc, c64, t64, adj, req, "port", "f64"), adj
 
 
-def _adjoint_case(case, family, O, checkpoints, stepsize):
+def _adjoint_case(case, family, O, checkpoints, stepsize, interval=16):
     cam = case.camera_mode == 0
-    inp, out = gpu_forward(case, family, checkpoints=checkpoints)
+    inp, out = gpu_forward(case, family, checkpoints=checkpoints, interval=interval)
     term = out.terminationIndex.cpu().numpy()
     adj = np.random.default_rng(7).normal(size=out.color.shape).astype(np.float32)
     req = O.AdjointRequest(volume=True, tf=True, camera=cam, stepsize=stepsize)
@@ -145,8 +145,9 @@ def _adjoint_case(case, family, O, checkpoints, stepsize):
     return got, ref, r32
 
 
-@pytest.mark.parametrize("family,checkpoints", [("plain", False), ("optimized", False), ("optimized", True)])
-def test_adjoint_all_modes(family, checkpoints, oracle_built, cuda_device):
+@pytest.mark.parametrize("family,checkpoints,interval", [("plain", False, 16), ("optimized", False, 16),
+                                                         ("optimized", True, 16), ("optimized", True, 5)])
+def test_adjoint_all_modes(family, checkpoints, interval, oracle_built, cuda_device):
     O = oracle_built
     failures = {}
     for i, (tfm, filt, blend, cam) in enumerate(all_mode_combos()):
@@ -154,7 +155,7 @@ def test_adjoint_all_modes(family, checkpoints, oracle_built, cuda_device):
                          pad_faces=True)
         # the optimized family returns the full step-size derivative, the
         # reference (and the oracle) only the last blend term; checked by FD below
-        got, ref, r32 = _adjoint_case(case, family, O, checkpoints, stepsize=(family == "plain"))
+        got, ref, r32 = _adjoint_case(case, family, O, checkpoints, stepsize=(family == "plain"), interval=interval)
         bad = _grad_errors(got, ref, r32)
         if bad:
             failures[(tfm, filt, blend, cam)] = bad
