@@ -143,7 +143,66 @@ cudaError_t adj_tf(const RenderParams* t, const AdjointParams* at, const int4* i
   }
 }
 
+std::mutex g_counter_mutex;
+int* g_counters[64] = {};
+unsigned g_counter_next[64] = {};
+constexpr unsigned kCounters = 4096;
+
+struct ScratchSlot {
+  int device = -1;
+  cudaStream_t stream = nullptr;
+  void* ptr = nullptr;
+  size_t bytes = 0;
+};
+std::mutex g_scratch_mutex;
+std::vector<ScratchSlot> g_scratch;
+
 }  // namespace
+
+void* acquire_scratch(int device, cudaStream_t s, size_t bytes, cudaError_t& err) {
+  err = cudaSuccess;
+  std::lock_guard<std::mutex> lock(g_scratch_mutex);
+  ScratchSlot* slot = nullptr;
+  for (auto& e : g_scratch)
+    if (e.device == device && e.stream == s) slot = &e;
+  if (!slot) {
+    g_scratch.push_back(ScratchSlot{device, s, nullptr, 0});
+    slot = &g_scratch.back();
+  }
+  if (slot->bytes < bytes) {
+    if (slot->ptr) {
+      // earlier launches on this stream may still use the old buffer
+      err = cudaStreamSynchronize(s);
+      if (err != cudaSuccess) return nullptr;
+      cudaFree(slot->ptr);
+      slot->ptr = nullptr;
+      slot->bytes = 0;
+    }
+    const size_t want = std::max(bytes, size_t(1) << 20);
+    err = cudaMalloc(&slot->ptr, want);
+    if (err != cudaSuccess) return nullptr;
+    slot->bytes = want;
+  }
+  return slot->ptr;
+}
+
+int* acquire_counter(int device, cudaStream_t s, cudaError_t& err) {
+  err = cudaSuccess;
+  int* c = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_counter_mutex);
+    const int d = device & 63;
+    if (!g_counters[d]) {
+      err = cudaMalloc(&g_counters[d], kCounters * sizeof(int));
+      if (err != cudaSuccess) return nullptr;
+    }
+    // launches in flight at the same time get different counters as long as
+    // fewer than kCounters of them overlap
+    c = g_counters[d] + (g_counter_next[d]++ % kCounters);
+  }
+  err = cudaMemsetAsync(c, 0, sizeof(int), s);
+  return err == cudaSuccess ? c : nullptr;
+}
 
 cudaError_t launch_batched_forward(const RenderParams* ps, int n, int filter, int tf_mode, int blend, int device,
                                    const LaunchInfo&, cudaStream_t s) {

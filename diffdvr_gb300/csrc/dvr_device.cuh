@@ -110,6 +110,17 @@ __device__ __forceinline__ void setup_ray(const RenderParams& p, int x, int y, i
   r.tmin = rmaxf(r.tmin, 0.f);
 }
 
+// Upper bound on the samples of a ray, so every march terminates: the
+// reference's loop (renderer/renderer_kernels.cuh:60-64) would not for a NaN
+// exit distance or a non-positive step, and float(k) stops growing past 2^24.
+// Such rays get no samples; regular rays stop at t > tmax long before the bound.
+constexpr int kMaxSamplesPerRay = 1 << 24;
+__device__ __forceinline__ int max_samples(float tmin, float tmax, float step) {
+  if (!(step > 0.f) || !(tmax >= tmin)) return 0;
+  const float n = floorf((tmax - tmin) / step) + 3.f;
+  return n < float(kMaxSamplesPerRay) ? int(n) : kMaxSamplesPerRay;
+}
+
 __device__ __forceinline__ f3 volume_pos(const Ray& r, float t) {
   const f3 w = mk3(r.start.x + t * r.dir.x, r.start.y + t * r.dir.y, r.start.z + t * r.dir.z);
   return mk3((w.x - r.bmin.x) / r.voxel.x, (w.y - r.bmin.y) / r.voxel.y, (w.z - r.bmin.z) / r.voxel.z);

@@ -149,8 +149,9 @@ __device__ __forceinline__ void fast_forward_tile(const RenderParams& p, int b, 
   float* ck = p.ckpt.p ? static_cast<float*>(p.ckpt.p) + b * p.ckpt.s[0] + y * p.ckpt.s[1] + x * p.ckpt.s[2] : nullptr;
   const int K = p.ckpt_interval;
   int next_ck = K, slot = 0;
+  const int kmax = max_samples(r.tmin, r.tmax, r.step);
   int k;
-  for (k = 0;; ++k) {
+  for (k = 0; k < kmax; ++k) {
     const float t = r.tmin + k * r.step;
     if (t > r.tmax) break;
     if (acc.w > p.early_out) break;
@@ -206,9 +207,9 @@ __global__ void __launch_bounds__(kFastThreads) fast_forward_batched_kernel(cons
 // accumulators and nothing is shared until the block ends:
 //  * identity (2 entries) and Gaussian with R <= kGaussRegs: registers, stored
 //    into the lane's shared-memory slots when the ray is done;
-//  * texture / linear (and larger Gaussian TFs): a register window over the
-//    few control points around the current density (RegWindow), flushed when
-//    the density leaves it into a private store of up to kLaneWin control
+//  * texture / linear (and larger Gaussian TFs): registers for the two
+//    control points of the current interval (PairCache), added when the
+//    density leaves them into a private store of up to kLaneWin control
 //    points per lane in shared memory, laid out [slot][lane] so the accesses
 //    of a warp never share a bank.  For R <= kLaneWin it holds
 //    the whole TF; else it is a circular window over the control points near
@@ -229,10 +230,11 @@ struct AdjointSmem {
     if (tf_mode == kTfIdentity) return 1;
     return R <= kLaneWin ? R : kLaneWin;
   }
-  __host__ __device__ AdjointSmem(int tf_mode, int R, int C, int threads, bool tfgrad, int seg_len) {
+  __host__ __device__ AdjointSmem(int tf_mode, int R, int C, int threads, bool tfgrad, int seg_len,
+                                  int tf_copies = 1) {
     int o = 0;
     tf = o;
-    o += (R * C + 3) & ~3;
+    o += (tf_copies * R * C + 3) & ~3;
     slots = slots_for(tf_mode, R);
     warp = o;
     if (tfgrad) o += ((threads / 32) * R * C + 3) & ~3;
@@ -269,24 +271,49 @@ struct LaneStore {
       for (int k = 0; k < C - 4; ++k) *x(s, k) = 0.f;
     }
   }
+  // where evicted control points go: the warp's dense R*C copy in shared
+  // memory, or (per-batch TF gradients) the global output with its strides
+  float* ev_base = nullptr;
+  int64_t ev_sr = C, ev_sc = 1;
+  __device__ __forceinline__ void add_to(float* g, int64_t sr, int64_t sc, int t, int s) const {
+    const float4 v = *q(s);
+    float* e = g + t * sr;
+    if (v.x != 0.f) atomicAdd(e, v.x);
+    if (v.y != 0.f) atomicAdd(e + sc, v.y);
+    if (v.z != 0.f) atomicAdd(e + 2 * sc, v.z);
+    if (v.w != 0.f) atomicAdd(e + 3 * sc, v.w);
+    if constexpr (C > 4) {
+#pragma unroll
+      for (int k = 0; k < C - 4; ++k) {
+        const float xv = *x(s, k);
+        if (xv != 0.f) atomicAdd(e + (4 + k) * sc, xv);
+      }
+    }
+  }
   __device__ __forceinline__ void evict(int t, float* warp_copy) {
     const int s = slot_of(t);
     if (t >= 0 && t < R) {
-      const float4 v = *q(s);
-      float* g = warp_copy + t * C;
-      if (v.x != 0.f) atomicAdd(g + 0, v.x);
-      if (v.y != 0.f) atomicAdd(g + 1, v.y);
-      if (v.z != 0.f) atomicAdd(g + 2, v.z);
-      if (v.w != 0.f) atomicAdd(g + 3, v.w);
-      if constexpr (C > 4) {
-#pragma unroll
-        for (int k = 0; k < C - 4; ++k) {
-          const float e = *x(s, k);
-          if (e != 0.f) atomicAdd(g + 4 + k, e);
-        }
-      }
+      if (ev_base) add_to(ev_base, ev_sr, ev_sc, t, s);
+      else add_to(warp_copy, C, 1, t, s);
     }
     clear(s);
+  }
+  // adds every held control point to g (strides sr, sc) and empties the store
+  __device__ __forceinline__ void flush_all(float* g, int64_t sr, int64_t sc) {
+    if (windowed()) {
+      if (lo >= 0) {
+        for (int t = lo; t < lo + kLaneWin; ++t) {
+          if (t < R) add_to(g, sr, sc, t, slot_of(t));
+          clear(slot_of(t));
+        }
+      }
+      lo = -1;
+    } else {
+      for (int t = 0; t < R; ++t) {
+        add_to(g, sr, sc, t, t);
+        clear(t);
+      }
+    }
   }
   // makes control points [t0, t1] resident (window mode only)
   __device__ __forceinline__ void ensure(int t0, int t1, float* warp_copy) {
@@ -319,48 +346,54 @@ struct LaneStore {
   __device__ __forceinline__ int window_lo() const { return windowed() ? max(lo, 0) : 0; }
 };
 
-// Register window in front of a lane store: kRegWin consecutive control
-// points around the current interval, re-centred when the density leaves it;
-// re-centring flushes the window into the lane store with independent
-// read-modify-writes (no dependency chain per sample).
-constexpr int kRegWin = 4;
-
+// Pair cache in front of a lane store: registers for the two control points
+// of the current interval (i, i+1).  When the density crosses into the next
+// or previous interval the point that leaves is added to the lane store and
+// the other one shifts over; a larger jump flushes both.  Per sample this is
+// a compare and 2*C FMAs.
 template <int C>
-struct RegWindow {
-  int base = -1;
-  float acc[kRegWin][C];
-  __device__ __forceinline__ void flush(LaneStore<C>& st, float* warp_copy) {
-    if (base < 0) return;
-    st.ensure(base, min(base + kRegWin - 1, st.R - 1), warp_copy);
-#pragma unroll
-    for (int w = 0; w < kRegWin; ++w) {
-      if (base + w < st.R) {
-        if constexpr (C == 4) st.add(base + w, mk4(acc[w][0], acc[w][1], acc[w][2], acc[w][3]));
-        else st.add(base + w, mk4(acc[w][0], acc[w][1], acc[w][2], acc[w][3]), acc[w][4]);
-      }
-    }
-    base = -1;
+struct PairCache {
+  int i = -1;
+  float a0[C], a1[C];
+  __device__ __forceinline__ void put(LaneStore<C>& st, int t, const float* v, float* warp_copy) {
+    if (t < 0 || t >= st.R) return;
+    st.ensure(t, t, warp_copy);
+    if constexpr (C == 4) st.add(t, mk4(v[0], v[1], v[2], v[3]));
+    else st.add(t, mk4(v[0], v[1], v[2], v[3]), v[4]);
   }
-  // adds k0 * v (+ e0 on channel 4) to point i0 and k1 * v (+ e1) to point i1
+  __device__ __forceinline__ void flush(LaneStore<C>& st, float* warp_copy) {
+    if (i < 0) return;
+    put(st, i, a0, warp_copy);
+    put(st, i + 1, a1, warp_copy);
+    i = -1;
+  }
+  // adds k0 * v (+ e0 on channel 4) to point i0 and k1 * v (+ e1) to point i1,
+  // where i1 is i0 + 1 or, at the clamped ends of a texture TF, i0 itself
   __device__ __forceinline__ void add(int i0, int i1, f4 v, float k0, float k1, float e0, float e1,
                                       LaneStore<C>& st, float* warp_copy) {
-    if (base < 0 || i0 < base || i1 >= base + kRegWin) {
-      flush(st, warp_copy);
-      base = max(0, min(i0 - 1, st.R - kRegWin));
+    if (i0 != i) {
+      if (i >= 0 && i0 == i + 1) {
+        put(st, i, a0, warp_copy);
 #pragma unroll
-      for (int w = 0; w < kRegWin; ++w)
+        for (int c = 0; c < C; ++c) { a0[c] = a1[c]; a1[c] = 0.f; }
+      } else if (i >= 0 && i0 == i - 1) {
+        put(st, i + 1, a1, warp_copy);
 #pragma unroll
-        for (int c = 0; c < C; ++c) acc[w][c] = 0.f;
+        for (int c = 0; c < C; ++c) { a1[c] = a0[c]; a0[c] = 0.f; }
+      } else {
+        flush(st, warp_copy);
+#pragma unroll
+        for (int c = 0; c < C; ++c) { a0[c] = 0.f; a1[c] = 0.f; }
+      }
+      i = i0;
     }
-    const int o0 = i0 - base, o1 = i1 - base;
-#pragma unroll
-    for (int w = 0; w < kRegWin; ++w) {
-      const float k = (o0 == w ? k0 : 0.f) + (o1 == w ? k1 : 0.f);
-      acc[w][0] += v.x * k;
-      acc[w][1] += v.y * k;
-      acc[w][2] += v.z * k;
-      acc[w][3] += v.w * k;
-      if constexpr (C == 5) acc[w][4] += (o0 == w ? e0 : 0.f) + (o1 == w ? e1 : 0.f);
+    const bool same = i1 == i0;
+    const float q0 = same ? k0 + k1 : k0, q1 = same ? 0.f : k1;
+    a0[0] += v.x * q0; a0[1] += v.y * q0; a0[2] += v.z * q0; a0[3] += v.w * q0;
+    a1[0] += v.x * q1; a1[1] += v.y * q1; a1[2] += v.z * q1; a1[3] += v.w * q1;
+    if constexpr (C == 5) {
+      a0[4] += same ? e0 + e1 : e0;
+      a1[4] += same ? 0.f : e1;
     }
   }
 };
@@ -383,6 +416,15 @@ struct TfGradAccum<kTfIdentity, TFGRAD> {
     const float adj_dc = (adj.x * sc + adj.y * sc + adj.z * sc) + adj.w * sa;
     return (density > 0 && density < 1) ? adj_dc : 0.f;
   }
+  __device__ __forceinline__ void set_evict_target(float*, int64_t, int64_t) {}
+  // adds the accumulated gradient to g (strides sr, sc) and restarts from zero
+  __device__ __forceinline__ void flush_global(float* g, int64_t, int64_t sc, float*) {
+    if constexpr (TFGRAD) {
+      if (ga != 0.f) atomicAdd(g, ga);
+      if (gc != 0.f) atomicAdd(g + sc, gc);
+      ga = gc = 0.f;
+    }
+  }
   // identity lane store: 2 floats [channel][lane]
   __device__ __forceinline__ void finish(float* lane_base, int T, int tid, int* lo_out) {
     if constexpr (TFGRAD) {
@@ -396,7 +438,7 @@ struct TfGradAccum<kTfIdentity, TFGRAD> {
 template <bool TFGRAD>
 struct TfGradAccum<kTfTexture, TFGRAD> {
   LaneStore<4> st;
-  RegWindow<4> win;
+  PairCache<4> win;
   float* warp_copy = nullptr;
   __device__ __forceinline__ void bind(float* lane_base, int T, int tid, int slots, int R) {
     st.base = lane_base;
@@ -419,6 +461,17 @@ struct TfGradAccum<kTfTexture, TFGRAD> {
     }
     return dot4(adj, mk4(c.x - a.x, c.y - a.y, c.z - a.z, c.w - a.w)) * R;
   }
+  __device__ __forceinline__ void set_evict_target(float* base, int64_t sr, int64_t sc) {
+    st.ev_base = base;
+    st.ev_sr = sr;
+    st.ev_sc = sc;
+  }
+  __device__ __forceinline__ void flush_global(float* g, int64_t sr, int64_t sc, float* wc) {
+    if constexpr (TFGRAD) {
+      win.flush(st, wc);
+      st.flush_all(g, sr, sc);
+    }
+  }
   __device__ __forceinline__ void finish(float*, int, int, int* lo_out) {
     if constexpr (TFGRAD) {
       win.flush(st, warp_copy);
@@ -430,7 +483,7 @@ struct TfGradAccum<kTfTexture, TFGRAD> {
 template <bool TFGRAD>
 struct TfGradAccum<kTfLinear, TFGRAD> {
   LaneStore<5> st;
-  RegWindow<5> win;
+  PairCache<5> win;
   float* warp_copy = nullptr;
   __device__ __forceinline__ void bind(float* lane_base, int T, int tid, int slots, int R) {
     st.base = lane_base;
@@ -453,6 +506,17 @@ struct TfGradAccum<kTfLinear, TFGRAD> {
       win.add(i, i + 1, adj, 1 - fr, fr, adj_fr * (d2 - p1) / den, adj_fr * (p0 - d2) / den, st, wc);
     }
     return adj_fr / (p1 - p0);
+  }
+  __device__ __forceinline__ void set_evict_target(float* base, int64_t sr, int64_t sc) {
+    st.ev_base = base;
+    st.ev_sr = sr;
+    st.ev_sc = sc;
+  }
+  __device__ __forceinline__ void flush_global(float* g, int64_t sr, int64_t sc, float* wc) {
+    if constexpr (TFGRAD) {
+      win.flush(st, wc);
+      st.flush_all(g, sr, sc);
+    }
   }
   __device__ __forceinline__ void finish(float*, int, int, int* lo_out) {
     if constexpr (TFGRAD) {
@@ -514,6 +578,29 @@ struct TfGradAccum<kTfGaussian, TFGRAD> {
     }
     return adj_density;
   }
+  __device__ __forceinline__ void set_evict_target(float* base, int64_t sr, int64_t sc) {
+    st.ev_base = base;
+    st.ev_sr = sr;
+    st.ev_sc = sc;
+  }
+  __device__ __forceinline__ void flush_global(float* g, int64_t sr, int64_t sc, float*) {
+    if constexpr (TFGRAD) {
+      if (regs) {
+#pragma unroll
+        for (int r = 0; r < kGaussRegs; ++r) {
+          if (r < st.R) {
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+              if (acc[r][c] != 0.f) atomicAdd(g + r * sr + c * sc, acc[r][c]);
+              acc[r][c] = 0.f;
+            }
+          }
+        }
+      } else {
+        st.flush_all(g, sr, sc);
+      }
+    }
+  }
   __device__ __forceinline__ void finish(float*, int, int, int* lo_out) {
     if constexpr (TFGRAD) {
       if (regs) {
@@ -535,7 +622,8 @@ struct TfGradAccum<kTfGaussian, TFGRAD> {
 // gradient (one global atomic per entry).
 template <int TF>
 __device__ __forceinline__ void reduce_tf_grad(const AdjointSmem& L, const float* smem, int R, float* out,
-                                               int64_t sb, int64_t sr, int64_t sc, int b) {
+                                               int64_t sb, int64_t sr, int64_t sc, int b,
+                                               const float* extra = nullptr) {
   constexpr int C = TfChannels<TF>::C;
   const int T = blockDim.x;
   const int n = R * C;
@@ -545,7 +633,7 @@ __device__ __forceinline__ void reduce_tf_grad(const AdjointSmem& L, const float
   const bool window = TF != kTfIdentity && R > L.slots;
   for (int e = threadIdx.x; e < n; e += T) {
     const int t = e / C, c = e - t * C;
-    float v = 0.f;
+    float v = extra ? extra[e] : 0.f;
     for (int w = 0; w < T / 32; ++w) v += warp[w * n + e];
     if constexpr (TF == kTfIdentity) {
       for (int l = 0; l < T; ++l) v += lane[c * T + l];
@@ -682,6 +770,7 @@ __device__ __forceinline__ void fast_adjoint_tile(const RenderParams& p, const A
   f4 adj_acc = mk4(0, 0, 0, 0);
   if (valid) {
     n = static_cast<const int*>(a.fwd_term.p)[b * a.fwd_term.s[0] + y * a.fwd_term.s[1] + x * a.fwd_term.s[2]];
+    n = min(n, max_samples(r.tmin, r.tmax, r.step));
     const float* ac = static_cast<const float*>(a.adj_color.p) + b * a.adj_color.s[0] + y * a.adj_color.s[1] +
                       x * a.adj_color.s[2];
     adj_acc = mk4(ac[0], ac[a.adj_color.s[3]], ac[2 * a.adj_color.s[3]], ac[3 * a.adj_color.s[3]]);

@@ -1,8 +1,10 @@
 // Launch logic of the optimized kernels for one TF mode and one volume
-// storage type (included by dvr_fast_tf*_*.cu).  One block per 16x8 pixel
-// tile; the hardware block scheduler balances tiles of unequal cost.
+// storage type (included by dvr_fast_tf*_*.cu).  Single-instance calls use
+// the persistent kernels (dvr_persist.cuh) with a work counter from the
+// library's pool; batched calls launch one block per (instance, batch entry,
+// tile) work item.
 #pragma once
-#include "dvr_fast.cuh"
+#include "dvr_persist.cuh"
 #include "dvr_kernels.h"
 
 namespace dvr {
@@ -76,61 +78,86 @@ cudaError_t launch_fast_adjoint_batched_vt(const RenderParams* table, const Adjo
              : fast_adjoint_batched_go<kTrilinear, TF, kAlphaBlend, VT>(table, atable, items, n_items, smem, volgrad, tfgrad, s);
 }
 
+// Grid of a persistent launch: every resident block slot, but no more
+// blocks than 128-ray groups of work.
+template <typename K>
+static int persistent_grid(K kernel, size_t smem, int64_t rays, const LaunchInfo& li) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kFastThreads, smem) != cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  const int64_t need = (rays + kFastThreads - 1) / kFastThreads;
+  const int64_t cap = int64_t(per_sm) * li.num_sms;
+  return int(need < cap ? (need > 0 ? need : 1) : cap);
+}
+
 template <int TF, typename VT>
-cudaError_t launch_fast_forward_vt(const RenderParams& p, int filter, int blend, const LaunchInfo&,
+cudaError_t launch_fast_forward_vt(const RenderParams& p, int filter, int blend, const LaunchInfo& li,
                                    cudaStream_t s) {
-  const int tiles_x = (p.W + kTileW - 1) / kTileW, tiles_y = (p.H + kTileH - 1) / kTileH;
-  const int64_t blocks = int64_t(tiles_x) * tiles_y * p.B;
-  if (blocks == 0) return cudaSuccess;
-  if (blocks > 0x7fffffff) return cudaErrorInvalidConfiguration;
-  const size_t smem = size_t(p.R) * p.C * sizeof(float);
+  const RayOrder order = RayOrder::make(p.W, p.H, p.B);
+  if (order.total() == 0) return cudaSuccess;
+  if (order.total() > 0x7fffffff) return cudaErrorInvalidConfiguration;
+  const int copies = p.tf.s[0] == 0 ? 1 : p.B;
+  const size_t smem = size_t(copies) * p.R * p.C * sizeof(float);
+  if (smem > size_t(li.max_smem_optin)) return cudaErrorInvalidConfiguration;
+  cudaError_t err;
+  int* counter = acquire_counter(li.device, s, err);
+  if (!counter) return err;
   auto go = [&](auto kernel) {
-    if (smem > 48 * 1024) {
-      cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-      if (e != cudaSuccess) return e;
-    }
-    kernel<<<unsigned(blocks), kFastThreads, smem, s>>>(p, tiles_x, tiles_y);
+    cudaError_t e = set_smem(kernel, smem);
+    if (e != cudaSuccess) return e;
+    kernel<<<persistent_grid(kernel, smem, order.total(), li), kFastThreads, smem, s>>>(p, order, counter);
     return cudaGetLastError();
   };
   if (filter == kNearest)
-    return blend == kBeerLambert ? go(fast_forward_kernel<kNearest, TF, kBeerLambert, VT>)
-                                 : go(fast_forward_kernel<kNearest, TF, kAlphaBlend, VT>);
-  return blend == kBeerLambert ? go(fast_forward_kernel<kTrilinear, TF, kBeerLambert, VT>)
-                               : go(fast_forward_kernel<kTrilinear, TF, kAlphaBlend, VT>);
+    return blend == kBeerLambert ? go(fast_forward_persistent_kernel<kNearest, TF, kBeerLambert, VT>)
+                                 : go(fast_forward_persistent_kernel<kNearest, TF, kAlphaBlend, VT>);
+  return blend == kBeerLambert ? go(fast_forward_persistent_kernel<kTrilinear, TF, kBeerLambert, VT>)
+                               : go(fast_forward_persistent_kernel<kTrilinear, TF, kAlphaBlend, VT>);
 }
 
 template <int FILTER, int TF, int BLEND, typename VT>
-static cudaError_t fast_adjoint_go(const RenderParams& p, const AdjointParams& a, cudaStream_t s) {
-  const int tiles_x = (p.W + kTileW - 1) / kTileW, tiles_y = (p.H + kTileH - 1) / kTileH;
-  const int64_t blocks = int64_t(tiles_x) * tiles_y * p.B;
-  if (blocks == 0) return cudaSuccess;
-  if (blocks > 0x7fffffff) return cudaErrorInvalidConfiguration;
+static cudaError_t fast_adjoint_go(const RenderParams& p, const AdjointParams& a, const LaunchInfo& li,
+                                   cudaStream_t s) {
+  const RayOrder order = RayOrder::make(p.W, p.H, p.B);
+  if (order.total() == 0) return cudaSuccess;
+  if (order.total() > 0x7fffffff) return cudaErrorInvalidConfiguration;
   constexpr int C = TfChannels<TF>::C;
   const bool tfgrad = a.has_tf != 0, volgrad = a.has_volume != 0;
-  const size_t smem = fast_adjoint_smem(TF, p.R, C, tfgrad, p.ckpt.p ? p.ckpt_interval : 0);
+  const int copies = p.tf.s[0] == 0 ? 1 : p.B;
+  const size_t smem = size_t(AdjointSmem(TF, p.R, C, kFastThreads, tfgrad, p.ckpt.p ? p.ckpt_interval : 0, copies)
+                                 .total) * sizeof(float);
+  if (smem > size_t(li.max_smem_optin)) return cudaErrorInvalidConfiguration;
+  cudaError_t err;
+  int* counter = acquire_counter(li.device, s, err);
+  if (!counter) return err;
   auto go = [&](auto kernel) {
-    if (smem > 48 * 1024) {
-      cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-      if (e != cudaSuccess) return e;
+    cudaError_t e = set_smem(kernel, smem);
+    if (e != cudaSuccess) return e;
+    const int grid = persistent_grid(kernel, smem, order.total(), li);
+    float* scratch = nullptr;
+    if (tfgrad) {
+      scratch = static_cast<float*>(acquire_scratch(li.device, s, size_t(grid) * p.R * C * sizeof(float), e));
+      if (!scratch) return e;
     }
-    kernel<<<unsigned(blocks), kFastThreads, smem, s>>>(p, a, tiles_x, tiles_y);
+    kernel<<<grid, kFastThreads, smem, s>>>(p, a, order, counter, scratch);
     return cudaGetLastError();
   };
   if (volgrad)
-    return tfgrad ? go(fast_adjoint_kernel<FILTER, TF, BLEND, true, true, VT>)
-                  : go(fast_adjoint_kernel<FILTER, TF, BLEND, true, false, VT>);
-  return tfgrad ? go(fast_adjoint_kernel<FILTER, TF, BLEND, false, true, VT>)
-                : go(fast_adjoint_kernel<FILTER, TF, BLEND, false, false, VT>);
+    return tfgrad ? go(fast_adjoint_persistent_kernel<FILTER, TF, BLEND, true, true, VT>)
+                  : go(fast_adjoint_persistent_kernel<FILTER, TF, BLEND, true, false, VT>);
+  return tfgrad ? go(fast_adjoint_persistent_kernel<FILTER, TF, BLEND, false, true, VT>)
+                : go(fast_adjoint_persistent_kernel<FILTER, TF, BLEND, false, false, VT>);
 }
 
 template <int TF, typename VT>
 cudaError_t launch_fast_adjoint_vt(const RenderParams& p, const AdjointParams& a, int filter, int blend,
-                                   const LaunchInfo&, cudaStream_t s) {
+                                   const LaunchInfo& li, cudaStream_t s) {
   if (filter == kNearest)
-    return blend == kBeerLambert ? fast_adjoint_go<kNearest, TF, kBeerLambert, VT>(p, a, s)
-                                 : fast_adjoint_go<kNearest, TF, kAlphaBlend, VT>(p, a, s);
-  return blend == kBeerLambert ? fast_adjoint_go<kTrilinear, TF, kBeerLambert, VT>(p, a, s)
-                               : fast_adjoint_go<kTrilinear, TF, kAlphaBlend, VT>(p, a, s);
+    return blend == kBeerLambert ? fast_adjoint_go<kNearest, TF, kBeerLambert, VT>(p, a, li, s)
+                                 : fast_adjoint_go<kNearest, TF, kAlphaBlend, VT>(p, a, li, s);
+  return blend == kBeerLambert ? fast_adjoint_go<kTrilinear, TF, kBeerLambert, VT>(p, a, li, s)
+                               : fast_adjoint_go<kTrilinear, TF, kAlphaBlend, VT>(p, a, li, s);
 }
 #endif
 

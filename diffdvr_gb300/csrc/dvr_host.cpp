@@ -138,6 +138,7 @@ LaunchInfo launch_info(int device) {
     }
     d.li.num_sms = sms;
     d.li.max_smem_optin = smem;
+    d.li.device = device;
     d.valid = true;
   }
   return d.li;

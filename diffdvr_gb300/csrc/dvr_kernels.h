@@ -10,7 +10,18 @@ namespace dvr {
 struct LaunchInfo {
   int num_sms;
   int max_smem_optin;  // cudaDevAttrMaxSharedMemoryPerBlockOptin
+  int device;
 };
+
+// A zeroed work counter for one persistent launch on stream s, from a
+// per-device pool owned by the library (allocated on first use, so make the
+// first call on a device before capturing a stream into a CUDA graph).
+int* acquire_counter(int device, cudaStream_t s, cudaError_t& err);
+
+// Scratch memory of at least `bytes` for launches on stream s, owned by the
+// library and reused by later launches on the same stream (grown on demand;
+// growing synchronises the stream).  Not zeroed.
+void* acquire_scratch(int device, cudaStream_t s, size_t bytes, cudaError_t& err);
 
 // Plain family (reference semantics).
 template <int TF>

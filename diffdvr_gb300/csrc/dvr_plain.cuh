@@ -30,8 +30,9 @@ __global__ void __launch_bounds__(256) plain_forward_kernel(const RenderParams p
     f4 acc = mk4(0, 0, 0, 0);
     int cx = -1, cy = -1, cz = -1;
     float d8[8];
+    const int kmax = max_samples(r.tmin, r.tmax, r.step);
     int k;
-    for (k = 0;; ++k) {
+    for (k = 0; k < kmax; ++k) {
       const float t = r.tmin + k * r.step;
       if (t > r.tmax) break;
       if (acc.w > p.early_out) break;
@@ -120,6 +121,7 @@ __global__ void __launch_bounds__(256) plain_adjoint_kernel(const RenderParams p
                       x * a.fwd_color.s[2];
     f4 acc = mk4(fc[0], fc[a.fwd_color.s[3]], fc[2 * a.fwd_color.s[3]], fc[3 * a.fwd_color.s[3]]);
     int k = static_cast<const int*>(a.fwd_term.p)[b * a.fwd_term.s[0] + y * a.fwd_term.s[1] + x * a.fwd_term.s[2]];
+    k = min(k, max_samples(r.tmin, r.tmax, r.step));
     const float* ac = static_cast<const float*>(a.adj_color.p) + b * a.adj_color.s[0] + y * a.adj_color.s[1] +
                       x * a.adj_color.s[2];
     f4 adj_acc = mk4(ac[0], ac[a.adj_color.s[3]], ac[2 * a.adj_color.s[3]], ac[3 * a.adj_color.s[3]]);
