@@ -101,6 +101,8 @@ SIGNATURES = {
     "dvr_render_forward": (ctypes.c_int, [_P(DvrRendererInputs), _P(DvrRendererOutputs), ctypes.c_void_p]),
     "dvr_render_adjoint": (ctypes.c_int, [_P(DvrRendererInputs), _P(DvrRendererOutputs), _P(DvrTensor),
                                           _P(DvrAdjointOutputs), ctypes.c_void_p]),
+    "dvr_render_adjoint_noalloc": (ctypes.c_int, [_P(DvrRendererInputs), _P(DvrRendererOutputs), _P(DvrTensor),
+                                                  _P(DvrAdjointOutputs), ctypes.c_void_p]),
     "dvr_render_forward_batched": (ctypes.c_int, [_P(DvrRendererInputs), _P(DvrRendererOutputs), ctypes.c_int32,
                                                   ctypes.c_void_p]),
     "dvr_render_adjoint_batched": (ctypes.c_int, [_P(DvrRendererInputs), _P(DvrRendererOutputs), _P(DvrTensor),

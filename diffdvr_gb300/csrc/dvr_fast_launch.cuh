@@ -23,6 +23,9 @@ template <int TF, typename VT>
 cudaError_t launch_fast_adjoint_batched_vt(const RenderParams* table, const AdjointParams* atable, const int4* items,
                                            int n_items, size_t smem, int filter, int blend, bool volgrad, bool tfgrad,
                                            cudaStream_t s);
+template <int TF, typename VT>
+cudaError_t launch_fast_adjoint_into_vt(const RenderParams& p, const AdjointParams& a, int filter, int blend,
+                                        const LaunchInfo& li, const CallerScratch& sc, cudaStream_t s);
 
 #ifdef DVR_FAST_DEFINE
 template <typename K>
@@ -159,6 +162,49 @@ cudaError_t launch_fast_adjoint_vt(const RenderParams& p, const AdjointParams& a
   return blend == kBeerLambert ? fast_adjoint_go<kTrilinear, TF, kBeerLambert, VT>(p, a, li, s)
                                : fast_adjoint_go<kTrilinear, TF, kAlphaBlend, VT>(p, a, li, s);
 }
+
+// Same kernels as fast_adjoint_go; the work counter and the TF-gradient
+// slices come from the caller, so nothing is allocated.
+template <int FILTER, int TF, int BLEND, typename VT>
+static cudaError_t fast_adjoint_into_go(const RenderParams& p, const AdjointParams& a, const LaunchInfo& li,
+                                        const CallerScratch& sc, cudaStream_t s) {
+  const RayOrder order = RayOrder::make(p.W, p.H, p.B);
+  if (order.total() == 0) return cudaSuccess;
+  if (order.total() > 0x7fffffff) return cudaErrorInvalidConfiguration;
+  constexpr int C = TfChannels<TF>::C;
+  const bool tfgrad = a.has_tf != 0, volgrad = a.has_volume != 0;
+  const int copies = p.tf.s[0] == 0 ? 1 : p.B;
+  const size_t smem = size_t(AdjointSmem(TF, p.R, C, kFastThreads, tfgrad, p.ckpt.p ? p.ckpt_interval : 0, copies)
+                                 .total) * sizeof(float);
+  if (smem > size_t(li.max_smem_optin)) return cudaErrorInvalidConfiguration;
+  const size_t slice = size_t(p.R) * C * sizeof(float);
+  const int64_t fit = tfgrad ? int64_t(sc.tf_bytes / slice) : int64_t(1) << 30;
+  if (fit < 1) return cudaErrorInvalidValue;
+  cudaError_t err = cudaMemsetAsync(sc.counter, 0, sizeof(int), s);
+  if (err != cudaSuccess) return err;
+  auto go = [&](auto kernel) {
+    cudaError_t e = set_smem(kernel, smem);
+    if (e != cudaSuccess) return e;
+    const int grid = int(std::min<int64_t>(persistent_grid(kernel, smem, order.total(), li), fit));
+    kernel<<<grid, kFastThreads, smem, s>>>(p, a, order, sc.counter, sc.tf);
+    return cudaGetLastError();
+  };
+  if (volgrad)
+    return tfgrad ? go(fast_adjoint_persistent_kernel<FILTER, TF, BLEND, true, true, VT>)
+                  : go(fast_adjoint_persistent_kernel<FILTER, TF, BLEND, true, false, VT>);
+  return tfgrad ? go(fast_adjoint_persistent_kernel<FILTER, TF, BLEND, false, true, VT>)
+                : go(fast_adjoint_persistent_kernel<FILTER, TF, BLEND, false, false, VT>);
+}
+
+template <int TF, typename VT>
+cudaError_t launch_fast_adjoint_into_vt(const RenderParams& p, const AdjointParams& a, int filter, int blend,
+                                        const LaunchInfo& li, const CallerScratch& sc, cudaStream_t s) {
+  if (filter == kNearest)
+    return blend == kBeerLambert ? fast_adjoint_into_go<kNearest, TF, kBeerLambert, VT>(p, a, li, sc, s)
+                                 : fast_adjoint_into_go<kNearest, TF, kAlphaBlend, VT>(p, a, li, sc, s);
+  return blend == kBeerLambert ? fast_adjoint_into_go<kTrilinear, TF, kBeerLambert, VT>(p, a, li, sc, s)
+                               : fast_adjoint_into_go<kTrilinear, TF, kAlphaBlend, VT>(p, a, li, sc, s);
+}
 #endif
 
 }  // namespace dvr
@@ -172,4 +218,7 @@ cudaError_t launch_fast_adjoint_vt(const RenderParams& p, const AdjointParams& a
                                                                    int, int, cudaStream_t);                  \
   template cudaError_t dvr::launch_fast_adjoint_batched_vt<TF, VT>(const RenderParams*, const AdjointParams*,  \
                                                                    const int4*, int, size_t, int, int, bool, bool, \
-                                                                   cudaStream_t);
+                                                                   cudaStream_t);                            \
+  template cudaError_t dvr::launch_fast_adjoint_into_vt<TF, VT>(const RenderParams&, const AdjointParams&, int,  \
+                                                                int, const LaunchInfo&, const CallerScratch&,  \
+                                                                cudaStream_t);

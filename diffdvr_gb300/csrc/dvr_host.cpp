@@ -21,6 +21,7 @@
 
 #include "dvr_kernels.h"
 #include "dvr_batch.h"
+#include "dvr_entry.h"
 
 namespace dvr {
 namespace {
@@ -542,7 +543,47 @@ cudaError_t dispatch_adjoint(const Checked& c, const AdjointParams& a, bool plai
   }
 }
 
+cudaError_t dispatch_adjoint_into(const Checked& c, const AdjointParams& a, const LaunchInfo& li,
+                                  const CallerScratch& sc, cudaStream_t s) {
+  switch (c.tf_mode) {
+    case DVR_TF_IDENTITY: return launch_fast_adjoint_into<0>(c.p, a, c.filter, c.blend, li, sc, s);
+    case DVR_TF_TEXTURE: return launch_fast_adjoint_into<1>(c.p, a, c.filter, c.blend, li, sc, s);
+    case DVR_TF_LINEAR: return launch_fast_adjoint_into<2>(c.p, a, c.filter, c.blend, li, sc, s);
+    default: return launch_fast_adjoint_into<3>(c.p, a, c.filter, c.blend, li, sc, s);
+  }
+}
+
 }  // namespace
+
+int render_adjoint_into(const DvrRendererInputs* inputs, const DvrRendererOutputs* outputs_from_forward,
+                        const DvrTensor* adj_color, const DvrAdjointOutputs* adj_outputs, void* cuda_stream,
+                        ScratchSource source) {
+  return guarded([&] {
+    if (!inputs || !outputs_from_forward || !adj_color || !adj_outputs)
+      fail(DVR_E_INVALID_ARGUMENT, "arguments must not be NULL");
+    Checked c = check_inputs(*inputs);
+    check_outputs(*outputs_from_forward, c, false);
+    const AdjointParams a = check_adjoint(*adj_color, *adj_outputs, c);
+    DeviceGuard guard(c.device);
+    const LaunchInfo li = launch_info(c.device);
+    CallerScratch sc{};
+    if (const char* msg = source(c.device, &sc)) fail(DVR_E_CUDA, msg);
+    if (a.has_tf) {
+      // one TF-gradient slice of R*C floats per block, at least one block per SM
+      const size_t need = size_t(li.num_sms) * size_t(c.p.R) * size_t(c.p.C) * sizeof(float);
+      if (need > sc.tf_bytes) {
+        std::ostringstream m;
+        m << "TF too large for the no-allocation adjoint: " << c.p.R << " control points x " << c.p.C
+          << " channels need " << need << " bytes of TF-gradient scratch (" << li.num_sms
+          << " SMs), the static scratch holds " << sc.tf_bytes << "; use dvr_render_adjoint";
+        fail(DVR_E_INVALID_ARGUMENT, m.str());
+      }
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+    after_launch(dispatch_adjoint_into(c, a, li, sc, s), s, "adjoint");
+  });
+}
+
 }  // namespace dvr
 
 using namespace dvr;

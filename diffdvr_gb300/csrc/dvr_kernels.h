@@ -23,6 +23,15 @@ int* acquire_counter(int device, cudaStream_t s, cudaError_t& err);
 // growing synchronises the stream).  Not zeroed.
 void* acquire_scratch(int device, cudaStream_t s, size_t bytes, cudaError_t& err);
 
+// Scratch handed in by the caller instead of the library's pools: `counter`
+// (one int, zeroed here on the stream before each launch) and `tf` (TF-gradient
+// slices of R*C floats per block, zeroed by the kernel; tf_bytes bytes).
+struct CallerScratch {
+  int* counter;
+  float* tf;
+  size_t tf_bytes;
+};
+
 // Plain family (reference semantics).
 template <int TF>
 cudaError_t launch_plain_forward(const RenderParams& p, int filter, int blend, const LaunchInfo& li, cudaStream_t s);
@@ -36,5 +45,10 @@ cudaError_t launch_fast_forward(const RenderParams& p, int filter, int blend, co
 template <int TF>
 cudaError_t launch_fast_adjoint(const RenderParams& p, const AdjointParams& a, int filter, int blend,
                                 const LaunchInfo& li, cudaStream_t s);
+// The optimized adjoint on caller-provided scratch: allocates nothing.  The
+// persistent grid is capped to the blocks whose TF slices fit in sc.tf_bytes.
+template <int TF>
+cudaError_t launch_fast_adjoint_into(const RenderParams& p, const AdjointParams& a, int filter, int blend,
+                                     const LaunchInfo& li, const CallerScratch& sc, cudaStream_t s);
 
 }  // namespace dvr

@@ -157,6 +157,28 @@ int dvr_render_forward(const DvrRendererInputs* inputs, const DvrRendererOutputs
 int dvr_render_adjoint(const DvrRendererInputs* inputs, const DvrRendererOutputs* outputs_from_forward,
                        const DvrTensor* adj_color, const DvrAdjointOutputs* adj_outputs, void* cuda_stream);
 
+/* The optimized adjoint of dvr_render_adjoint (same arguments, validation,
+ * errors and results) for callers that cannot let a library allocate device
+ * memory: applications whose own allocator owns the device or that run under
+ * a hard memory budget, and render loops that must not stall on cudaMalloc's
+ * implicit synchronisation.  dvr_render_adjoint grows internal scratch pools
+ * with cudaMalloc; this entry point allocates nothing and uses a static
+ * 4 MiB device array per device instead (one work counter, zeroed on the
+ * stream before each launch, and per-block TF-gradient slices that the kernel
+ * zeroes itself).
+ * Limit: with has_tf_derivatives, R x C x 4 bytes x (SM count) must fit in
+ * 4 MiB - 256 bytes (R = TF control points, C = channels), i.e. R x C <= 6898
+ * on a 152-SM GPU; larger TFs are rejected with DVR_E_INVALID_ARGUMENT.
+ * Volume and image sizes are not limited.  The kernel-family switch does not
+ * apply.  The first call on a device resolves the array's address; make it
+ * before capturing the stream into a CUDA graph.  All calls on one device
+ * share the array: calls that may overlap (other streams or host threads)
+ * race, so the caller serialises them.
+ * No counterpart in the reference. */
+int dvr_render_adjoint_noalloc(const DvrRendererInputs* inputs, const DvrRendererOutputs* outputs_from_forward,
+                               const DvrTensor* adj_color, const DvrAdjointOutputs* adj_outputs,
+                               void* cuda_stream);
+
 /* Batched rendering of n independent instances, each with its own volume
  * size, image size, camera and TF, in ONE persistent launch over a work list
  * of (instance, view, tile) items.  All instances share the filter, TF and
