@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline budget")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--interval", type=int, default=16, help="transmittance checkpoint interval (samples)")
+    ap.add_argument("--record", choices=["full", "none"], default="full",
+                    help="sample-density record: a pool for every ray, or none (the adjoint re-samples)")
     return ap.parse_args()
 
 
@@ -182,6 +184,9 @@ def run_gpu(args):
     term = torch.empty(B, H, W, dtype=torch.int32, device=dev)
     ckpt = torch.empty(B, H, W, slots, device=dev)
     out = pr.RendererOutputs(color, term, ckpt, K)
+    if args.record == "full":
+        out.sample_density = torch.empty(pr.Renderer.sample_density_size(inp16, B), device=dev)
+        out.sample_offset = torch.empty(B, H, W, dtype=torch.int32, device=dev)
     adj_tf = torch.zeros_like(tf)
     adj = pr.AdjointOutputs()
     adj.has_tf_derivatives = True
@@ -348,15 +353,22 @@ def run_gpu(args):
     V = args.res ** 3
     P = B * H * W
     ck_written = int(torch.clamp((term.to(torch.int64) - 1) // K, min=0).clamp_max(slots).sum().item())
-    fwd_bytes = V * 2 + P * (16 + 4) + ck_written * 4
-    adj_bytes = V * 2 + P * (4 + 16) + ck_written * 4 + tf.numel() * 4 * 2
+    if args.record == "full":
+        # forward: volume, colour + termination + offset, checkpoints, one density per sample;
+        # adjoint: termination + adj_color + offset, checkpoints, densities, TF (no volume reads)
+        fwd_bytes = V * 2 + P * (16 + 4 + 4) + ck_written * 4 + samples * 4
+        adj_bytes = P * (4 + 16 + 4) + ck_written * 4 + samples * 4 + tf.numel() * 4 * 2
+    else:
+        fwd_bytes = V * 2 + P * (16 + 4) + ck_written * 4
+        adj_bytes = V * 2 + P * (4 + 16) + ck_written * 4 + tf.numel() * 4 * 2
     dominant = ("adjoint", adj_bytes, adj_ms) if adj_ms >= fwd_ms else ("forward", fwd_bytes, fwd_ms)
     achieved = dominant[1] / (dominant[2] / 1e3) / 1e9
     tr = profiled_traffic()
     traffic = None
     if tr and tr.get("kernel") == dominant[0]:
         traffic = tr.get("dram_bytes_per_launch")
-    gather_bytes = samples * 8 * 2 * 2  # 8 BF16 corner reads per sample, forward and adjoint
+    # 8 BF16 corner reads per sample in the forward, and in the adjoint unless it reads the record
+    gather_bytes = samples * 8 * 2 * (1 if args.record == "full" else 2)
 
     result = {
         "metric": METRIC,
@@ -373,7 +385,8 @@ def run_gpu(args):
         "data": "synthetic (seeded blobs + noise, random TF, Fibonacci views)",
         "config": {"workload": WORKLOAD, "volume_storage": "bf16", "tf_storage": "f32", "views": B,
                    "image": [H, W], "volume": [args.res] * 3, "samples_per_step": samples, "rays_hit": rays_hit,
-                   "checkpoint_interval": K, "l2": "flushed (256 MB write) before every timed step",
+                   "checkpoint_interval": K, "sample_density_record": args.record,
+                   "l2": "flushed (256 MB write) before every timed step",
                    "graph": "forward+loss+adjoint captured in one CUDA graph",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": "samples/s", "h2d_bytes_per_step": int(h2d),

@@ -76,6 +76,8 @@ class DvrRendererOutputs(ctypes.Structure):
         ("checkpoints", DvrTensor),
         ("checkpoint_interval", ctypes.c_int32),
         ("pad_", ctypes.c_int32),
+        ("sample_density", DvrTensor),
+        ("sample_offset", DvrTensor),
     ]
 
 
@@ -137,7 +139,7 @@ def load() -> ctypes.CDLL:
             fn = getattr(lib, name)
             fn.restype = res
             fn.argtypes = args
-        if lib.dvr_abi_version() != 1:
+        if lib.dvr_abi_version() != 2:
             raise RuntimeError("libdvr_gb300.so has an unexpected ABI version")
         _LIB = lib
     return _LIB

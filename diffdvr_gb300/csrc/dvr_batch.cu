@@ -147,6 +147,7 @@ std::mutex g_counter_mutex;
 int* g_counters[64] = {};
 unsigned g_counter_next[64] = {};
 constexpr unsigned kCounters = 4096;
+constexpr unsigned kCounterInts = 4;  // 16 bytes per launch
 
 struct ScratchSlot {
   int device = -1;
@@ -193,14 +194,14 @@ int* acquire_counter(int device, cudaStream_t s, cudaError_t& err) {
     std::lock_guard<std::mutex> lock(g_counter_mutex);
     const int d = device & 63;
     if (!g_counters[d]) {
-      err = cudaMalloc(&g_counters[d], kCounters * sizeof(int));
+      err = cudaMalloc(&g_counters[d], kCounters * kCounterInts * sizeof(int));
       if (err != cudaSuccess) return nullptr;
     }
     // launches in flight at the same time get different counters as long as
     // fewer than kCounters of them overlap
-    c = g_counters[d] + (g_counter_next[d]++ % kCounters);
+    c = g_counters[d] + (g_counter_next[d]++ % kCounters) * kCounterInts;
   }
-  err = cudaMemsetAsync(c, 0, sizeof(int), s);
+  err = cudaMemsetAsync(c, 0, kCounterInts * sizeof(int), s);
   return err == cudaSuccess ? c : nullptr;
 }
 

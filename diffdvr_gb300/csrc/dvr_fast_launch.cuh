@@ -138,12 +138,17 @@ static cudaError_t fast_adjoint_go(const RenderParams& p, const AdjointParams& a
     cudaError_t e = set_smem(kernel, smem);
     if (e != cudaSuccess) return e;
     const int grid = persistent_grid(kernel, smem, order.total(), li);
-    float* scratch = nullptr;
-    if (tfgrad) {
-      scratch = static_cast<float*>(acquire_scratch(li.device, s, size_t(grid) * p.R * C * sizeof(float), e));
-      if (!scratch) return e;
-    }
-    kernel<<<grid, kFastThreads, smem, s>>>(p, a, order, counter, scratch);
+    // scratch: the longest-first ray list, then the blocks' TF-gradient slices
+    const size_t list_bytes = (work_order_ints(p) * sizeof(int) + 255) & ~size_t(255);
+    const size_t tf_bytes = tfgrad ? size_t(grid) * p.R * C * sizeof(float) : 0;
+    char* scratch = static_cast<char*>(acquire_scratch(li.device, s, list_bytes + tf_bytes, e));
+    if (!scratch) return e;
+    int* order_ints = reinterpret_cast<int*>(scratch);
+    e = order_rays_by_work(p, a, order_ints, li, s);
+    if (e != cudaSuccess) return e;
+    kernel<<<grid, kFastThreads, smem, s>>>(p, a, order, counter, tfgrad ? reinterpret_cast<float*>(scratch + list_bytes)
+                                                                       : nullptr,
+                                            order_ints + work_order_list_offset);
     return cudaGetLastError();
   };
   if (volgrad)
@@ -186,7 +191,7 @@ static cudaError_t fast_adjoint_into_go(const RenderParams& p, const AdjointPara
     cudaError_t e = set_smem(kernel, smem);
     if (e != cudaSuccess) return e;
     const int grid = int(std::min<int64_t>(persistent_grid(kernel, smem, order.total(), li), fit));
-    kernel<<<grid, kFastThreads, smem, s>>>(p, a, order, sc.counter, sc.tf);
+    kernel<<<grid, kFastThreads, smem, s>>>(p, a, order, sc.counter, sc.tf, nullptr);
     return cudaGetLastError();
   };
   if (volgrad)

@@ -8,6 +8,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdarg>
@@ -390,6 +391,32 @@ void check_outputs(const DvrRendererOutputs& out, Checked& c, bool forward) {
     p.ckpt = out_view(ck, false);
     p.ckpt_slots = int(ck.sizes[3]);
   }
+  p.dens = nullptr;
+  p.dens_off = OutView{};
+  p.dens_units = 0;
+  const bool has_dens = out.sample_density.ndim >= 0 && out.sample_density.data != nullptr;
+  const bool has_off = out.sample_offset.ndim >= 0 && out.sample_offset.data != nullptr;
+  if (has_dens != has_off) fail(DVR_E_INVALID_ARGUMENT, "sample_density and sample_offset go together");
+  if (has_dens) {
+    if (!p.ckpt.p) fail(DVR_E_INVALID_ARGUMENT, "sample_density needs a checkpoint buffer");
+    const DvrTensor& d = out.sample_density;
+    check_dim(d, "sample_density", 1);
+    check_device(d, "sample_density", c.device);
+    check_dtype(d, "sample_density", DVR_FLOAT32);
+    if (d.sizes[0] < 4 || (d.sizes[0] > 1 && d.strides[0] != 1) ||
+        (reinterpret_cast<uintptr_t>(d.data) & 15u) != 0)
+      fail(DVR_E_INVALID_ARGUMENT, "sample_density must be contiguous, 16-byte aligned and hold at least 4 values");
+    const DvrTensor& o = out.sample_offset;
+    check_dim(o, "sample_offset", 3);
+    check_device(o, "sample_offset", c.device);
+    check_size(o, "sample_offset", 0, p.B);
+    check_size(o, "sample_offset", 1, p.H);
+    check_size(o, "sample_offset", 2, p.W);
+    check_dtype(o, "sample_offset", DVR_INT32);
+    p.dens = static_cast<float*>(d.data);
+    p.dens_off = out_view(o, false);
+    p.dens_units = std::min<int64_t>(d.sizes[0] / 4, 0x7fffffff);
+  }
 }
 
 // checkAdjointOutput (renderer/renderer.cpp:265-365) plus the forward-output
@@ -488,6 +515,8 @@ bool use_plain(const Checked& c) {
   if (g_family.load() == DVR_KERNELS_PLAIN) {
     if (c.p.vol_storage != DVR_FLOAT32 || c.p.tf_storage != DVR_FLOAT32)
       fail(DVR_E_UNSUPPORTED, "the plain kernel family renders float32 volumes and TFs only");
+    if (c.p.dens)
+      fail(DVR_E_UNSUPPORTED, "sample_density is recorded and read by the optimized kernel family only");
     return true;
   }
   return false;
@@ -628,6 +657,7 @@ extern "C" int dvr_render_forward_batched(const DvrRendererInputs* inputs, const
     for (int i = 0; i < n; ++i) {
       cs[i] = check_inputs(inputs[i]);
       check_outputs(outputs[i], cs[i], true);
+      if (cs[i].p.dens) fail(DVR_E_UNSUPPORTED, "the batched entry points do not record sample_density");
       if (i > 0 && (cs[i].filter != cs[0].filter || cs[i].tf_mode != cs[0].tf_mode || cs[i].blend != cs[0].blend ||
                     cs[i].p.vol_storage != cs[0].p.vol_storage || cs[i].p.tf_storage != cs[0].p.tf_storage ||
                     cs[i].device != cs[0].device))
@@ -656,6 +686,7 @@ extern "C" int dvr_render_adjoint_batched(const DvrRendererInputs* inputs,
     for (int i = 0; i < n; ++i) {
       cs[i] = check_inputs(inputs[i]);
       check_outputs(outputs_from_forward[i], cs[i], false);
+      if (cs[i].p.dens) fail(DVR_E_UNSUPPORTED, "the batched entry points do not record sample_density");
       as[i] = check_adjoint(adj_colors[i], adj_outputs[i], cs[i]);
       if (i > 0 && (cs[i].filter != cs[0].filter || cs[i].tf_mode != cs[0].tf_mode || cs[i].blend != cs[0].blend ||
                     cs[i].p.vol_storage != cs[0].p.vol_storage || cs[i].p.tf_storage != cs[0].p.tf_storage ||

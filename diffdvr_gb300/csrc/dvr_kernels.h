@@ -13,7 +13,8 @@ struct LaunchInfo {
   int device;
 };
 
-// A zeroed work counter for one persistent launch on stream s, from a
+// Zeroed counters for one persistent launch on stream s: 16 bytes, 16-byte
+// aligned (int [0] = ray counter, bytes 8..15 = a 64-bit counter), from a
 // per-device pool owned by the library (allocated on first use, so make the
 // first call on a device before capturing a stream into a CUDA graph).
 int* acquire_counter(int device, cudaStream_t s, cudaError_t& err);
@@ -31,6 +32,14 @@ struct CallerScratch {
   float* tf;
   size_t tf_bytes;
 };
+
+// Longest-first ray order for the persistent adjoint: ray ids bucketed by
+// descending forward sample count.  scratch holds work_order_ints(p) ints; the
+// ordered list starts at scratch + work_order_list_offset.
+constexpr size_t work_order_list_offset = 512;
+size_t work_order_ints(const RenderParams& p);
+cudaError_t order_rays_by_work(const RenderParams& p, const AdjointParams& a, int* scratch, const LaunchInfo& li,
+                               cudaStream_t s);
 
 // Plain family (reference semantics).
 template <int TF>

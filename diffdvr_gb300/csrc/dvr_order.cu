@@ -1,0 +1,95 @@
+// Longest-first ray order for the persistent adjoint.
+//
+// The adjoint knows each ray's exact work, the forward's termination index n
+// (samples).  With one or two rays per resident lane, fetching rays in pixel
+// order lets a long ray fetched late set the end of the launch while the other
+// warps wait.  These kernels bucket the ray ids by descending n (key = 255 -
+// min(255, floor(4 sqrt(n))): buckets a few samples wide for short rays, a
+// few tens for rays of thousands of samples) so the tail of the launch is made
+// of short rays.  Within a bucket, ids of one block of consecutive rays stay
+// together, so neighbouring rays are still fetched by the same warp.
+#include "dvr_kernels.h"
+#include "dvr_persist.cuh"
+
+namespace dvr {
+namespace {
+
+constexpr int kBuckets = 256;
+constexpr int kOrderThreads = 256;
+static_assert(work_order_list_offset == 2 * kBuckets, "list follows the histogram and the bucket starts");
+
+__device__ __forceinline__ int work_key(const RenderParams& p, const AdjointParams& a, const RayOrder& o, int id) {
+  int b, x, y;
+  if (!o.pixel(id, b, x, y)) return kBuckets - 1;
+  const int n = static_cast<const int*>(a.fwd_term.p)[b * a.fwd_term.s[0] + y * a.fwd_term.s[1] + x * a.fwd_term.s[2]];
+  const int r = n <= 0 ? 0 : min(kBuckets - 1, int(sqrtf(float(n)) * 4.f));
+  return kBuckets - 1 - r;
+}
+
+__global__ void __launch_bounds__(kOrderThreads) work_histogram_kernel(const RenderParams p, const AdjointParams a,
+                                                                       const RayOrder o, int* hist) {
+  __shared__ int sh[kBuckets];
+  sh[threadIdx.x] = 0;
+  __syncthreads();
+  const int total = int(o.total());
+  for (int id = blockIdx.x * kOrderThreads + threadIdx.x; id < total; id += gridDim.x * kOrderThreads)
+    atomicAdd(&sh[work_key(p, a, o, id)], 1);
+  __syncthreads();
+  if (sh[threadIdx.x] > 0) atomicAdd(&hist[threadIdx.x], sh[threadIdx.x]);
+}
+
+// exclusive scan of the histogram into the bucket starts (one block)
+__global__ void __launch_bounds__(kOrderThreads) work_scan_kernel(const int* hist, int* start) {
+  __shared__ int sh[kBuckets];
+  sh[threadIdx.x] = hist[threadIdx.x];
+  __syncthreads();
+  for (int o = 1; o < kBuckets; o <<= 1) {
+    const int v = threadIdx.x >= o ? sh[threadIdx.x - o] : 0;
+    __syncthreads();
+    sh[threadIdx.x] += v;
+    __syncthreads();
+  }
+  start[threadIdx.x] = sh[threadIdx.x] - hist[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(kOrderThreads) work_scatter_kernel(const RenderParams p, const AdjointParams a,
+                                                                     const RayOrder o, int* start, int* list) {
+  __shared__ int cnt[kBuckets];
+  __shared__ int base[kBuckets];
+  const int total = int(o.total());
+  for (int first = blockIdx.x * kOrderThreads; first < total; first += gridDim.x * kOrderThreads) {
+    cnt[threadIdx.x] = 0;
+    __syncthreads();
+    const int id = first + threadIdx.x;
+    const int key = id < total ? work_key(p, a, o, id) : 0;
+    const int rank = id < total ? atomicAdd(&cnt[key], 1) : 0;
+    __syncthreads();
+    if (cnt[threadIdx.x] > 0) base[threadIdx.x] = atomicAdd(&start[threadIdx.x], cnt[threadIdx.x]);
+    __syncthreads();
+    if (id < total) list[base[key] + rank] = id;
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+size_t work_order_ints(const RenderParams& p) { return 2 * kBuckets + size_t(RayOrder::make(p.W, p.H, p.B).total()); }
+
+cudaError_t order_rays_by_work(const RenderParams& p, const AdjointParams& a, int* scratch, const LaunchInfo& li,
+                               cudaStream_t s) {
+  const RayOrder o = RayOrder::make(p.W, p.H, p.B);
+  const int64_t total = o.total();
+  if (total == 0) return cudaSuccess;
+  int* hist = scratch;
+  int* start = scratch + kBuckets;
+  int* list = scratch + 2 * kBuckets;
+  cudaError_t e = cudaMemsetAsync(hist, 0, kBuckets * sizeof(int), s);
+  if (e != cudaSuccess) return e;
+  const int blocks = int(std::min<int64_t>((total + kOrderThreads - 1) / kOrderThreads, int64_t(li.num_sms) * 8));
+  work_histogram_kernel<<<blocks, kOrderThreads, 0, s>>>(p, a, o, hist);
+  work_scan_kernel<<<1, kOrderThreads, 0, s>>>(hist, start);
+  work_scatter_kernel<<<blocks, kOrderThreads, 0, s>>>(p, a, o, start, list);
+  return cudaGetLastError();
+}
+
+}  // namespace dvr

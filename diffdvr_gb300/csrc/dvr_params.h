@@ -48,6 +48,10 @@ struct RenderParams {
   OutView ckpt;                 // [b][y][x][j] float, transmittance before sample (j+1)*K
   int32_t ckpt_slots;           // C slots per ray
   int32_t ckpt_interval;        // K
+  // per-sample density record (optimized kernels); dens == nullptr when absent
+  float* dens;                  // pool of dens_units groups of 4 floats, 16-byte aligned
+  OutView dens_off;             // [b][y][x] int32: first group of the ray's densities, -1 = not recorded
+  int64_t dens_units;
 };
 
 struct AdjointParams {

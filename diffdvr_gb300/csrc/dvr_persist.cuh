@@ -88,6 +88,15 @@ __global__ void __launch_bounds__(kFastThreads) fast_forward_persistent_kernel(c
   TfShared<C> tf{s_tf, p.R};
   float* ck = nullptr;
   const int K = p.ckpt_interval;
+  // density record: this lane's ray stores its samples from group dgrp on
+  float4* const dens4 = reinterpret_cast<float4*>(p.dens);
+  unsigned long long* const bump = reinterpret_cast<unsigned long long*>(counter + 2);
+  int dgrp = -1;
+  float4 dstage = make_float4(0.f, 0.f, 0.f, 0.f);
+  const int lane = threadIdx.x & 31;
+  auto dens_off_at = [&]() -> int* {
+    return static_cast<int*>(p.dens_off.p) + b * p.dens_off.s[0] + y * p.dens_off.s[1] + x * p.dens_off.s[2];
+  };
 
   auto write_out = [&](float4 c, int term) {
     float* col = static_cast<float*>(p.color.p) + b * p.color.s[0] + y * p.color.s[1] + x * p.color.s[2];
@@ -102,12 +111,15 @@ __global__ void __launch_bounds__(kFastThreads) fast_forward_persistent_kernel(c
     // refill idle lanes; rays that miss the box are finished right here
     while (true) {
       const int id = fetch_rays(counter, total, !active, exhausted);
+      int claim = 0;  // groups of 4 densities the new ray records
       if (id >= 0 && order.pixel(id, b, x, y)) {
         fast_setup(p, x, y, b, r);
         kmax = max_samples(r.tmin, r.tmax, r.step);
         if (kmax == 0 || r.tmin > r.tmax || 0.f > p.early_out) {
           write_out(make_float4(0.f, 0.f, 0.f, 0.f), 0);
+          if (dens4) *dens_off_at() = -1;
         } else {
+          claim = dens4 ? (kmax + 3) >> 2 : 0;
           active = true;
           acc = mk4(0, 0, 0, 0);
           k = 0;
@@ -120,6 +132,26 @@ __global__ void __launch_bounds__(kFastThreads) fast_forward_persistent_kernel(c
           slot = 0;
         }
       }
+      if (dens4) {
+        // room in the pool for the warp's new rays: one 64-bit atomic per warp
+        int incl = claim;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int v = __shfl_up_sync(kFullMask, incl, o);
+          if (lane >= o) incl += v;
+        }
+        const int tot = __shfl_sync(kFullMask, incl, 31);
+        if (tot > 0) {
+          unsigned long long base = 0;
+          if (lane == 31) base = atomicAdd(bump, static_cast<unsigned long long>(tot));
+          base = __shfl_sync(kFullMask, base, 31);
+          if (claim > 0) {
+            const unsigned long long first = base + static_cast<unsigned long long>(incl - claim);
+            dgrp = first + claim <= static_cast<unsigned long long>(p.dens_units) ? int(first) : -1;
+            *dens_off_at() = dgrp;
+          }
+        }
+      }
       if (exhausted || __ballot_sync(kFullMask, !active) == 0u) break;
     }
     if (__ballot_sync(kFullMask, active) == 0u) break;
@@ -130,6 +162,8 @@ __global__ void __launch_bounds__(kFastThreads) fast_forward_persistent_kernel(c
         const float t = r.tmin + k * r.step;
         if (t > r.tmax || acc.w > p.early_out || k >= kmax) {
           write_out(make_float4(acc.x, acc.y, acc.z, acc.w), k);
+          if (dgrp >= 0 && (k & 3) != 0) __stcs(dens4 + dgrp + (k >> 2), dstage);
+          dgrp = -1;
           active = false;
         } else {
           if (ck && k == next_ck) {  // opacity before sample k = (slot+1)*K
@@ -139,6 +173,14 @@ __global__ void __launch_bounds__(kFastThreads) fast_forward_persistent_kernel(c
           }
           const float density = smp.sample(vol, fast_pos(r, t));
           acc = blend<BLEND>(acc, tf_eval<TF>(tf, density), r.step);
+          if (dgrp >= 0) {
+            switch (k & 3) {
+              case 0: dstage.x = density; break;
+              case 1: dstage.y = density; break;
+              case 2: dstage.z = density; break;
+              default: dstage.w = density; __stcs(dens4 + dgrp + (k >> 2), dstage);
+            }
+          }
           ++k;
         }
       }
@@ -152,7 +194,8 @@ template <int FILTER, int TF, int BLEND, bool VOLGRAD, bool TFGRAD, typename VT>
 __global__ void __launch_bounds__(kFastThreads) fast_adjoint_persistent_kernel(const RenderParams p,
                                                                                 const AdjointParams a,
                                                                                 const RayOrder order, int* counter,
-                                                                                float* tf_scratch) {
+                                                                                float* tf_scratch,
+                                                                                const int* ray_list) {
   extern __shared__ float4 fast_smem4[];
   constexpr int C = TfChannels<TF>::C;
   float* smem = reinterpret_cast<float*>(fast_smem4);
@@ -197,6 +240,7 @@ __global__ void __launch_bounds__(kFastThreads) fast_adjoint_persistent_kernel(c
   TfShared<C> tf{s_tf, p.R};
   float* adjv = nullptr;
   const float* ck = nullptr;
+  const float4* drow = nullptr;  // the ray's recorded densities, if any
 
   auto write_ray_grads = [&]() {
     if (a.has_stepsize) {
@@ -226,7 +270,8 @@ __global__ void __launch_bounds__(kFastThreads) fast_adjoint_persistent_kernel(c
   while (true) {
     // refill idle lanes; rays without samples are finished right here
     while (true) {
-      const int id = fetch_rays(counter, total, !active, exhausted);
+      int id = fetch_rays(counter, total, !active, exhausted);
+      if (id >= 0 && ray_list) id = ray_list[id];
       if (id >= 0 && order.pixel(id, b, x, y)) {
         n = static_cast<const int*>(a.fwd_term.p)[b * a.fwd_term.s[0] + y * a.fwd_term.s[1] + x * a.fwd_term.s[2]];
         adj_step = 0.f;
@@ -248,9 +293,15 @@ __global__ void __launch_bounds__(kFastThreads) fast_adjoint_persistent_kernel(c
           tf.p = s_tf + (copies > 1 ? b : 0) * p.R * C;
           adjv = VOLGRAD ? static_cast<float*>(a.adj_volume.p) + b * a.adj_volume.s[0] : nullptr;
           ckpt_ray = p.ckpt.p != nullptr && n <= (p.ckpt_slots + 1) * K;
+          drow = nullptr;
           if (ckpt_ray) {
             ck = static_cast<const float*>(p.ckpt.p) + b * p.ckpt.s[0] + y * p.ckpt.s[1] + x * p.ckpt.s[2];
             j = (n + K - 1) / K - 1;
+            if (p.dens) {
+              const int g = static_cast<const int*>(p.dens_off.p)[b * p.dens_off.s[0] + y * p.dens_off.s[1] +
+                                                                  x * p.dens_off.s[2]];
+              if (g >= 0) drow = reinterpret_cast<const float4*>(p.dens) + g;
+            }
           } else {
             // no checkpoints: invert the blend from the final colour, K samples per round
             const float* fc = static_cast<const float*>(a.fwd_color.p) + b * a.fwd_color.s[0] +
@@ -277,11 +328,19 @@ __global__ void __launch_bounds__(kFastThreads) fast_adjoint_persistent_kernel(c
     const int k1 = ckpt_ray ? min(n, k0 + K) : 0;
     if (seg_len > 0) {
       float alpha = (active && ckpt_ray && j > 0) ? ck[(j - 1) * p.ckpt.s[3]] : 0.f;
+      float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
       for (int kk = 0; kk < K; ++kk) {
         const int k = k0 + kk;
         if (active && ckpt_ray && k < k1) {
-          const float t = r.tmin + k * r.step;
-          const float density = smp.sample(vol, fast_pos(r, t));
+          float density;
+          if (drow) {
+            if (kk == 0 || (k & 3) == 0) q = __ldcs(drow + (k >> 2));
+            const int c = k & 3;
+            density = c == 0 ? q.x : c == 1 ? q.y : c == 2 ? q.z : q.w;
+          } else {
+            const float t = r.tmin + k * r.step;
+            density = smp.sample(vol, fast_pos(r, t));
+          }
           const float a_k = blend_alpha<BLEND>(tf_eval<TF>(tf, density).w, r.step);
           seg_d[kk * blockDim.x] = density;
           seg_a[kk * blockDim.x] = alpha;

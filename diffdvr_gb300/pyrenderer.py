@@ -150,14 +150,23 @@ class RendererOutputs:
 
     ``checkpoints`` (optional, B*H*W*C float32) receives the accumulated opacity
     every ``checkpoint_interval`` samples during the forward pass; see
-    ``Renderer.checkpoint_slots``."""
+    ``Renderer.checkpoint_slots``.
+
+    ``sample_density`` (optional, 1-D float32 pool, with ``sample_offset``, a
+    B*H*W int32 tensor, and checkpoints) receives the density of every sample
+    of each ray; the adjoint then rebuilds its segments from these instead of
+    re-sampling the volume.  Rays that find the pool full are re-sampled;
+    ``Renderer.sample_density_size`` gives a size that holds every ray."""
 
     def __init__(self, color: Optional[torch.Tensor] = None, terminationIndex: Optional[torch.Tensor] = None,
-                 checkpoints: Optional[torch.Tensor] = None, checkpoint_interval: int = 16):
+                 checkpoints: Optional[torch.Tensor] = None, checkpoint_interval: int = 16,
+                 sample_density: Optional[torch.Tensor] = None, sample_offset: Optional[torch.Tensor] = None):
         self.color = color
         self.terminationIndex = terminationIndex
         self.checkpoints = checkpoints
         self.checkpoint_interval = checkpoint_interval
+        self.sample_density = sample_density
+        self.sample_offset = sample_offset
 
 
 class AdjointOutputs:
@@ -264,6 +273,8 @@ def _outputs(out: RendererOutputs) -> _abi.DvrRendererOutputs:
     c.termination_index = _tensor(out.terminationIndex, "terminationIndex")
     c.checkpoints = _tensor(getattr(out, "checkpoints", None), "checkpoints")
     c.checkpoint_interval = int(getattr(out, "checkpoint_interval", 16) or 16)
+    c.sample_density = _tensor(getattr(out, "sample_density", None), "sample_density")
+    c.sample_offset = _tensor(getattr(out, "sample_offset", None), "sample_offset")
     return c
 
 
@@ -350,6 +361,15 @@ class Renderer:
         if n < 0:
             _abi.check(int(n))
         return int(n)
+
+    @staticmethod
+    def sample_density_size(inputs: RendererInputs, batch: int) -> int:
+        """Floats of a RendererOutputs.sample_density pool that holds every
+        ray of a batch-``batch`` image: B*H*W rays of at most 4*ceil(n/4)
+        samples each, n the sample bound from the box diagonal and the
+        smallest step size."""
+        W, H = int(inputs.screen_size.x), int(inputs.screen_size.y)
+        return int(batch) * H * W * 4 * Renderer.checkpoint_slots(inputs, 4)
 
 
 # --------------------------------------------------------------------- module functions

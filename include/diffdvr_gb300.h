@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define DVR_ABI_VERSION 1
+#define DVR_ABI_VERSION 2
 
 /* ---- status codes ---- */
 #define DVR_OK 0
@@ -118,16 +118,29 @@ typedef struct DvrRendererInputs {
   double blending_early_out;     /* default 1 - 1e-5 */
 } DvrRendererInputs;
 
-/* Mirrors renderer::RendererOutputsHost (renderer/renderer.h:67-71), plus an
- * optional transmittance-checkpoint buffer (B*H*W*C float32, ndim < 0 when
- * absent) that the forward pass fills every `checkpoint_interval` samples for
- * the optimized adjoint.  C >= ceil(max samples per ray / interval) - 1. */
+/* Mirrors renderer::RendererOutputsHost (renderer/renderer.h:67-71), plus
+ * state the forward pass records for the optimized adjoint (ndim < 0 when
+ * absent):
+ *  - checkpoints: B*H*W*C float32, the accumulated opacity every
+ *    `checkpoint_interval` samples.  C >= ceil(max samples per ray / interval) - 1.
+ *  - sample_density + sample_offset (both or neither; need checkpoints): a
+ *    1-D float32 pool of any size N (16-byte aligned, contiguous, N >= 4) and
+ *    a B*H*W int32 tensor.  The forward stores the density of every sample of
+ *    a ray in the pool (rays claim room in launch order, a multiple of 4
+ *    floats each) and writes the ray's first float index / 4 to
+ *    sample_offset, or -1 when the pool was full.  The adjoint then rebuilds
+ *    each checkpoint segment from the stored densities instead of re-sampling
+ *    the volume; rays with offset -1 re-sample.  N = B*H*W*S with
+ *    S = 4 * dvr_checkpoint_slots(length, step, 4) holds every ray.
+ *    Written and read by the optimized single-instance entry points only. */
 typedef struct DvrRendererOutputs {
   DvrTensor color;
   DvrTensor termination_index;
   DvrTensor checkpoints;
   int32_t checkpoint_interval;   /* samples between checkpoints; 0 = default (32) */
   int32_t pad_;
+  DvrTensor sample_density;
+  DvrTensor sample_offset;
 } DvrRendererOutputs;
 
 /* Mirrors renderer::AdjointOutputsHost (renderer/renderer.h:95-111). */

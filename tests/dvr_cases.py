@@ -157,8 +157,11 @@ def golden_prefixes(g: dict) -> list:
 
 # ---------------------------------------------------------------- GPU runs
 def gpu_forward(case: Case, family: str = "optimized", volume_dtype=None, tf_dtype=None, checkpoints: bool = False,
-                interval: int = 16):
-    """Renders case on cuda:0; returns (inputs, outputs) with torch tensors."""
+                interval: int = 16, record=None):
+    """Renders case on cuda:0; returns (inputs, outputs) with torch tensors.
+    record: None, "full" (a sample-density pool that holds every ray), a
+    float fraction of that size or an int number of floats (rays that find
+    the pool full are re-sampled)."""
     import torch
     from diffdvr_gb300 import pyrenderer as pr
     pr.set_kernel_family(family)
@@ -171,6 +174,16 @@ def gpu_forward(case: Case, family: str = "optimized", volume_dtype=None, tf_dty
         ck = torch.full((B, case.height, case.width, pr.Renderer.checkpoint_slots(inp, interval)), float("nan"),
                         device="cuda")
     out = pr.RendererOutputs(color, term, ck, interval)
+    if record is not None:
+        full = pr.Renderer.sample_density_size(inp, B)
+        if record == "full":
+            n = full
+        elif isinstance(record, int):
+            n = max(4, record // 4 * 4)
+        else:
+            n = max(4, int(full * float(record)) // 4 * 4)
+        out.sample_density = torch.full((n,), float("nan"), device="cuda")
+        out.sample_offset = torch.full((B, case.height, case.width), -7, dtype=torch.int32, device="cuda")
     pr.Renderer.render_forward(inp, out)
     torch.cuda.synchronize()
     return inp, out

@@ -26,7 +26,7 @@ def test_library_exports_every_header_symbol(dvr_lib):
     for n in names:
         assert hasattr(dvr_lib, n), n
     assert set(names) == set(_abi.SIGNATURES)
-    assert dvr_lib.dvr_abi_version() == 1
+    assert dvr_lib.dvr_abi_version() == 2
 
 
 def _fake(shape, dtype=_abi.DVR_FLOAT32, cuda=True, ptr=0x100000):

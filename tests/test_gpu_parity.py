@@ -129,9 +129,9 @@ def reference_adjoint(case, O, gpu_term, adj, req, oracle_case=None):
     return O.adjoint(sc, c64, t64, adj, req, "port", "f64"), adj
 
 
-def _adjoint_case(case, family, O, checkpoints, stepsize, interval=16):
+def _adjoint_case(case, family, O, checkpoints, stepsize, interval=16, record=None):
     cam = case.camera_mode == 0
-    inp, out = gpu_forward(case, family, checkpoints=checkpoints, interval=interval)
+    inp, out = gpu_forward(case, family, checkpoints=checkpoints, interval=interval, record=record)
     term = out.terminationIndex.cpu().numpy()
     adj = np.random.default_rng(7).normal(size=out.color.shape).astype(np.float32)
     req = O.AdjointRequest(volume=True, tf=True, camera=cam, stepsize=stepsize)
@@ -145,9 +145,13 @@ def _adjoint_case(case, family, O, checkpoints, stepsize, interval=16):
     return got, ref, r32
 
 
-@pytest.mark.parametrize("family,checkpoints,interval", [("plain", False, 16), ("optimized", False, 16),
-                                                         ("optimized", True, 16), ("optimized", True, 5)])
-def test_adjoint_all_modes(family, checkpoints, interval, oracle_built, cuda_device):
+@pytest.mark.parametrize("family,checkpoints,interval,record", [
+    ("plain", False, 16, None), ("optimized", False, 16, None), ("optimized", True, 16, None),
+    ("optimized", True, 5, None),
+    # sample densities recorded by the forward: a pool for every ray, and one
+    # for about half of them (the rest re-sample the volume)
+    ("optimized", True, 16, "full"), ("optimized", True, 5, 0.15)])
+def test_adjoint_all_modes(family, checkpoints, interval, record, oracle_built, cuda_device):
     O = oracle_built
     failures = {}
     for i, (tfm, filt, blend, cam) in enumerate(all_mode_combos()):
@@ -155,7 +159,8 @@ def test_adjoint_all_modes(family, checkpoints, interval, oracle_built, cuda_dev
                          pad_faces=True)
         # the optimized family returns the full step-size derivative, the
         # reference (and the oracle) only the last blend term; checked by FD below
-        got, ref, r32 = _adjoint_case(case, family, O, checkpoints, stepsize=(family == "plain"), interval=interval)
+        got, ref, r32 = _adjoint_case(case, family, O, checkpoints, stepsize=(family == "plain"), interval=interval,
+                                      record=record)
         bad = _grad_errors(got, ref, r32)
         if bad:
             failures[(tfm, filt, blend, cam)] = bad
@@ -421,3 +426,48 @@ def test_invalid_inputs_raise(cuda_device):
     wrong = pr.RendererOutputs(out.color[:, :, :-1], out.terminationIndex)
     with pytest.raises(RuntimeError, match="color must have"):
         pr.Renderer.render_forward(inp, wrong)
+
+
+@pytest.mark.parametrize("fraction", ["full", 0.5])
+def test_sample_density_record(fraction, cuda_device):
+    """The forward's density record: every ray with samples that got room
+    holds n finite densities inside the volume's range in its own disjoint
+    4-aligned run of the pool; rays without samples or without room are -1;
+    the adjoint from the record equals the re-sampling adjoint (same kernels,
+    the densities are the re-march's own values, so only the order of float
+    atomics differs: relative L2 <= 1e-5)."""
+    case = make_case(71, tf_mode=1, filter_mode=1, blend_mode=0, shape=(20, 24, 28), W=40, H=36, B=2, R=32,
+                     opacity=0.3, pad_faces=True)
+    inp, out = gpu_forward(case, checkpoints=True, record="full")
+    if fraction != "full":
+        # a pool for about half of the samples the rays actually recorded
+        t = out.terminationIndex.cpu().numpy()
+        inp, out = gpu_forward(case, checkpoints=True, record=int(fraction * 4 * ((t + 3) // 4).sum()))
+    term = out.terminationIndex.cpu().numpy()
+    off = out.sample_offset.cpu().numpy()
+    pool = out.sample_density.cpu().numpy()
+    assert ((off >= 0) | (off == -1)).all()
+    assert (off[term == 0] == -1).all()
+    hit = (term > 0) & (off >= 0)
+    if fraction == "full":
+        assert (off[term > 0] >= 0).all()
+    else:
+        assert ((term > 0) & (off == -1)).any() and hit.any()
+    lo, hi = float(case.volume.min()), float(case.volume.max())
+    starts, ends = [], []
+    for o, n in zip(off[hit], term[hit]):
+        d = pool[4 * o: 4 * o + n]
+        assert len(d) == n and np.isfinite(d).all() and d.min() >= lo - 1e-6 and d.max() <= hi + 1e-6
+        starts.append(4 * o)
+        ends.append(4 * o + n)
+    order = np.argsort(starts)
+    assert (np.asarray(starts)[order][1:] >= np.asarray(ends)[order][:-1]).all()
+    assert max(ends) <= pool.size
+
+    rng = np.random.default_rng(3)
+    adj = rng.standard_normal(out.color.shape).astype(np.float32)
+    got = gpu_adjoint(case, inp, out, adj, volume=True, tf=True, camera=True, stepsize=True)
+    plain_out = type(out)(out.color, out.terminationIndex, out.checkpoints, out.checkpoint_interval)
+    ref = gpu_adjoint(case, inp, plain_out, adj, volume=True, tf=True, camera=True, stepsize=True)
+    for k in ref:
+        assert rel_l2(got[k], ref[k]) <= 1e-5, (k, rel_l2(got[k], ref[k]))
