@@ -106,10 +106,15 @@ cudaError_t launch_fast_forward_vt(const RenderParams& p, int filter, int blend,
   cudaError_t err;
   int* counter = acquire_counter(li.device, s, err);
   if (!counter) return err;
+  int* order_ints = static_cast<int*>(acquire_scratch(li.device, s, work_order_ints(p) * sizeof(int), err));
+  if (!order_ints) return err;
+  err = order_rays_by_work(p, nullptr, order_ints, li, s);
+  if (err != cudaSuccess) return err;
   auto go = [&](auto kernel) {
     cudaError_t e = set_smem(kernel, smem);
     if (e != cudaSuccess) return e;
-    kernel<<<persistent_grid(kernel, smem, order.total(), li), kFastThreads, smem, s>>>(p, order, counter);
+    kernel<<<persistent_grid(kernel, smem, order.total(), li), kFastThreads, smem, s>>>(
+        p, order, counter, order_ints + work_order_list_offset);
     return cudaGetLastError();
   };
   if (filter == kNearest)
@@ -144,7 +149,7 @@ static cudaError_t fast_adjoint_go(const RenderParams& p, const AdjointParams& a
     char* scratch = static_cast<char*>(acquire_scratch(li.device, s, list_bytes + tf_bytes, e));
     if (!scratch) return e;
     int* order_ints = reinterpret_cast<int*>(scratch);
-    e = order_rays_by_work(p, a, order_ints, li, s);
+    e = order_rays_by_work(p, &a, order_ints, li, s);
     if (e != cudaSuccess) return e;
     kernel<<<grid, kFastThreads, smem, s>>>(p, a, order, counter, tfgrad ? reinterpret_cast<float*>(scratch + list_bytes)
                                                                        : nullptr,

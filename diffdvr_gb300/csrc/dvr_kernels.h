@@ -33,12 +33,14 @@ struct CallerScratch {
   size_t tf_bytes;
 };
 
-// Longest-first ray order for the persistent adjoint: ray ids bucketed by
-// descending forward sample count.  scratch holds work_order_ints(p) ints; the
-// ordered list starts at scratch + work_order_list_offset.
+// Longest-first ray order for the persistent kernels: ray ids bucketed by
+// descending sample count (the forward's termination index for the adjoint,
+// a = its parameters; the sample bound of the ray for the forward, a =
+// nullptr).  scratch holds work_order_ints(p) ints; the ordered list starts at
+// scratch + work_order_list_offset.
 constexpr size_t work_order_list_offset = 512;
 size_t work_order_ints(const RenderParams& p);
-cudaError_t order_rays_by_work(const RenderParams& p, const AdjointParams& a, int* scratch, const LaunchInfo& li,
+cudaError_t order_rays_by_work(const RenderParams& p, const AdjointParams* a, int* scratch, const LaunchInfo& li,
                                cudaStream_t s);
 
 // Plain family (reference semantics).

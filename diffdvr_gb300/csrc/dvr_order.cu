@@ -1,13 +1,15 @@
-// Longest-first ray order for the persistent adjoint.
+// Longest-first ray order for the persistent kernels.
 //
-// The adjoint knows each ray's exact work, the forward's termination index n
-// (samples).  With one or two rays per resident lane, fetching rays in pixel
-// order lets a long ray fetched late set the end of the launch while the other
-// warps wait.  These kernels bucket the ray ids by descending n (key = 255 -
+// With one or two rays per resident lane, fetching rays in pixel order lets a
+// long ray fetched late set the end of the launch while the other warps wait.
+// These kernels bucket the ray ids by descending work n (key = 255 -
 // min(255, floor(4 sqrt(n))): buckets a few samples wide for short rays, a
 // few tens for rays of thousands of samples) so the tail of the launch is made
-// of short rays.  Within a bucket, ids of one block of consecutive rays stay
-// together, so neighbouring rays are still fetched by the same warp.
+// of short rays.  The adjoint's n is exact, the forward's termination index;
+// the forward's is the ray's sample bound from the box entry and exit (early
+// termination may end it sooner).  Within a bucket, ids of one block of
+// consecutive rays stay together, so neighbouring rays are still fetched by
+// the same warp.
 #include "dvr_kernels.h"
 #include "dvr_persist.cuh"
 
@@ -18,14 +20,23 @@ constexpr int kBuckets = 256;
 constexpr int kOrderThreads = 256;
 static_assert(work_order_list_offset == 2 * kBuckets, "list follows the histogram and the bucket starts");
 
+template <bool FWD>
 __device__ __forceinline__ int work_key(const RenderParams& p, const AdjointParams& a, const RayOrder& o, int id) {
   int b, x, y;
   if (!o.pixel(id, b, x, y)) return kBuckets - 1;
-  const int n = static_cast<const int*>(a.fwd_term.p)[b * a.fwd_term.s[0] + y * a.fwd_term.s[1] + x * a.fwd_term.s[2]];
+  int n;
+  if constexpr (FWD) {
+    FastRay r;
+    fast_setup(p, x, y, b, r);
+    n = max_samples(r.tmin, r.tmax, r.step);
+  } else {
+    n = static_cast<const int*>(a.fwd_term.p)[b * a.fwd_term.s[0] + y * a.fwd_term.s[1] + x * a.fwd_term.s[2]];
+  }
   const int r = n <= 0 ? 0 : min(kBuckets - 1, int(sqrtf(float(n)) * 4.f));
   return kBuckets - 1 - r;
 }
 
+template <bool FWD>
 __global__ void __launch_bounds__(kOrderThreads) work_histogram_kernel(const RenderParams p, const AdjointParams a,
                                                                        const RayOrder o, int* hist) {
   __shared__ int sh[kBuckets];
@@ -33,7 +44,7 @@ __global__ void __launch_bounds__(kOrderThreads) work_histogram_kernel(const Ren
   __syncthreads();
   const int total = int(o.total());
   for (int id = blockIdx.x * kOrderThreads + threadIdx.x; id < total; id += gridDim.x * kOrderThreads)
-    atomicAdd(&sh[work_key(p, a, o, id)], 1);
+    atomicAdd(&sh[work_key<FWD>(p, a, o, id)], 1);
   __syncthreads();
   if (sh[threadIdx.x] > 0) atomicAdd(&hist[threadIdx.x], sh[threadIdx.x]);
 }
@@ -52,6 +63,7 @@ __global__ void __launch_bounds__(kOrderThreads) work_scan_kernel(const int* his
   start[threadIdx.x] = sh[threadIdx.x] - hist[threadIdx.x];
 }
 
+template <bool FWD>
 __global__ void __launch_bounds__(kOrderThreads) work_scatter_kernel(const RenderParams p, const AdjointParams a,
                                                                      const RayOrder o, int* start, int* list) {
   __shared__ int cnt[kBuckets];
@@ -61,7 +73,7 @@ __global__ void __launch_bounds__(kOrderThreads) work_scatter_kernel(const Rende
     cnt[threadIdx.x] = 0;
     __syncthreads();
     const int id = first + threadIdx.x;
-    const int key = id < total ? work_key(p, a, o, id) : 0;
+    const int key = id < total ? work_key<FWD>(p, a, o, id) : 0;
     const int rank = id < total ? atomicAdd(&cnt[key], 1) : 0;
     __syncthreads();
     if (cnt[threadIdx.x] > 0) base[threadIdx.x] = atomicAdd(&start[threadIdx.x], cnt[threadIdx.x]);
@@ -75,7 +87,7 @@ __global__ void __launch_bounds__(kOrderThreads) work_scatter_kernel(const Rende
 
 size_t work_order_ints(const RenderParams& p) { return 2 * kBuckets + size_t(RayOrder::make(p.W, p.H, p.B).total()); }
 
-cudaError_t order_rays_by_work(const RenderParams& p, const AdjointParams& a, int* scratch, const LaunchInfo& li,
+cudaError_t order_rays_by_work(const RenderParams& p, const AdjointParams* a, int* scratch, const LaunchInfo& li,
                                cudaStream_t s) {
   const RayOrder o = RayOrder::make(p.W, p.H, p.B);
   const int64_t total = o.total();
@@ -86,9 +98,16 @@ cudaError_t order_rays_by_work(const RenderParams& p, const AdjointParams& a, in
   cudaError_t e = cudaMemsetAsync(hist, 0, kBuckets * sizeof(int), s);
   if (e != cudaSuccess) return e;
   const int blocks = int(std::min<int64_t>((total + kOrderThreads - 1) / kOrderThreads, int64_t(li.num_sms) * 8));
-  work_histogram_kernel<<<blocks, kOrderThreads, 0, s>>>(p, a, o, hist);
-  work_scan_kernel<<<1, kOrderThreads, 0, s>>>(hist, start);
-  work_scatter_kernel<<<blocks, kOrderThreads, 0, s>>>(p, a, o, start, list);
+  if (a) {
+    work_histogram_kernel<false><<<blocks, kOrderThreads, 0, s>>>(p, *a, o, hist);
+    work_scan_kernel<<<1, kOrderThreads, 0, s>>>(hist, start);
+    work_scatter_kernel<false><<<blocks, kOrderThreads, 0, s>>>(p, *a, o, start, list);
+  } else {
+    const AdjointParams none{};
+    work_histogram_kernel<true><<<blocks, kOrderThreads, 0, s>>>(p, none, o, hist);
+    work_scan_kernel<<<1, kOrderThreads, 0, s>>>(hist, start);
+    work_scatter_kernel<true><<<blocks, kOrderThreads, 0, s>>>(p, none, o, start, list);
+  }
   return cudaGetLastError();
 }
 

@@ -69,7 +69,7 @@ __device__ __forceinline__ int tf_copies(const RenderParams& p) { return p.tf.s[
 // ----------------------------------------------------------------- forward
 template <int FILTER, int TF, int BLEND, typename VT>
 __global__ void __launch_bounds__(kFastThreads) fast_forward_persistent_kernel(const RenderParams p, const RayOrder order,
-                                                                                int* counter) {
+                                                                                int* counter, const int* ray_list) {
   extern __shared__ float4 fast_smem4[];
   constexpr int C = TfChannels<TF>::C;
   float* s_tf = reinterpret_cast<float*>(fast_smem4);
@@ -110,7 +110,8 @@ __global__ void __launch_bounds__(kFastThreads) fast_forward_persistent_kernel(c
   while (true) {
     // refill idle lanes; rays that miss the box are finished right here
     while (true) {
-      const int id = fetch_rays(counter, total, !active, exhausted);
+      int id = fetch_rays(counter, total, !active, exhausted);
+      if (id >= 0 && ray_list) id = ray_list[id];
       int claim = 0;  // groups of 4 densities the new ray records
       if (id >= 0 && order.pixel(id, b, x, y)) {
         fast_setup(p, x, y, b, r);
