@@ -4,7 +4,7 @@
 // library's pool; batched calls launch one block per (instance, batch entry,
 // tile) work item.
 #pragma once
-#include "dvr_persist.cuh"
+#include "dvr_record.cuh"
 #include "dvr_kernels.h"
 
 namespace dvr {
@@ -124,6 +124,47 @@ cudaError_t launch_fast_forward_vt(const RenderParams& p, int filter, int blend,
                                : go(fast_forward_persistent_kernel<kTrilinear, TF, kAlphaBlend, VT>);
 }
 
+// TF-gradient-only adjoint of a texture TF from the sample-density record:
+// longest-first order, the record kernel, then the general kernel over the
+// rays the record does not cover (usually none; a small grid).
+template <int FILTER, int BLEND, typename VT>
+static cudaError_t fast_adjoint_record_go(const RenderParams& p, const AdjointParams& a, const RayOrder& order,
+                                          int* counter, size_t rsmem, size_t gsmem, const LaunchInfo& li,
+                                          cudaStream_t s) {
+  constexpr int C = 4;
+  const int64_t total = order.total();
+  auto rec = fast_adjoint_record_kernel<BLEND>;
+  auto gen = fast_adjoint_persistent_kernel<FILTER, kTfTexture, BLEND, false, true, VT>;
+  cudaError_t e = set_smem(rec, rsmem);
+  if (e != cudaSuccess) return e;
+  e = set_smem(gen, gsmem);
+  if (e != cudaSuccess) return e;
+  const int rgrid = persistent_grid(rec, rsmem, total, li);
+  const int ggrid = li.num_sms;
+  // scratch: order ints, leftover list, the general kernel's TF-gradient slices
+  const size_t order_bytes = (work_order_ints(p) * sizeof(int) + 255) & ~size_t(255);
+  const size_t left_bytes = (size_t(total) * sizeof(int) + 255) & ~size_t(255);
+  const size_t tf_bytes = (size_t(ggrid) * p.R * C * sizeof(float) + 255) & ~size_t(255);
+  const size_t slice_bytes = size_t(rgrid) * (kFastThreads / 32) * p.R * C * sizeof(float);
+  char* scratch =
+      static_cast<char*>(acquire_scratch(li.device, s, order_bytes + left_bytes + tf_bytes + slice_bytes, e));
+  if (!scratch) return e;
+  int* order_ints = reinterpret_cast<int*>(scratch);
+  int* leftover = reinterpret_cast<int*>(scratch + order_bytes);
+  e = order_rays_by_work(p, &a, order_ints, li, s);
+  if (e != cudaSuccess) return e;
+  rec<<<rgrid, kFastThreads, rsmem, s>>>(p, a, order, counter, order_ints + work_order_list_offset, leftover,
+                                         reinterpret_cast<float*>(scratch + order_bytes + left_bytes + tf_bytes));
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  int* counter2 = acquire_counter(li.device, s, e);
+  if (!counter2) return e;
+  gen<<<ggrid, kFastThreads, gsmem, s>>>(p, a, order, counter2,
+                                         reinterpret_cast<float*>(scratch + order_bytes + left_bytes), leftover,
+                                         counter + 1);
+  return cudaGetLastError();
+}
+
 template <int FILTER, int TF, int BLEND, typename VT>
 static cudaError_t fast_adjoint_go(const RenderParams& p, const AdjointParams& a, const LaunchInfo& li,
                                    cudaStream_t s) {
@@ -153,9 +194,20 @@ static cudaError_t fast_adjoint_go(const RenderParams& p, const AdjointParams& a
     if (e != cudaSuccess) return e;
     kernel<<<grid, kFastThreads, smem, s>>>(p, a, order, counter, tfgrad ? reinterpret_cast<float*>(scratch + list_bytes)
                                                                        : nullptr,
-                                            order_ints + work_order_list_offset);
+                                            order_ints + work_order_list_offset, nullptr);
     return cudaGetLastError();
   };
+  if constexpr (TF == kTfTexture) {
+    // TF gradient only, from the sample-density record
+    if (tfgrad && !volgrad && !a.has_camera && !a.has_stepsize && p.dens && p.ckpt.p) {
+      const bool per_batch = a.adj_tf.s[0] != 0;
+      (void)per_batch;
+      const size_t rsmem = size_t(RecordSmem(p.R, C, kFastThreads, p.ckpt_interval, copies, false).total) *
+                           sizeof(float);
+      if (rsmem <= size_t(li.max_smem_optin))
+        return fast_adjoint_record_go<FILTER, BLEND, VT>(p, a, order, counter, rsmem, smem, li, s);
+    }
+  }
   if (volgrad)
     return tfgrad ? go(fast_adjoint_persistent_kernel<FILTER, TF, BLEND, true, true, VT>)
                   : go(fast_adjoint_persistent_kernel<FILTER, TF, BLEND, true, false, VT>);
@@ -196,7 +248,7 @@ static cudaError_t fast_adjoint_into_go(const RenderParams& p, const AdjointPara
     cudaError_t e = set_smem(kernel, smem);
     if (e != cudaSuccess) return e;
     const int grid = int(std::min<int64_t>(persistent_grid(kernel, smem, order.total(), li), fit));
-    kernel<<<grid, kFastThreads, smem, s>>>(p, a, order, sc.counter, sc.tf, nullptr);
+    kernel<<<grid, kFastThreads, smem, s>>>(p, a, order, sc.counter, sc.tf, nullptr, nullptr);
     return cudaGetLastError();
   };
   if (volgrad)

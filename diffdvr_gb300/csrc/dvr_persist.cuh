@@ -196,7 +196,8 @@ __global__ void __launch_bounds__(kFastThreads) fast_adjoint_persistent_kernel(c
                                                                                 const AdjointParams a,
                                                                                 const RayOrder order, int* counter,
                                                                                 float* tf_scratch,
-                                                                                const int* ray_list) {
+                                                                                const int* ray_list,
+                                                                                const int* ray_count) {
   extern __shared__ float4 fast_smem4[];
   constexpr int C = TfChannels<TF>::C;
   float* smem = reinterpret_cast<float*>(fast_smem4);
@@ -225,7 +226,8 @@ __global__ void __launch_bounds__(kFastThreads) fast_adjoint_persistent_kernel(c
   float* seg_d = smem + L.seg + threadIdx.x;  // [offset][thread]
   float* seg_a = smem + L.seg + K * blockDim.x + threadIdx.x;
 
-  const int total = int(order.total());
+  // rays to process: the whole order, or the first *ray_count entries of ray_list
+  const int total = ray_count ? *ray_count : int(order.total());
   bool exhausted = false, active = false;
   int b = 0, x = 0, y = 0, n = 0, j = 0;
   bool ckpt_ray = false;

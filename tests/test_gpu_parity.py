@@ -471,3 +471,31 @@ def test_sample_density_record(fraction, cuda_device):
     ref = gpu_adjoint(case, inp, plain_out, adj, volume=True, tf=True, camera=True, stepsize=True)
     for k in ref:
         assert rel_l2(got[k], ref[k]) <= 1e-5, (k, rel_l2(got[k], ref[k]))
+
+
+@pytest.mark.parametrize("blend,per_batch,pool", [(0, False, "full"), (1, False, "full"), (0, True, "full"),
+                                                  (1, False, 0.5)])
+def test_tf_only_adjoint_from_record(blend, per_batch, pool, oracle_built, cuda_device):
+    """TF gradient alone with checkpoints and a sample-density record (the
+    texture-TF record kernel; rays without room in the pool go through the
+    general kernel) against the FP64 oracle, tolerances as above; per_batch:
+    a TF per batch entry and a TF gradient per batch entry."""
+    O = oracle_built
+    rng = np.random.default_rng(11 + blend)
+    case = make_case(90 + blend, tf_mode=1, filter_mode=1, blend_mode=blend, shape=(20, 24, 28), W=40, H=36, B=2,
+                     R=32, opacity=0.3, pad_faces=True)
+    if not per_batch:
+        case.tf = np.ascontiguousarray(case.tf[:1])  # one TF for both views, one TF gradient
+    inp, out = gpu_forward(case, checkpoints=True, record="full")
+    if pool != "full":
+        t = out.terminationIndex.cpu().numpy()
+        inp, out = gpu_forward(case, checkpoints=True, record=int(pool * 4 * ((t + 3) // 4).sum()))
+        t = out.terminationIndex.cpu().numpy()
+        assert (out.sample_offset.cpu().numpy()[t > 0] == -1).any()
+    term = out.terminationIndex.cpu().numpy()
+    adj = rng.standard_normal(out.color.shape).astype(np.float32)
+    ref, adj = reference_adjoint(case, O, term, adj, O.AdjointRequest(tf=True))
+    got = gpu_adjoint(case, inp, out, adj, tf=True)
+    assert got["adj_tf"].shape == case.tf.shape
+    bad = _grad_errors(got, ref)
+    assert not bad, bad
