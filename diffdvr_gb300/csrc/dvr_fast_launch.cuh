@@ -5,6 +5,7 @@
 // tile) work item.
 #pragma once
 #include "dvr_record.cuh"
+#include "dvr_warpray.cuh"
 #include "dvr_kernels.h"
 
 namespace dvr {
@@ -113,15 +114,16 @@ cudaError_t launch_fast_forward_vt(const RenderParams& p, int filter, int blend,
   auto go = [&](auto kernel) {
     cudaError_t e = set_smem(kernel, smem);
     if (e != cudaSuccess) return e;
-    kernel<<<persistent_grid(kernel, smem, order.total(), li), kFastThreads, smem, s>>>(
-        p, order, counter, order_ints + work_order_list_offset);
+    // one warp per ray: as many warps as fit, up to one per ray
+    kernel<<<persistent_grid(kernel, smem, order.total() * 32, li), kFastThreads, smem, s>>>(
+        p, order, counter, order_ints + work_order_list_offset, order_ints + work_order_count_offset);
     return cudaGetLastError();
   };
   if (filter == kNearest)
-    return blend == kBeerLambert ? go(fast_forward_persistent_kernel<kNearest, TF, kBeerLambert, VT>)
-                                 : go(fast_forward_persistent_kernel<kNearest, TF, kAlphaBlend, VT>);
-  return blend == kBeerLambert ? go(fast_forward_persistent_kernel<kTrilinear, TF, kBeerLambert, VT>)
-                               : go(fast_forward_persistent_kernel<kTrilinear, TF, kAlphaBlend, VT>);
+    return blend == kBeerLambert ? go(fast_forward_warp_kernel<kNearest, TF, kBeerLambert, VT>)
+                                 : go(fast_forward_warp_kernel<kNearest, TF, kAlphaBlend, VT>);
+  return blend == kBeerLambert ? go(fast_forward_warp_kernel<kTrilinear, TF, kBeerLambert, VT>)
+                               : go(fast_forward_warp_kernel<kTrilinear, TF, kAlphaBlend, VT>);
 }
 
 // TF-gradient-only adjoint of a texture TF from the sample-density record:

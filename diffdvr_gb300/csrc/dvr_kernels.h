@@ -37,8 +37,11 @@ struct CallerScratch {
 // descending sample count (the forward's termination index for the adjoint,
 // a = its parameters; the sample bound of the ray for the forward, a =
 // nullptr).  scratch holds work_order_ints(p) ints; the ordered list starts at
-// scratch + work_order_list_offset.
-constexpr size_t work_order_list_offset = 512;
+// scratch + work_order_list_offset, and scratch[work_order_count_offset] is
+// the number of rays with samples, which come first.  The forward ordering
+// also finishes the rays without samples (zero outputs).
+constexpr size_t work_order_count_offset = 512;
+constexpr size_t work_order_list_offset = 516;
 size_t work_order_ints(const RenderParams& p);
 cudaError_t order_rays_by_work(const RenderParams& p, const AdjointParams* a, int* scratch, const LaunchInfo& li,
                                cudaStream_t s);

@@ -10,6 +10,11 @@
 // termination may end it sooner).  Within a bucket, ids of one block of
 // consecutive rays stay together, so neighbouring rays are still fetched by
 // the same warp.
+//
+// For the forward, rays without samples (outside the image or missing the
+// box) form the last bucket; the scatter pass writes their outputs (zero
+// colour and sample count, no density record) and the scan publishes the
+// number of rays before that bucket, which is all the forward kernel marches.
 #include "dvr_kernels.h"
 #include "dvr_persist.cuh"
 
@@ -18,7 +23,8 @@ namespace {
 
 constexpr int kBuckets = 256;
 constexpr int kOrderThreads = 256;
-static_assert(work_order_list_offset == 2 * kBuckets, "list follows the histogram and the bucket starts");
+static_assert(work_order_count_offset == 2 * kBuckets && work_order_list_offset > work_order_count_offset,
+              "histogram, bucket starts, count of rays with work, list");
 
 template <bool FWD>
 __device__ __forceinline__ int work_key(const RenderParams& p, const AdjointParams& a, const RayOrder& o, int id) {
@@ -49,8 +55,9 @@ __global__ void __launch_bounds__(kOrderThreads) work_histogram_kernel(const Ren
   if (sh[threadIdx.x] > 0) atomicAdd(&hist[threadIdx.x], sh[threadIdx.x]);
 }
 
-// exclusive scan of the histogram into the bucket starts (one block)
-__global__ void __launch_bounds__(kOrderThreads) work_scan_kernel(const int* hist, int* start) {
+// exclusive scan of the histogram into the bucket starts (one block); the
+// start of the last bucket (rays without samples) is the number of rays with work
+__global__ void __launch_bounds__(kOrderThreads) work_scan_kernel(const int* hist, int* start, int* with_work) {
   __shared__ int sh[kBuckets];
   sh[threadIdx.x] = hist[threadIdx.x];
   __syncthreads();
@@ -61,6 +68,20 @@ __global__ void __launch_bounds__(kOrderThreads) work_scan_kernel(const int* his
     __syncthreads();
   }
   start[threadIdx.x] = sh[threadIdx.x] - hist[threadIdx.x];
+  if (threadIdx.x == kBuckets - 1) *with_work = sh[threadIdx.x] - hist[threadIdx.x];
+}
+
+// outputs of a forward ray without samples
+__device__ __forceinline__ void finish_empty_ray(const RenderParams& p, const RayOrder& o, int id) {
+  int b, x, y;
+  if (!o.pixel(id, b, x, y)) return;
+  float* col = static_cast<float*>(p.color.p) + b * p.color.s[0] + y * p.color.s[1] + x * p.color.s[2];
+  col[0] = 0.f;
+  col[p.color.s[3]] = 0.f;
+  col[2 * p.color.s[3]] = 0.f;
+  col[3 * p.color.s[3]] = 0.f;
+  static_cast<int*>(p.term.p)[b * p.term.s[0] + y * p.term.s[1] + x * p.term.s[2]] = 0;
+  if (p.dens) static_cast<int*>(p.dens_off.p)[b * p.dens_off.s[0] + y * p.dens_off.s[1] + x * p.dens_off.s[2]] = -1;
 }
 
 template <bool FWD>
@@ -78,14 +99,19 @@ __global__ void __launch_bounds__(kOrderThreads) work_scatter_kernel(const Rende
     __syncthreads();
     if (cnt[threadIdx.x] > 0) base[threadIdx.x] = atomicAdd(&start[threadIdx.x], cnt[threadIdx.x]);
     __syncthreads();
-    if (id < total) list[base[key] + rank] = id;
+    if (id < total) {
+      list[base[key] + rank] = id;
+      if (FWD && key == kBuckets - 1) finish_empty_ray(p, o, id);
+    }
     __syncthreads();
   }
 }
 
 }  // namespace
 
-size_t work_order_ints(const RenderParams& p) { return 2 * kBuckets + size_t(RayOrder::make(p.W, p.H, p.B).total()); }
+size_t work_order_ints(const RenderParams& p) {
+  return work_order_list_offset + size_t(RayOrder::make(p.W, p.H, p.B).total());
+}
 
 cudaError_t order_rays_by_work(const RenderParams& p, const AdjointParams* a, int* scratch, const LaunchInfo& li,
                                cudaStream_t s) {
@@ -94,18 +120,19 @@ cudaError_t order_rays_by_work(const RenderParams& p, const AdjointParams* a, in
   if (total == 0) return cudaSuccess;
   int* hist = scratch;
   int* start = scratch + kBuckets;
-  int* list = scratch + 2 * kBuckets;
+  int* with_work = scratch + work_order_count_offset;
+  int* list = scratch + work_order_list_offset;
   cudaError_t e = cudaMemsetAsync(hist, 0, kBuckets * sizeof(int), s);
   if (e != cudaSuccess) return e;
   const int blocks = int(std::min<int64_t>((total + kOrderThreads - 1) / kOrderThreads, int64_t(li.num_sms) * 8));
   if (a) {
     work_histogram_kernel<false><<<blocks, kOrderThreads, 0, s>>>(p, *a, o, hist);
-    work_scan_kernel<<<1, kOrderThreads, 0, s>>>(hist, start);
+    work_scan_kernel<<<1, kOrderThreads, 0, s>>>(hist, start, with_work);
     work_scatter_kernel<false><<<blocks, kOrderThreads, 0, s>>>(p, *a, o, start, list);
   } else {
     const AdjointParams none{};
     work_histogram_kernel<true><<<blocks, kOrderThreads, 0, s>>>(p, none, o, hist);
-    work_scan_kernel<<<1, kOrderThreads, 0, s>>>(hist, start);
+    work_scan_kernel<<<1, kOrderThreads, 0, s>>>(hist, start, with_work);
     work_scatter_kernel<true><<<blocks, kOrderThreads, 0, s>>>(p, none, o, start, list);
   }
   return cudaGetLastError();

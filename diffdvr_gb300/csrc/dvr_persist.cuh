@@ -1,4 +1,5 @@
-// Persistent forward and adjoint kernels with per-lane ray refill.
+// Persistent adjoint kernel with per-lane ray refill, and the ray numbering
+// and work fetching shared by the persistent kernels.
 //
 // One block per SM slot stays resident; each warp pulls rays from a global
 // counter whenever some of its lanes are idle (one atomicAdd per refill for
@@ -8,8 +9,7 @@
 // batch entries), so the rays a warp fetches together are neighbours and their
 // corner gathers share cache lines.
 //
-// The forward advances every active lane a few samples per round.  The
-// adjoint keeps the lanes of a warp in lock step at segment granularity: per
+// The adjoint keeps the lanes of a warp in lock step at segment granularity: per
 // round each active lane re-marches one K-sample segment of its ray from its
 // checkpoint and runs the reverse recursion over it; lanes may be on different
 // rays and segment indices.  The per-step math is that of dvr_fast.cuh.
@@ -19,7 +19,6 @@
 namespace dvr {
 
 constexpr int kPatchW = 8, kPatchH = 4;
-constexpr int kFwdChunk = 16;  // forward samples per lane between refills
 constexpr unsigned kFullMask = 0xffffffffu;
 
 // Ray numbering in 8x4 patches.
@@ -65,130 +64,6 @@ __device__ __forceinline__ int fetch_rays(int* counter, int total, bool idle, bo
 }
 
 __device__ __forceinline__ int tf_copies(const RenderParams& p) { return p.tf.s[0] == 0 ? 1 : p.B; }
-
-// ----------------------------------------------------------------- forward
-template <int FILTER, int TF, int BLEND, typename VT>
-__global__ void __launch_bounds__(kFastThreads) fast_forward_persistent_kernel(const RenderParams p, const RayOrder order,
-                                                                                int* counter, const int* ray_list) {
-  extern __shared__ float4 fast_smem4[];
-  constexpr int C = TfChannels<TF>::C;
-  float* s_tf = reinterpret_cast<float*>(fast_smem4);
-  const int copies = tf_copies(p);
-  for (int bb = 0; bb < copies; ++bb) stage_tf(p, bb, s_tf + bb * p.R * C);
-  __syncthreads();
-
-  const int total = int(order.total());
-  bool exhausted = false, active = false;
-  int b = 0, x = 0, y = 0, k = 0, next_ck = 0, slot = 0, kmax = 0;
-  FastRay r{};
-  f4 acc = mk4(0, 0, 0, 0);
-  Sampler<FILTER, VT> smp;
-  VolumeFast<VT> vol{static_cast<const VT*>(p.volume.p), int(p.volume.s[1]), int(p.volume.s[2]),
-                     int(p.volume.s[3]), p.X - 1, p.Y - 1, p.Z - 1};
-  TfShared<C> tf{s_tf, p.R};
-  float* ck = nullptr;
-  const int K = p.ckpt_interval;
-  // density record: this lane's ray stores its samples from group dgrp on
-  float4* const dens4 = reinterpret_cast<float4*>(p.dens);
-  unsigned long long* const bump = reinterpret_cast<unsigned long long*>(counter + 2);
-  int dgrp = -1;
-  float4 dstage = make_float4(0.f, 0.f, 0.f, 0.f);
-  const int lane = threadIdx.x & 31;
-  auto dens_off_at = [&]() -> int* {
-    return static_cast<int*>(p.dens_off.p) + b * p.dens_off.s[0] + y * p.dens_off.s[1] + x * p.dens_off.s[2];
-  };
-
-  auto write_out = [&](float4 c, int term) {
-    float* col = static_cast<float*>(p.color.p) + b * p.color.s[0] + y * p.color.s[1] + x * p.color.s[2];
-    col[0] = c.x;
-    col[p.color.s[3]] = c.y;
-    col[2 * p.color.s[3]] = c.z;
-    col[3 * p.color.s[3]] = c.w;
-    static_cast<int*>(p.term.p)[b * p.term.s[0] + y * p.term.s[1] + x * p.term.s[2]] = term;
-  };
-
-  while (true) {
-    // refill idle lanes; rays that miss the box are finished right here
-    while (true) {
-      int id = fetch_rays(counter, total, !active, exhausted);
-      if (id >= 0 && ray_list) id = ray_list[id];
-      int claim = 0;  // groups of 4 densities the new ray records
-      if (id >= 0 && order.pixel(id, b, x, y)) {
-        fast_setup(p, x, y, b, r);
-        kmax = max_samples(r.tmin, r.tmax, r.step);
-        if (kmax == 0 || r.tmin > r.tmax || 0.f > p.early_out) {
-          write_out(make_float4(0.f, 0.f, 0.f, 0.f), 0);
-          if (dens4) *dens_off_at() = -1;
-        } else {
-          claim = dens4 ? (kmax + 3) >> 2 : 0;
-          active = true;
-          acc = mk4(0, 0, 0, 0);
-          k = 0;
-          smp.cx = -1;
-          vol.p = static_cast<const VT*>(p.volume.p) + b * p.volume.s[0];
-          tf.p = s_tf + (copies > 1 ? b : 0) * p.R * C;
-          ck = p.ckpt.p ? static_cast<float*>(p.ckpt.p) + b * p.ckpt.s[0] + y * p.ckpt.s[1] + x * p.ckpt.s[2]
-                        : nullptr;
-          next_ck = K;
-          slot = 0;
-        }
-      }
-      if (dens4) {
-        // room in the pool for the warp's new rays: one 64-bit atomic per warp
-        int incl = claim;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const int v = __shfl_up_sync(kFullMask, incl, o);
-          if (lane >= o) incl += v;
-        }
-        const int tot = __shfl_sync(kFullMask, incl, 31);
-        if (tot > 0) {
-          unsigned long long base = 0;
-          if (lane == 31) base = atomicAdd(bump, static_cast<unsigned long long>(tot));
-          base = __shfl_sync(kFullMask, base, 31);
-          if (claim > 0) {
-            const unsigned long long first = base + static_cast<unsigned long long>(incl - claim);
-            dgrp = first + claim <= static_cast<unsigned long long>(p.dens_units) ? int(first) : -1;
-            *dens_off_at() = dgrp;
-          }
-        }
-      }
-      if (exhausted || __ballot_sync(kFullMask, !active) == 0u) break;
-    }
-    if (__ballot_sync(kFullMask, active) == 0u) break;
-
-#pragma unroll 1
-    for (int s = 0; s < kFwdChunk; ++s) {
-      if (active) {
-        const float t = r.tmin + k * r.step;
-        if (t > r.tmax || acc.w > p.early_out || k >= kmax) {
-          write_out(make_float4(acc.x, acc.y, acc.z, acc.w), k);
-          if (dgrp >= 0 && (k & 3) != 0) __stcs(dens4 + dgrp + (k >> 2), dstage);
-          dgrp = -1;
-          active = false;
-        } else {
-          if (ck && k == next_ck) {  // opacity before sample k = (slot+1)*K
-            if (slot < p.ckpt_slots) ck[slot * p.ckpt.s[3]] = acc.w;
-            ++slot;
-            next_ck += K;
-          }
-          const float density = smp.sample(vol, fast_pos(r, t));
-          acc = blend<BLEND>(acc, tf_eval<TF>(tf, density), r.step);
-          if (dgrp >= 0) {
-            switch (k & 3) {
-              case 0: dstage.x = density; break;
-              case 1: dstage.y = density; break;
-              case 2: dstage.z = density; break;
-              default: dstage.w = density; __stcs(dens4 + dgrp + (k >> 2), dstage);
-            }
-          }
-          ++k;
-        }
-      }
-    }
-    __syncwarp();
-  }
-}
 
 // ----------------------------------------------------------------- adjoint
 template <int FILTER, int TF, int BLEND, bool VOLGRAD, bool TFGRAD, typename VT>

@@ -1,0 +1,153 @@
+// Forward march with one warp per ray.
+//
+// The 32 lanes of a warp take 32 consecutive samples of the same ray at once:
+// each lane gathers its sample's density and evaluates the TF, then the warp
+// composites the 32 samples front to back.  Compositing is associative (the
+// "over" operator: opacity a then b gives a + (1 - a) b, colour likewise), so
+// a 5-step warp scan gives every sample's incoming opacity, from which follow
+// the early-termination point (the first sample whose incoming opacity
+// exceeds blendingEarlyOut, renderer/renderer_kernels.cuh:55-58), each
+// sample's colour contribution (1 - incoming opacity) a c (summed per lane,
+// then over the warp at the end of the ray) and the transmittance checkpoints.  The per-sample arithmetic is the
+// reference's (renderer/renderer_blending.cuh:30-49); only the order of the
+// compositing sums differs, by rounding.
+//
+// All 32 gathers of a step are independent and issued together, lanes never
+// diverge on cell or termination events, and a lane keeps no per-ray state,
+// so registers are few and many warps fit per SM.  Warps fetch one ray at a
+// time from the longest-first order of the rays with samples.
+#pragma once
+#include "dvr_persist.cuh"
+
+namespace dvr {
+
+template <int FILTER, typename VT>
+__device__ __forceinline__ float sample_density(const VolumeFast<VT>& v, float3 q) {
+  if constexpr (FILTER == kNearest) {
+    return v.at(nearest_coord(q.x, v.X1 + 1), nearest_coord(q.y, v.Y1 + 1), nearest_coord(q.z, v.Z1 + 1));
+  } else {
+    const int ix = int(q.x), iy = int(q.y), iz = int(q.z);
+    float d[8];
+    v.corners(ix, iy, iz, d);
+    return trilerp(d, q.x - float(ix), q.y - float(iy), q.z - float(iz));
+  }
+}
+
+// opacity a, then b: a + (1 - a) b
+__device__ __forceinline__ float over(float a, float b) { return a + (1.f - a) * b; }
+
+// ray_list[0 .. *ray_count): the rays with samples (longest first); the
+// ordering pass has already finished the others.
+template <int FILTER, int TF, int BLEND, typename VT>
+__global__ void __launch_bounds__(kFastThreads) fast_forward_warp_kernel(const RenderParams p, const RayOrder order,
+                                                                         int* counter, const int* ray_list,
+                                                                         const int* ray_count) {
+  extern __shared__ float4 fast_smem4[];
+  constexpr int C = TfChannels<TF>::C;
+  float* s_tf = reinterpret_cast<float*>(fast_smem4);
+  const int copies = tf_copies(p);
+  for (int bb = 0; bb < copies; ++bb) stage_tf(p, bb, s_tf + bb * p.R * C);
+  __syncthreads();
+
+  const int lane = threadIdx.x & 31;
+  const int total = *ray_count;
+  const int K = p.ckpt_interval;
+  const int kshift = (K & (K - 1)) == 0 ? __ffs(K) - 1 : -1;  // log2 K for a power-of-two interval
+  unsigned long long* const bump = reinterpret_cast<unsigned long long*>(counter + 2);
+
+  while (true) {
+    int pos = 0;
+    if (lane == 0) pos = atomicAdd(counter, 1);
+    pos = __shfl_sync(kFullMask, pos, 0);
+    if (pos >= total) break;
+    int b, x, y;
+    if (!order.pixel(ray_list[pos], b, x, y)) continue;
+    FastRay q;
+    fast_setup(p, x, y, b, q);
+    const int kmax = max_samples(q.tmin, q.tmax, q.step);
+
+    float* rec = nullptr;
+    if (p.dens) {
+      // room for 4 * ceil(kmax / 4) densities in the pool
+      const unsigned long long claim = static_cast<unsigned long long>((kmax + 3) >> 2);
+      unsigned long long g = 0;
+      if (lane == 0) g = atomicAdd(bump, claim);
+      g = __shfl_sync(kFullMask, g, 0);
+      const bool fits = g + claim <= static_cast<unsigned long long>(p.dens_units);
+      if (lane == 0)
+        static_cast<int*>(p.dens_off.p)[b * p.dens_off.s[0] + y * p.dens_off.s[1] + x * p.dens_off.s[2]] =
+            fits ? int(g) : -1;
+      if (fits) rec = p.dens + 4 * g;
+    }
+    const VolumeFast<VT> vol{static_cast<const VT*>(p.volume.p) + b * p.volume.s[0], int(p.volume.s[1]),
+                             int(p.volume.s[2]), int(p.volume.s[3]), p.X - 1, p.Y - 1, p.Z - 1};
+    const TfShared<C> tf{s_tf + (copies > 1 ? b : 0) * p.R * C, p.R};
+    float* ck = p.ckpt.p ? static_cast<float*>(p.ckpt.p) + b * p.ckpt.s[0] + y * p.ckpt.s[1] + x * p.ckpt.s[2]
+                         : nullptr;
+
+    float alpha = 0.f;  // accumulated opacity before the chunk
+    float cr = 0.f, cg = 0.f, cb = 0.f;  // this lane's samples' colour contributions
+    int n = 0;
+    for (int k0 = 0;; k0 += 32) {
+      const int k = k0 + lane;
+      const float t = q.tmin + k * q.step;
+      const bool in_ray = k < kmax && !(t > q.tmax);
+      float density = 0.f, a = 0.f;
+      f4 c = mk4(0, 0, 0, 0);
+      if (in_ray) {
+        density = sample_density<FILTER, VT>(vol, fast_pos(q, t));
+        c = tf_eval<TF>(tf, density);
+        a = blend_alpha<BLEND>(c.w, q.step);
+      }
+      // incoming opacity of each sample: exclusive "over" scan
+      float incl = a;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const float v = __shfl_up_sync(kFullMask, incl, o);
+        if (lane >= o) incl = over(v, incl);
+      }
+      float excl = __shfl_up_sync(kFullMask, incl, 1);
+      if (lane == 0) excl = 0.f;
+      const float a_in = over(alpha, excl);
+      const bool go = in_ray && !(a_in > p.early_out);
+      const unsigned gm = __ballot_sync(kFullMask, go);
+      const int f = gm == kFullMask ? 32 : __ffs(~gm) - 1;  // first sample not taken
+      const bool used = lane < f;
+      if (used) {
+        if (rec) rec[k] = density;
+        if (ck && k > 0) {
+          // opacity before sample (slot + 1) * K
+          const bool at = kshift >= 0 ? (k & (K - 1)) == 0 : k % K == 0;
+          const int slot = (kshift >= 0 ? k >> kshift : k / K) - 1;
+          if (at && slot < p.ckpt_slots) ck[slot * p.ckpt.s[3]] = a_in;
+        }
+        const float w = (1.f - a_in) * a;
+        cr = fmaf(w, c.x, cr);
+        cg = fmaf(w, c.y, cg);
+        cb = fmaf(w, c.z, cb);
+      }
+      if (f < 32) {
+        alpha = __shfl_sync(kFullMask, a_in, f);
+        n = k0 + f;
+        break;
+      }
+      alpha = over(alpha, __shfl_sync(kFullMask, incl, 31));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      cr += __shfl_xor_sync(kFullMask, cr, o);
+      cg += __shfl_xor_sync(kFullMask, cg, o);
+      cb += __shfl_xor_sync(kFullMask, cb, o);
+    }
+    if (lane == 0) {
+      float* col = static_cast<float*>(p.color.p) + b * p.color.s[0] + y * p.color.s[1] + x * p.color.s[2];
+      col[0] = cr;
+      col[p.color.s[3]] = cg;
+      col[2 * p.color.s[3]] = cb;
+      col[3 * p.color.s[3]] = alpha;
+      static_cast<int*>(p.term.p)[b * p.term.s[0] + y * p.term.s[1] + x * p.term.s[2]] = n;
+    }
+  }
+}
+
+}  // namespace dvr
