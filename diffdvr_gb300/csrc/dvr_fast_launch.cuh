@@ -141,7 +141,7 @@ static cudaError_t fast_adjoint_record_go(const RenderParams& p, const AdjointPa
   if (e != cudaSuccess) return e;
   e = set_smem(gen, gsmem);
   if (e != cudaSuccess) return e;
-  const int rgrid = persistent_grid(rec, rsmem, total, li);
+  const int rgrid = persistent_grid(rec, rsmem, total * 32, li);  // one warp per ray
   const int ggrid = li.num_sms;
   // scratch: order ints, leftover list, the general kernel's TF-gradient slices
   const size_t order_bytes = (work_order_ints(p) * sizeof(int) + 255) & ~size_t(255);
@@ -155,7 +155,8 @@ static cudaError_t fast_adjoint_record_go(const RenderParams& p, const AdjointPa
   int* leftover = reinterpret_cast<int*>(scratch + order_bytes);
   e = order_rays_by_work(p, &a, order_ints, li, s);
   if (e != cudaSuccess) return e;
-  rec<<<rgrid, kFastThreads, rsmem, s>>>(p, a, order, counter, order_ints + work_order_list_offset, leftover,
+  rec<<<rgrid, kFastThreads, rsmem, s>>>(p, a, order, counter, order_ints + work_order_list_offset,
+                                         order_ints + work_order_count_offset, leftover,
                                          reinterpret_cast<float*>(scratch + order_bytes + left_bytes + tf_bytes));
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
@@ -204,8 +205,7 @@ static cudaError_t fast_adjoint_go(const RenderParams& p, const AdjointParams& a
     if (tfgrad && !volgrad && !a.has_camera && !a.has_stepsize && p.dens && p.ckpt.p) {
       const bool per_batch = a.adj_tf.s[0] != 0;
       (void)per_batch;
-      const size_t rsmem = size_t(RecordSmem(p.R, C, kFastThreads, p.ckpt_interval, copies, false).total) *
-                           sizeof(float);
+      const size_t rsmem = size_t(record_smem_floats(p.R, C, copies)) * sizeof(float);
       if (rsmem <= size_t(li.max_smem_optin))
         return fast_adjoint_record_go<FILTER, BLEND, VT>(p, a, order, counter, rsmem, smem, li, s);
     }

@@ -118,7 +118,7 @@ __global__ void __launch_bounds__(kFastThreads) fast_adjoint_persistent_kernel(c
   TfShared<C> tf{s_tf, p.R};
   float* adjv = nullptr;
   const float* ck = nullptr;
-  const float4* drow = nullptr;  // the ray's recorded densities, if any
+  const float2* drow = nullptr;  // the ray's recorded (density, incoming opacity) pairs, if any
 
   auto write_ray_grads = [&]() {
     if (a.has_stepsize) {
@@ -178,7 +178,8 @@ __global__ void __launch_bounds__(kFastThreads) fast_adjoint_persistent_kernel(c
             if (p.dens) {
               const int g = static_cast<const int*>(p.dens_off.p)[b * p.dens_off.s[0] + y * p.dens_off.s[1] +
                                                                   x * p.dens_off.s[2]];
-              if (g >= 0) drow = reinterpret_cast<const float4*>(p.dens) + g;
+              if (g >= 0 && int64_t(g) + ((n + 1) >> 1) <= p.dens_units)
+                drow = reinterpret_cast<const float2*>(p.dens + 4 * size_t(g));
             }
           } else {
             // no checkpoints: invert the blend from the final colour, K samples per round
@@ -205,24 +206,22 @@ __global__ void __launch_bounds__(kFastThreads) fast_adjoint_persistent_kernel(c
     const int k0 = ckpt_ray ? j * K : 0;
     const int k1 = ckpt_ray ? min(n, k0 + K) : 0;
     if (seg_len > 0) {
-      float alpha = (active && ckpt_ray && j > 0) ? ck[(j - 1) * p.ckpt.s[3]] : 0.f;
-      float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+      float alpha = (active && ckpt_ray && j > 0 && !drow) ? ck[(j - 1) * p.ckpt.s[3]] : 0.f;
       for (int kk = 0; kk < K; ++kk) {
         const int k = k0 + kk;
         if (active && ckpt_ray && k < k1) {
-          float density;
-          if (drow) {
-            if (kk == 0 || (k & 3) == 0) q = __ldcs(drow + (k >> 2));
-            const int c = k & 3;
-            density = c == 0 ? q.x : c == 1 ? q.y : c == 2 ? q.z : q.w;
+          if (drow) {  // recorded density and incoming opacity
+            const float2 v = __ldcs(drow + k);
+            seg_d[kk * blockDim.x] = v.x;
+            seg_a[kk * blockDim.x] = v.y;
           } else {
             const float t = r.tmin + k * r.step;
-            density = smp.sample(vol, fast_pos(r, t));
+            const float density = smp.sample(vol, fast_pos(r, t));
+            const float a_k = blend_alpha<BLEND>(tf_eval<TF>(tf, density).w, r.step);
+            seg_d[kk * blockDim.x] = density;
+            seg_a[kk * blockDim.x] = alpha;
+            alpha = alpha + (1 - alpha) * a_k;
           }
-          const float a_k = blend_alpha<BLEND>(tf_eval<TF>(tf, density).w, r.step);
-          seg_d[kk * blockDim.x] = density;
-          seg_a[kk * blockDim.x] = alpha;
-          alpha = alpha + (1 - alpha) * a_k;
         }
       }
       __syncwarp();

@@ -68,8 +68,8 @@ __global__ void __launch_bounds__(kFastThreads) fast_forward_warp_kernel(const R
 
     float* rec = nullptr;
     if (p.dens) {
-      // room for 4 * ceil(kmax / 4) densities in the pool
-      const unsigned long long claim = static_cast<unsigned long long>((kmax + 3) >> 2);
+      // room for kmax (density, incoming opacity) pairs, in groups of 4 floats
+      const unsigned long long claim = static_cast<unsigned long long>((kmax + 1) >> 1);
       unsigned long long g = 0;
       if (lane == 0) g = atomicAdd(bump, claim);
       g = __shfl_sync(kFullMask, g, 0);
@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(kFastThreads) fast_forward_warp_kernel(const R
       const int f = gm == kFullMask ? 32 : __ffs(~gm) - 1;  // first sample not taken
       const bool used = lane < f;
       if (used) {
-        if (rec) rec[k] = density;
+        if (rec) __stcs(reinterpret_cast<float2*>(rec) + k, make_float2(density, a_in));
         if (ck && k > 0) {
           // opacity before sample (slot + 1) * K
           const bool at = kshift >= 0 ? (k & (K - 1)) == 0 : k % K == 0;

@@ -153,10 +153,11 @@ class RendererOutputs:
     ``Renderer.checkpoint_slots``.
 
     ``sample_density`` (optional, 1-D float32 pool, with ``sample_offset``, a
-    B*H*W int32 tensor, and checkpoints) receives the density of every sample
-    of each ray; the adjoint then rebuilds its segments from these instead of
-    re-sampling the volume.  Rays that find the pool full are re-sampled;
-    ``Renderer.sample_density_size`` gives a size that holds every ray."""
+    B*H*W int32 tensor, and checkpoints) receives, for every sample of each
+    ray, its density and the opacity accumulated in front of it; the adjoint
+    then reads these instead of re-sampling the volume.  Rays that find the
+    pool full are re-sampled; ``Renderer.sample_density_size`` gives a size
+    that holds every ray."""
 
     def __init__(self, color: Optional[torch.Tensor] = None, terminationIndex: Optional[torch.Tensor] = None,
                  checkpoints: Optional[torch.Tensor] = None, checkpoint_interval: int = 16,
@@ -365,11 +366,11 @@ class Renderer:
     @staticmethod
     def sample_density_size(inputs: RendererInputs, batch: int) -> int:
         """Floats of a RendererOutputs.sample_density pool that holds every
-        ray of a batch-``batch`` image: B*H*W rays of at most 4*ceil(n/4)
-        samples each, n the sample bound from the box diagonal and the
-        smallest step size."""
+        ray of a batch-``batch`` image: B*H*W rays of 2 floats per sample,
+        4*ceil(n/2) floats each, n the sample bound from the box diagonal and
+        the smallest step size."""
         W, H = int(inputs.screen_size.x), int(inputs.screen_size.y)
-        return int(batch) * H * W * 4 * Renderer.checkpoint_slots(inputs, 4)
+        return int(batch) * H * W * 4 * Renderer.checkpoint_slots(inputs, 2)
 
 
 # --------------------------------------------------------------------- module functions

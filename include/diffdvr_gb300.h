@@ -125,13 +125,14 @@ typedef struct DvrRendererInputs {
  *    `checkpoint_interval` samples.  C >= ceil(max samples per ray / interval) - 1.
  *  - sample_density + sample_offset (both or neither; need checkpoints): a
  *    1-D float32 pool of any size N (16-byte aligned, contiguous, N >= 4) and
- *    a B*H*W int32 tensor.  The forward stores the density of every sample of
- *    a ray in the pool (rays claim room in launch order, a multiple of 4
- *    floats each) and writes the ray's first float index / 4 to
- *    sample_offset, or -1 when the pool was full.  The adjoint then rebuilds
- *    each checkpoint segment from the stored densities instead of re-sampling
- *    the volume; rays with offset -1 re-sample.  N = B*H*W*S with
- *    S = 4 * dvr_checkpoint_slots(length, step, 4) holds every ray.
+ *    a B*H*W int32 tensor.  The forward stores, for every sample k of a ray,
+ *    the density and the opacity accumulated in front of the sample as floats
+ *    2k and 2k+1 of the ray's run in the pool (rays claim room in launch
+ *    order, a multiple of 4 floats each) and writes the run's first float
+ *    index / 4 to sample_offset, or -1 when the pool was full.  The adjoint
+ *    then reads these instead of re-sampling the volume and re-marching from
+ *    checkpoints; rays with offset -1 re-sample.  N = B*H*W*S with
+ *    S = 4 * dvr_checkpoint_slots(length, step, 2) holds every ray.
  *    Written and read by the optimized single-instance entry points only. */
 typedef struct DvrRendererOutputs {
   DvrTensor color;

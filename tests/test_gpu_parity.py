@@ -435,19 +435,21 @@ def test_invalid_inputs_raise(cuda_device):
 
 @pytest.mark.parametrize("fraction", ["full", 0.5])
 def test_sample_density_record(fraction, cuda_device):
-    """The forward's density record: every ray with samples that got room
-    holds n finite densities inside the volume's range in its own disjoint
-    4-aligned run of the pool; rays without samples or without room are -1;
-    the adjoint from the record equals the re-sampling adjoint (same kernels,
-    the densities are the re-march's own values, so only the order of float
-    atomics differs: relative L2 <= 1e-5)."""
+    """The forward's sample record: every ray with samples that got room holds
+    n (density, incoming opacity) pairs in its own disjoint 4-aligned run of
+    the pool: densities finite and inside the volume's range, opacities
+    starting at 0, non-decreasing, below 1 and equal to the checkpoints at
+    multiples of the interval; rays without samples or without room are -1;
+    the adjoint from the record equals the re-sampling adjoint (relative L2
+    <= 1e-5: the recorded opacities are the forward's, the re-march's agree
+    to rounding)."""
     case = make_case(71, tf_mode=1, filter_mode=1, blend_mode=0, shape=(20, 24, 28), W=40, H=36, B=2, R=32,
                      opacity=0.3, pad_faces=True)
     inp, out = gpu_forward(case, checkpoints=True, record="full")
     if fraction != "full":
         # a pool for about half of the samples the rays actually recorded
         t = out.terminationIndex.cpu().numpy()
-        inp, out = gpu_forward(case, checkpoints=True, record=int(fraction * 4 * ((t + 3) // 4).sum()))
+        inp, out = gpu_forward(case, checkpoints=True, record=int(fraction * 4 * ((t + 1) // 2).sum()))
     term = out.terminationIndex.cpu().numpy()
     off = out.sample_offset.cpu().numpy()
     pool = out.sample_density.cpu().numpy()
@@ -459,12 +461,18 @@ def test_sample_density_record(fraction, cuda_device):
     else:
         assert ((term > 0) & (off == -1)).any() and hit.any()
     lo, hi = float(case.volume.min()), float(case.volume.max())
+    ck = out.checkpoints.cpu().numpy()
+    K = out.checkpoint_interval
     starts, ends = [], []
-    for o, n in zip(off[hit], term[hit]):
-        d = pool[4 * o: 4 * o + n]
-        assert len(d) == n and np.isfinite(d).all() and d.min() >= lo - 1e-6 and d.max() <= hi + 1e-6
+    for (bi, yi, xi), o, n in zip(np.argwhere(hit), off[hit], term[hit]):
+        run = pool[4 * o: 4 * o + 2 * n].reshape(n, 2)
+        d, a_in = run[:, 0], run[:, 1]
+        assert np.isfinite(run).all() and d.min() >= lo - 1e-6 and d.max() <= hi + 1e-6
+        assert a_in[0] == 0 and (np.diff(a_in) >= 0).all() and a_in.max() < 1
+        js = np.arange(1, (n - 1) // K + 1)
+        np.testing.assert_allclose(a_in[js * K], ck[bi, yi, xi, js - 1], rtol=0, atol=1e-6)
         starts.append(4 * o)
-        ends.append(4 * o + n)
+        ends.append(4 * o + 2 * n)
     order = np.argsort(starts)
     assert (np.asarray(starts)[order][1:] >= np.asarray(ends)[order][:-1]).all()
     assert max(ends) <= pool.size
@@ -478,23 +486,26 @@ def test_sample_density_record(fraction, cuda_device):
         assert rel_l2(got[k], ref[k]) <= 1e-5, (k, rel_l2(got[k], ref[k]))
 
 
-@pytest.mark.parametrize("blend,per_batch,pool", [(0, False, "full"), (1, False, "full"), (0, True, "full"),
-                                                  (1, False, 0.5)])
-def test_tf_only_adjoint_from_record(blend, per_batch, pool, oracle_built, cuda_device):
+@pytest.mark.parametrize("blend,per_batch,pool,interval", [(0, False, "full", 16), (1, False, "full", 16),
+                                                           (0, True, "full", 16), (1, False, 0.5, 16),
+                                                           (0, False, "full", 5), (1, True, "full", 64)])
+def test_tf_only_adjoint_from_record(blend, per_batch, pool, interval, oracle_built, cuda_device):
     """TF gradient alone with checkpoints and a sample-density record (the
     texture-TF record kernel; rays without room in the pool go through the
     general kernel) against the FP64 oracle, tolerances as above; per_batch:
-    a TF per batch entry and a TF gradient per batch entry."""
+    a TF per batch entry and a TF gradient per batch entry; intervals that do
+    not divide 32 make the kernel advance from a checkpoint to a step start."""
     O = oracle_built
     rng = np.random.default_rng(11 + blend)
     case = make_case(90 + blend, tf_mode=1, filter_mode=1, blend_mode=blend, shape=(20, 24, 28), W=40, H=36, B=2,
                      R=32, opacity=0.3, pad_faces=True)
     if not per_batch:
         case.tf = np.ascontiguousarray(case.tf[:1])  # one TF for both views, one TF gradient
-    inp, out = gpu_forward(case, checkpoints=True, record="full")
+    inp, out = gpu_forward(case, checkpoints=True, interval=interval, record="full")
     if pool != "full":
         t = out.terminationIndex.cpu().numpy()
-        inp, out = gpu_forward(case, checkpoints=True, record=int(pool * 4 * ((t + 3) // 4).sum()))
+        inp, out = gpu_forward(case, checkpoints=True, interval=interval,
+                               record=int(pool * 4 * ((t + 1) // 2).sum()))
         t = out.terminationIndex.cpu().numpy()
         assert (out.sample_offset.cpu().numpy()[t > 0] == -1).any()
     term = out.terminationIndex.cpu().numpy()
