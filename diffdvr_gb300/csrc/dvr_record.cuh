@@ -3,13 +3,11 @@
 //
 // The forward records, per sample, the density and the opacity accumulated in
 // front of the sample.  With those, the adjoint of a ray needs no volume
-// access, no ray geometry and no checkpoints: each lane walks its ray back to
-// front through the record and runs the reverse recursion
+// access, no ray geometry and no checkpoints: the reverse recursion
 // (renderer/renderer_kernels.cuh:367-444 with the blend adjoint of
 // renderer/renderer_blending.cuh:63-98, the accumulator before each sample
-// read from the record instead of recovered by inverting the blend).  The
-// state of a lane is a few registers, so many warps fit per SM, and lanes
-// whose ray is done take the next ray from the longest-first order.
+// read from the record instead of recovered by inverting the blend) runs over
+// the record, split over the 32 lanes of a warp (see the kernel).
 //  * TF gradient: the two texels (i, i+1) of the current sample in registers;
 //    a texel leaving them is added with fire-and-forget global reductions to
 //    the warp's slice of an L2-resident scratch (or to the per-batch output);
@@ -22,6 +20,12 @@
 #include "dvr_warpray.cuh"
 
 namespace dvr {
+
+// composition of affine maps x -> A x + B: (A, B) becomes f o g with g = (Ag, Bg)
+__device__ __forceinline__ void compose(float& A, float& B, float Ag, float Bg) {
+  B = fmaf(A, Bg, B);
+  A = A * Ag;
+}
 
 // Shared memory of the record adjoint (floats): the TF copies.
 __host__ __device__ inline int record_smem_floats(int R, int C, int tf_copies) { return (tf_copies * R * C + 3) & ~3; }
@@ -92,9 +96,26 @@ __device__ __forceinline__ void record_reverse_step(const TfShared<4>& tf, float
   acc_tf.add(i0, i1, adj_cur, 1 - df, df);
 }
 
+// Affine map x -> A x + B of the opacity adjoint across one sample:
+// adj_in = (1 - a) adj_out - a (c . adj_rgb)   (renderer/renderer_blending.cuh:75-93)
+template <int BLEND>
+__device__ __forceinline__ void record_sample_map(const TfShared<4>& tf, float step, float d, f4 adj_rgb, float& A,
+                                                  float& B) {
+  const f4 cur = tf_eval<kTfTexture>(tf, d);
+  const float a_k = blend_alpha<BLEND>(cur.w, step);
+  A = 1.f - a_k;
+  B = -a_k * (cur.x * adj_rgb.x + cur.y * adj_rgb.y + cur.z * adj_rgb.z);
+}
+
 // ray_list[0 .. *ray_count): the rays with samples; leftover[0 .. counter[1]):
 // the rays left to the general kernel.  tf_slices: (blocks x warps) slices of
 // R*C floats, one per warp (TF gradient of a broadcast TF), zeroed here.
+//
+// One warp per ray: lane j takes the j-th of 32 consecutive segments of
+// L = ceil(n / 32) samples.  Each lane composes the affine maps of its
+// segment, a warp suffix scan gives the opacity adjoint at the end of every
+// segment, and each lane then walks its segment back to front with the full
+// reverse step.  The serial depth of a ray is 2 L samples instead of n.
 template <int BLEND>
 __global__ void __launch_bounds__(kFastThreads) fast_adjoint_record_kernel(const RenderParams p, const AdjointParams a,
                                                                             const RayOrder order, int* counter,
@@ -113,79 +134,92 @@ __global__ void __launch_bounds__(kFastThreads) fast_adjoint_record_kernel(const
     for (int e = threadIdx.x; e < warps * n_tf; e += blockDim.x) block_slices[e] = 0.f;
   __syncthreads();
 
+  const int lane = threadIdx.x & 31;
   const int total = *ray_count;
   TexelPairAtomic acc_tf;
   acc_tf.R = p.R;
   if (!per_batch) acc_tf.dst = block_slices + (threadIdx.x >> 5) * n_tf;
   int cur_b = -1;
 
-  // The record of a ray is read as groups of 4 floats (samples 2m and 2m+1);
-  // a round walks back over two groups, the next round's two are loaded
-  // during it.
-  bool exhausted = false, active = false;
-  int n = 0, m = 0;  // samples of the ray; the round's upper group
-  float step = 0.f;
-  f4 adj_acc = mk4(0, 0, 0, 0);
-  const float4* rec = nullptr;
-  float4 g0 = make_float4(0.f, 0.f, 0.f, 0.f), g1 = g0;  // groups m and m - 1
-  TfShared<C> tf{s_tf, p.R};
-
   while (true) {
-    while (true) {
-      int id = fetch_rays(counter, total, !active, exhausted);
-      if (id >= 0) id = ray_list[id];
-      int b, x, y;
-      if (id >= 0 && order.pixel(id, b, x, y)) {
-        n = static_cast<const int*>(a.fwd_term.p)[b * a.fwd_term.s[0] + y * a.fwd_term.s[1] + x * a.fwd_term.s[2]];
-        if (n > 0) {
-          const int g = static_cast<const int*>(p.dens_off.p)[b * p.dens_off.s[0] + y * p.dens_off.s[1] +
-                                                              x * p.dens_off.s[2]];
-          // the ray's ceil(n / 2) groups must lie inside the pool
-          if (g < 0 || int64_t(g) + ((n + 1) >> 1) > p.dens_units) {
-            leftover[atomicAdd(counter + 1, 1)] = id;
-          } else {
-            active = true;
-            step = step_at(p.step, b, y, x);
-            const float* ac = static_cast<const float*>(a.adj_color.p) + b * a.adj_color.s[0] +
-                              y * a.adj_color.s[1] + x * a.adj_color.s[2];
-            adj_acc = mk4(ac[0], ac[a.adj_color.s[3]], ac[2 * a.adj_color.s[3]], ac[3 * a.adj_color.s[3]]);
-            rec = reinterpret_cast<const float4*>(p.dens) + g;
-            m = (n - 1) >> 1;
-            g0 = __ldcs(rec + m);
-            g1 = m >= 1 ? __ldcs(rec + m - 1) : make_float4(0.f, 0.f, 0.f, 0.f);
-            tf.p = s_tf + (copies > 1 ? b : 0) * n_tf;
-            if (per_batch && b != cur_b) {
-              acc_tf.flush();
-              cur_b = b;
-              acc_tf.dst = static_cast<float*>(a.adj_tf.p) + b * a.adj_tf.s[0];
-              acc_tf.sr = a.adj_tf.s[1];
-              acc_tf.sc = a.adj_tf.s[2];
-            }
-          }
-        }
-      }
-      if (exhausted || __ballot_sync(kFullMask, !active) == 0u) break;
+    int pos = 0;
+    if (lane == 0) pos = atomicAdd(counter, 1);
+    pos = __shfl_sync(kFullMask, pos, 0);
+    if (pos >= total) break;
+    const int id = ray_list[pos];
+    int b, x, y;
+    if (!order.pixel(id, b, x, y)) continue;
+    const int n = static_cast<const int*>(a.fwd_term.p)[b * a.fwd_term.s[0] + y * a.fwd_term.s[1] +
+                                                         x * a.fwd_term.s[2]];
+    if (n <= 0) continue;
+    const int g = static_cast<const int*>(p.dens_off.p)[b * p.dens_off.s[0] + y * p.dens_off.s[1] +
+                                                        x * p.dens_off.s[2]];
+    // the ray's ceil(n / 2) groups of 4 floats must lie inside the pool
+    if (g < 0 || int64_t(g) + ((n + 1) >> 1) > p.dens_units) {
+      if (lane == 0) leftover[atomicAdd(counter + 1, 1)] = id;
+      continue;
     }
-    if (__ballot_sync(kFullMask, active) == 0u) break;
+    const float step = step_at(p.step, b, y, x);
+    const float* ac = static_cast<const float*>(a.adj_color.p) + b * a.adj_color.s[0] + y * a.adj_color.s[1] +
+                      x * a.adj_color.s[2];
+    const f4 adj_col = mk4(ac[0], ac[a.adj_color.s[3]], ac[2 * a.adj_color.s[3]], ac[3 * a.adj_color.s[3]]);
+    const float2* rec = reinterpret_cast<const float2*>(p.dens + 4 * size_t(g));
+    const TfShared<C> tf{s_tf + (copies > 1 ? b : 0) * n_tf, p.R};
+    if (per_batch && b != cur_b) {
+      acc_tf.flush();
+      cur_b = b;
+      acc_tf.dst = static_cast<float*>(a.adj_tf.p) + b * a.adj_tf.s[0];
+      acc_tf.sr = a.adj_tf.s[1];
+      acc_tf.sc = a.adj_tf.s[2];
+    }
 
-#pragma unroll 1
-    for (int round = 0; round < 2; ++round) {
-      if (active) {
-        const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-        const float4 h0 = m >= 2 ? __ldcs(rec + m - 2) : z;  // next round's groups
-        const float4 h1 = m >= 3 ? __ldcs(rec + m - 3) : z;
-        if (2 * m + 1 < n) record_reverse_step<BLEND>(tf, step, g0.z, g0.w, adj_acc, acc_tf);
-        record_reverse_step<BLEND>(tf, step, g0.x, g0.y, adj_acc, acc_tf);
-        if (m >= 1) {
-          record_reverse_step<BLEND>(tf, step, g1.z, g1.w, adj_acc, acc_tf);
-          record_reverse_step<BLEND>(tf, step, g1.x, g1.y, adj_acc, acc_tf);
-        }
-        m -= 2;
-        g0 = h0;
-        g1 = h1;
-        if (m < 0) active = false;
+    // this lane's segment [s0, s1)
+    const int L = (n + 31) >> 5;
+    const int s0 = min(n, lane * L), s1 = min(n, s0 + L);
+
+    // 1. affine map of the segment: G = f_s0 o f_s0+1 o ... o f_s1-1
+    float A = 1.f, B = 0.f;
+    {
+      int k = s0;
+      for (; k + 1 < s1; k += 2) {
+        const float2 v0 = __ldcs(rec + k), v1 = __ldcs(rec + k + 1);
+        float A0, B0, A1, B1;
+        record_sample_map<BLEND>(tf, step, v0.x, adj_col, A0, B0);
+        record_sample_map<BLEND>(tf, step, v1.x, adj_col, A1, B1);
+        compose(A0, B0, A1, B1);
+        compose(A, B, A0, B0);
       }
-      __syncwarp();
+      if (k < s1) {
+        float A0, B0;
+        record_sample_map<BLEND>(tf, step, __ldcs(rec + k).x, adj_col, A0, B0);
+        compose(A, B, A0, B0);
+      }
+    }
+    // 2. opacity adjoint behind each segment: suffix composition over the lanes
+    float SA = A, SB = B;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const float Ao = __shfl_down_sync(kFullMask, SA, o), Bo = __shfl_down_sync(kFullMask, SB, o);
+      if (lane + o < 32) compose(SA, SB, Ao, Bo);
+    }
+    const float NA = __shfl_down_sync(kFullMask, SA, 1), NB = __shfl_down_sync(kFullMask, SB, 1);
+    f4 adj_acc = adj_col;
+    if (lane < 31) adj_acc.w = fmaf(NA, adj_col.w, NB);
+
+    // 3. reverse walk over the segment
+    {
+      int k = s1 - 1;
+      float2 v0 = k >= s0 ? __ldcs(rec + k) : make_float2(0.f, 0.f);
+      float2 v1 = k - 1 >= s0 ? __ldcs(rec + k - 1) : make_float2(0.f, 0.f);
+      for (; k - 1 >= s0; k -= 2) {
+        const float2 u0 = k - 2 >= s0 ? __ldcs(rec + k - 2) : make_float2(0.f, 0.f);  // next pair, in flight
+        const float2 u1 = k - 3 >= s0 ? __ldcs(rec + k - 3) : make_float2(0.f, 0.f);
+        record_reverse_step<BLEND>(tf, step, v0.x, v0.y, adj_acc, acc_tf);
+        record_reverse_step<BLEND>(tf, step, v1.x, v1.y, adj_acc, acc_tf);
+        v0 = u0;
+        v1 = u1;
+      }
+      if (k >= s0) record_reverse_step<BLEND>(tf, step, v0.x, v0.y, adj_acc, acc_tf);
     }
   }
 
