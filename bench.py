@@ -79,10 +79,16 @@ class ClockSampler:
         self.proc = None
 
     def __enter__(self):
+        # 10 ms samples; the timed region starts once the first sample is out
+        # (nvidia-smi takes a while to start), so it lies inside the record
+        self.first = []
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "10"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            line = self.proc.stdout.readline()
+            if line.strip():
+                self.first.append(line)
         except Exception:
             self.proc = None
         return self
@@ -96,7 +102,7 @@ class ClockSampler:
             except Exception:
                 self.proc.kill()
                 out, _ = self.proc.communicate()
-            self.lines = [l for l in out.splitlines() if l.strip()]
+            self.lines = [l for l in self.first + out.splitlines() if l.strip()]
 
     def summary(self):
         sm, mx, reasons = [], None, set()
@@ -354,10 +360,10 @@ def run_gpu(args):
     P = B * H * W
     ck_written = int(torch.clamp((term.to(torch.int64) - 1) // K, min=0).clamp_max(slots).sum().item())
     if args.record == "full":
-        # forward: volume, colour + termination + offset, checkpoints, one density per sample;
-        # adjoint: termination + adj_color + offset, checkpoints, densities, TF (no volume reads)
-        fwd_bytes = V * 2 + P * (16 + 4 + 4) + ck_written * 4 + samples * 4
-        adj_bytes = P * (4 + 16 + 4) + ck_written * 4 + samples * 4 + tf.numel() * 4 * 2
+        # forward: volume, colour + termination + offset, checkpoints, a (density, opacity) pair per sample;
+        # adjoint: termination + adj_color + offset, the pairs, TF in and out (no volume, no checkpoints)
+        fwd_bytes = V * 2 + P * (16 + 4 + 4) + ck_written * 4 + samples * 8
+        adj_bytes = P * (4 + 16 + 4) + samples * 8 + tf.numel() * 4 * 2
     else:
         fwd_bytes = V * 2 + P * (16 + 4) + ck_written * 4
         adj_bytes = V * 2 + P * (4 + 16) + ck_written * 4 + tf.numel() * 4 * 2
@@ -365,8 +371,8 @@ def run_gpu(args):
     achieved = dominant[1] / (dominant[2] / 1e3) / 1e9
     tr = profiled_traffic()
     traffic = None
-    if tr and tr.get("kernel") == dominant[0]:
-        traffic = tr.get("dram_bytes_per_launch")
+    if tr and tr.get("record") == args.record and tr.get("views") == B:
+        traffic = tr.get("dram_bytes_per_launch", {}).get(dominant[0])
     # 8 BF16 corner reads per sample in the forward, and in the adjoint unless it reads the record
     gather_bytes = samples * 8 * 2 * (1 if args.record == "full" else 2)
 

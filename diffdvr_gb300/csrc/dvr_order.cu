@@ -42,15 +42,20 @@ __device__ __forceinline__ int work_key(const RenderParams& p, const AdjointPara
   return kBuckets - 1 - r;
 }
 
+// keys[id] keeps each ray's bucket for the scatter pass
 template <bool FWD>
 __global__ void __launch_bounds__(kOrderThreads) work_histogram_kernel(const RenderParams p, const AdjointParams a,
-                                                                       const RayOrder o, int* hist) {
+                                                                       const RayOrder o, int* hist,
+                                                                       unsigned char* keys) {
   __shared__ int sh[kBuckets];
   sh[threadIdx.x] = 0;
   __syncthreads();
   const int total = int(o.total());
-  for (int id = blockIdx.x * kOrderThreads + threadIdx.x; id < total; id += gridDim.x * kOrderThreads)
-    atomicAdd(&sh[work_key<FWD>(p, a, o, id)], 1);
+  for (int id = blockIdx.x * kOrderThreads + threadIdx.x; id < total; id += gridDim.x * kOrderThreads) {
+    const int key = work_key<FWD>(p, a, o, id);
+    keys[id] = static_cast<unsigned char>(key);
+    atomicAdd(&sh[key], 1);
+  }
   __syncthreads();
   if (sh[threadIdx.x] > 0) atomicAdd(&hist[threadIdx.x], sh[threadIdx.x]);
 }
@@ -85,8 +90,9 @@ __device__ __forceinline__ void finish_empty_ray(const RenderParams& p, const Ra
 }
 
 template <bool FWD>
-__global__ void __launch_bounds__(kOrderThreads) work_scatter_kernel(const RenderParams p, const AdjointParams a,
-                                                                     const RayOrder o, int* start, int* list) {
+__global__ void __launch_bounds__(kOrderThreads) work_scatter_kernel(const RenderParams p, const RayOrder o,
+                                                                     const unsigned char* keys, int* start,
+                                                                     int* list) {
   __shared__ int cnt[kBuckets];
   __shared__ int base[kBuckets];
   const int total = int(o.total());
@@ -94,7 +100,7 @@ __global__ void __launch_bounds__(kOrderThreads) work_scatter_kernel(const Rende
     cnt[threadIdx.x] = 0;
     __syncthreads();
     const int id = first + threadIdx.x;
-    const int key = id < total ? work_key<FWD>(p, a, o, id) : 0;
+    const int key = id < total ? int(keys[id]) : 0;
     const int rank = id < total ? atomicAdd(&cnt[key], 1) : 0;
     __syncthreads();
     if (cnt[threadIdx.x] > 0) base[threadIdx.x] = atomicAdd(&start[threadIdx.x], cnt[threadIdx.x]);
@@ -109,8 +115,10 @@ __global__ void __launch_bounds__(kOrderThreads) work_scatter_kernel(const Rende
 
 }  // namespace
 
+// histogram, bucket starts, count, list (total ints), keys (total bytes)
 size_t work_order_ints(const RenderParams& p) {
-  return work_order_list_offset + size_t(RayOrder::make(p.W, p.H, p.B).total());
+  const size_t total = size_t(RayOrder::make(p.W, p.H, p.B).total());
+  return work_order_list_offset + total + (total + 3) / 4;
 }
 
 cudaError_t order_rays_by_work(const RenderParams& p, const AdjointParams* a, int* scratch, const LaunchInfo& li,
@@ -122,18 +130,19 @@ cudaError_t order_rays_by_work(const RenderParams& p, const AdjointParams* a, in
   int* start = scratch + kBuckets;
   int* with_work = scratch + work_order_count_offset;
   int* list = scratch + work_order_list_offset;
+  unsigned char* keys = reinterpret_cast<unsigned char*>(list + total);
   cudaError_t e = cudaMemsetAsync(hist, 0, kBuckets * sizeof(int), s);
   if (e != cudaSuccess) return e;
   const int blocks = int(std::min<int64_t>((total + kOrderThreads - 1) / kOrderThreads, int64_t(li.num_sms) * 8));
   if (a) {
-    work_histogram_kernel<false><<<blocks, kOrderThreads, 0, s>>>(p, *a, o, hist);
+    work_histogram_kernel<false><<<blocks, kOrderThreads, 0, s>>>(p, *a, o, hist, keys);
     work_scan_kernel<<<1, kOrderThreads, 0, s>>>(hist, start, with_work);
-    work_scatter_kernel<false><<<blocks, kOrderThreads, 0, s>>>(p, *a, o, start, list);
+    work_scatter_kernel<false><<<blocks, kOrderThreads, 0, s>>>(p, o, keys, start, list);
   } else {
     const AdjointParams none{};
-    work_histogram_kernel<true><<<blocks, kOrderThreads, 0, s>>>(p, none, o, hist);
+    work_histogram_kernel<true><<<blocks, kOrderThreads, 0, s>>>(p, none, o, hist, keys);
     work_scan_kernel<<<1, kOrderThreads, 0, s>>>(hist, start, with_work);
-    work_scatter_kernel<true><<<blocks, kOrderThreads, 0, s>>>(p, none, o, start, list);
+    work_scatter_kernel<true><<<blocks, kOrderThreads, 0, s>>>(p, o, keys, start, list);
   }
   return cudaGetLastError();
 }

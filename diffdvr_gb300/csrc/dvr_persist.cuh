@@ -74,6 +74,7 @@ __global__ void __launch_bounds__(kFastThreads) fast_adjoint_persistent_kernel(c
                                                                                 const int* ray_list,
                                                                                 const int* ray_count) {
   extern __shared__ float4 fast_smem4[];
+  if (ray_count && *ray_count == 0) return;  // an empty list: nothing to add
   constexpr int C = TfChannels<TF>::C;
   float* smem = reinterpret_cast<float*>(fast_smem4);
   const int copies = tf_copies(p);
