@@ -4,8 +4,13 @@ function (pytests/diffdvr/renderer.py:61-359), adjoint method.
 ``forward`` renders with ``pyrenderer.Renderer.render_forward`` and saves the
 outputs; ``backward`` zero-initialises the enabled gradients and calls
 ``render_adjoint``.  When gradients are required, the forward pass also
-fills a transmittance-checkpoint buffer so the adjoint re-marches segments
-instead of inverting the blend.
+fills a transmittance-checkpoint buffer (the adjoint re-marches segments
+instead of inverting the blend) and, by default, a sample record: every
+sample's density and incoming opacity, which the adjoint reads instead of
+re-sampling the volume.  The record takes 8 bytes per sample; with
+``sample_record="auto"`` the pool is sized for every ray when that fits in a
+quarter of the free device memory, else as large as that allows (rays that
+find it full are re-sampled).
 
 The reference's forward-mode differentiation (``gradient_method="forward"``)
 is not part of this renderer; requesting it raises ``NotImplementedError``.
@@ -58,12 +63,31 @@ def _implies(a, b) -> bool:
     return (not a) or b
 
 
+def _record_floats(inputs, batch: int, sample_record, device) -> int:
+    """Floats of the sample-record pool for a forward pass (0: none).
+    sample_record: False / 0 (none), True (every ray), "auto" (every ray if
+    that fits in a quarter of the free device memory, else as much as fits),
+    or an int number of bytes."""
+    if sample_record is False or sample_record is None or sample_record == 0:
+        return 0
+    full = pyrenderer.Renderer.sample_density_size(inputs, batch)
+    if sample_record is True:
+        n = full
+    elif sample_record == "auto":
+        free, _ = torch.cuda.mem_get_info(device)
+        n = min(full, free // 4 // 4)
+    else:
+        n = min(full, int(sample_record) // 4)
+    n = n // 4 * 4
+    return n if n >= 4 else 0
+
+
 class _RendererFunction(torch.autograd.Function):
     @staticmethod
     def forward(ctx, camera_matrix, camera_ray_start, camera_ray_dir, tf, volume,
                 inputs: pyrenderer.RendererInputs, fov_y_radians,
                 optimize_camera, optimize_tf, optimize_volume, tf_delayed_accumulation,
-                checkpoint_interval, profiling: Optional[ProfileRenderer]):
+                checkpoint_interval, sample_record, profiling: Optional[ProfileRenderer]):
         ctx.inputs = inputs
         ctx.fov_y_radians = fov_y_radians
         ctx.optimize = (optimize_camera, optimize_tf, optimize_volume)
@@ -88,19 +112,24 @@ class _RendererFunction(torch.autograd.Function):
             slots = pyrenderer.Renderer.checkpoint_slots(inputs, checkpoint_interval)
             ckpt = torch.empty(B, H, W, slots, dtype=torch.float32, device=volume.device)
         outputs = pyrenderer.RendererOutputs(color, term, ckpt, checkpoint_interval)
+        pool = _record_floats(inputs, B, sample_record, volume.device) if ckpt is not None else 0
+        if pool > 0:
+            outputs.sample_density = torch.empty(pool, dtype=torch.float32, device=volume.device)
+            outputs.sample_offset = torch.empty(B, H, W, dtype=torch.int32, device=volume.device)
         with _Timer(profiling is not None) as timer:
             pyrenderer.Renderer.render_forward(inputs, outputs)
         if profiling is not None:
             profiling.forward_ms += timer.elapsed_ms()
             profiling.forward_bytes += _size_of(camera_matrix, camera_ray_start, camera_ray_dir, tf, volume, color,
-                                                term, ckpt)
-        ctx.save_for_backward(camera_matrix, camera_ray_start, camera_ray_dir, tf, volume, color, term, ckpt)
+                                                term, ckpt, outputs.sample_density, outputs.sample_offset)
+        ctx.save_for_backward(camera_matrix, camera_ray_start, camera_ray_dir, tf, volume, color, term, ckpt,
+                              outputs.sample_density, outputs.sample_offset)
         ctx.checkpoint_interval = checkpoint_interval
         return color
 
     @staticmethod
     def backward(ctx, grad_color):
-        camera_matrix, ray_start, ray_dir, tf, volume, color, term, ckpt = ctx.saved_tensors
+        camera_matrix, ray_start, ray_dir, tf, volume, color, term, ckpt, rec, rec_off = ctx.saved_tensors
         optimize_camera, optimize_tf, optimize_volume = ctx.optimize
         inputs = ctx.inputs
         if inputs.camera_mode == pyrenderer.CameraMode.RayStartDir:
@@ -126,7 +155,7 @@ class _RendererFunction(torch.autograd.Function):
             g_volume = torch.zeros(volume.shape, dtype=torch.float32, device=volume.device)
             adj.has_volume_derivatives = True
             adj.adj_volume = g_volume
-        fwd = pyrenderer.RendererOutputs(color, term, ckpt, ctx.checkpoint_interval)
+        fwd = pyrenderer.RendererOutputs(color, term, ckpt, ctx.checkpoint_interval, rec, rec_off)
         with _Timer(ctx.profiling is not None) as timer:
             pyrenderer.Renderer.render_adjoint(inputs, fwd, grad_color.contiguous().float(), adj)
         if ctx.profiling is not None:
@@ -135,7 +164,7 @@ class _RendererFunction(torch.autograd.Function):
             g_tf = g_tf.to(tf.dtype)
         if g_volume is not None and volume.dtype != torch.float32:
             g_volume = g_volume.to(volume.dtype)
-        return None, g_start, g_dir, g_tf, g_volume, None, None, None, None, None, None, None, None
+        return None, g_start, g_dir, g_tf, g_volume, None, None, None, None, None, None, None, None, None
 
 
 class Renderer(nn.Module):
@@ -143,7 +172,8 @@ class Renderer(nn.Module):
 
     def __init__(self, settings: Optional[pyrenderer.RendererInputs] = None, optimize_camera=False,
                  optimize_tf=False, optimize_volume=False, gradient_method="adjoint",
-                 forward_delayed_gradients=False, tf_delayed_accumulation=True, checkpoint_interval: int = 16):
+                 forward_delayed_gradients=False, tf_delayed_accumulation=True, checkpoint_interval: int = 16,
+                 sample_record="auto"):
         super().__init__()
         self._settings = settings if settings is not None else pyrenderer.RendererInputs()
         self._optimize_camera = optimize_camera
@@ -156,6 +186,7 @@ class Renderer(nn.Module):
                                       "use gradient_method='adjoint'")
         self._tf_delayed_accumulation = tf_delayed_accumulation
         self._checkpoint_interval = int(checkpoint_interval)
+        self._sample_record = sample_record
         self._renderer_function = _RendererFunction.apply
 
     def get_settings(self):
@@ -199,4 +230,5 @@ class Renderer(nn.Module):
             volume = inputs.volume
         return self._renderer_function(camera_matrix, ray_start, ray_dir, tf, volume, inputs, fov_y_radians,
                                        self._optimize_camera, self._optimize_tf, self._optimize_volume,
-                                       self._tf_delayed_accumulation, self._checkpoint_interval, profiling)
+                                       self._tf_delayed_accumulation, self._checkpoint_interval,
+                                       self._sample_record, profiling)

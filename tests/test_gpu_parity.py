@@ -397,6 +397,25 @@ def test_autograd_module_matches_direct_calls(cuda_device):
     assert rel_l2(vol.grad.cpu().numpy(), g["adj_volume"]) <= 1e-5
 
 
+@pytest.mark.parametrize("sample_record", ["auto", 4096, False])
+def test_autograd_module_sample_record(sample_record, cuda_device):
+    """The module's TF gradient with the sample record (every ray, a 4 KB pool
+    that holds a few rays, none) equals the direct adjoint without a record to
+    rounding (relative L2 <= 1e-5)."""
+    from diffdvr_gb300 import Renderer
+    case = make_case(92, tf_mode=1, shape=(16, 18, 20), W=24, H=20, B=2, R=16, opacity=0.3, pad_faces=True)
+    inp = case.inputs("cuda")
+    tf = inp.tf.clone().requires_grad_(True)
+    r = Renderer(inp, optimize_tf=True, sample_record=sample_record)
+    img = r(tf=tf)
+    w = torch.randn_like(img)
+    (img * w).sum().backward()
+    inp2, out2 = gpu_forward(case, "optimized", checkpoints=True)
+    assert symmetric_error(img.detach().cpu().numpy(), out2.color.cpu().numpy()) <= 1e-5
+    g = gpu_adjoint(case, inp2, out2, w.cpu().numpy(), tf=True)
+    assert rel_l2(tf.grad.cpu().numpy(), g["adj_tf"]) <= 1e-5
+
+
 def test_camera_gradient_through_generate_rays(cuda_device):
     """optimize_camera: the module generates per-pixel rays from the viewport
     with differentiable torch ops and the adjoint returns ray gradients."""
