@@ -20,6 +20,11 @@ Arms:
                    cores (the reference's own CPU marcher where it was built
                    here, else the oracle port), on a bounded sample of rays.
 
+Other configurations of the metric (`--workload`, not the default line):
+absorption_recon_128 (volume gradient, 64 views into 128^3), large_mixed_512
+(512^3 BF16, 16 views at 1024^2, ray + volume + TF gradients) and
+plain_cpu_64 (the CPU-sized case).
+
 Multi-GPU: rays and views shard without any exchange in a TF-only step except
 the TF-gradient sum, so N GPUs run N replicas ("scaling": "weak").
 """
@@ -38,7 +43,23 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "fwd+adjoint samples/sec: batched-BF16 vs plain FP32, grad rel err ≤1e-3"
-WORKLOAD = "tf_reconstruction_256: 256^3 blobs+noise, texture TF R=64, 8 views 256x256, step 0.25 voxel, TF grad"
+# the headline workload (the default) and the other configurations of the metric
+WORKLOADS = {
+    "tf_reconstruction_256": {
+        "desc": "tf_reconstruction_256: 256^3 blobs+noise, texture TF R=64, 8 views 256x256, step 0.25 voxel, TF grad",
+        "camera": "frame", "interval": 16, "estimate": "target", "res": 256, "views": 8, "image": 256},
+    "absorption_recon_128": {
+        "desc": "absorption_recon_128: 128^3 ellipsoid target, estimate 0.1, identity TF (absorption 20), "
+                "64 views 256x256, step 0.5 voxel, volume grad",
+        "camera": "frame", "interval": 32, "estimate": "const0.1", "res": 128, "views": 64, "image": 256},
+    "large_mixed_512": {
+        "desc": "large_mixed_512: 512^3 blobs+band-limited noise, linear TF R=16, 16 views 1024x1024 as per-pixel "
+                "rays, step 0.5 voxel, ray + volume + TF grads",
+        "camera": "rays", "interval": 16, "estimate": "target", "res": 512, "views": 16, "image": 1024},
+    "plain_cpu_64": {
+        "desc": "plain_cpu_64: 64^3 blobs, linear TF R=8, one 128x128 view, step 0.5 voxel, TF + volume grads",
+        "camera": "frame", "interval": 16, "estimate": "target", "res": 64, "views": 1, "image": 128},
+}
 
 
 def parse():
@@ -47,16 +68,24 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--res", type=int, default=256)
-    ap.add_argument("--views", type=int, default=8)
-    ap.add_argument("--image", type=int, default=256)
+    ap.add_argument("--workload", default="tf_reconstruction_256", choices=sorted(WORKLOADS))
+    ap.add_argument("--res", type=int, default=None, help="volume edge (workload default)")
+    ap.add_argument("--views", type=int, default=None, help="views (workload default)")
+    ap.add_argument("--image", type=int, default=None, help="image edge (workload default)")
+    ap.add_argument("--storage", choices=["bf16", "f16", "f32"], default="bf16", help="volume storage type")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP32 comparison arm")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline budget")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
-    ap.add_argument("--interval", type=int, default=16, help="transmittance checkpoint interval (samples)")
-    ap.add_argument("--record", choices=["full", "none"], default="full",
-                    help="sample-density record: a pool for every ray, or none (the adjoint re-samples)")
-    return ap.parse_args()
+    ap.add_argument("--interval", type=int, default=0, help="transmittance checkpoint interval (workload default)")
+    ap.add_argument("--record", choices=["full", "auto", "none"], default="auto",
+                    help="sample record: a pool for every ray; one for every ray if that fits in a quarter of "
+                         "the free device memory, else as large as that; or none")
+    a = ap.parse_args()
+    spec = WORKLOADS[a.workload]
+    for k in ("res", "views", "image"):
+        if getattr(a, k) is None:
+            setattr(a, k, spec[k])
+    return a
 
 
 def dist_env():
@@ -126,8 +155,13 @@ class ClockSampler:
 # ------------------------------------------------------------------ workload
 def make_workload(args):
     from diffdvr_gb300 import scenes
-    w = scenes.tf_reconstruction_256(seed=1, res=args.res, views=args.views, image=args.image)
-    return w
+    if args.workload == "absorption_recon_128":
+        return scenes.absorption_recon_128(seed=2, views=args.views, image=args.image)
+    if args.workload == "large_mixed_512":
+        return scenes.large_mixed_512(seed=4, res=args.res, views=args.views, image=args.image)
+    if args.workload == "plain_cpu_64":
+        return scenes.plain_cpu_64(seed=0)
+    return scenes.tf_reconstruction_256(seed=1, res=args.res, views=args.views, image=args.image)
 
 
 def measured_peaks():
@@ -149,6 +183,29 @@ def profiled_traffic():
 
 
 # ------------------------------------------------------------------ GPU arm
+def algorithmic_bytes(w, s_v, V, P, S, ck_written, recorded, record_kernel, tf_numel):
+    """Compulsory HBM bytes per forward and adjoint launch (SURVEY §8(d) model,
+    with the sample record): volume once, per-ray outputs/inputs, checkpoints,
+    the record (8 B per sample), gradients read-modify-written once."""
+    grads = set(w.grads)
+    fwd = V * s_v + P * (16 + 4) + ck_written * 4
+    if recorded:
+        fwd += P * 4 + S * 8
+    if record_kernel:
+        adj = P * (4 + 16 + 4) + S * 8 + tf_numel * 4 * 2
+    else:
+        regather = (not recorded) or ("camera" in grads)
+        adj = (V * s_v if regather else 0) + P * (4 + 16)
+        adj += (P * 4 + S * 8) if recorded else ck_written * 4
+        if "tf" in grads:
+            adj += tf_numel * 4 * 2
+        if "volume" in grads:
+            adj += V * 4 * 2
+        if "camera" in grads:
+            adj += P * 24 * 2
+    return fwd, adj
+
+
 def run_gpu(args):
     import torch
     import torch.distributed as dist
@@ -162,50 +219,89 @@ def run_gpu(args):
     _abi.load()
 
     w = make_workload(args)
-    B, H, W = args.views, args.image, args.image
-    vol32 = torch.from_numpy(w.volume).to(dev)
-    vol16 = vol32.to(torch.bfloat16)
+    spec = WORKLOADS[args.workload]
+    grads = set(w.grads)
+    B, H, W = w.ray_start.shape[0], w.height, w.width
+    vol_target32 = torch.from_numpy(w.volume).to(dev)
+    # the absorption reconstruction renders its estimate (0.1 everywhere) against the target's images
+    vol32 = torch.full_like(vol_target32, 0.1) if spec["estimate"] == "const0.1" else vol_target32
+    sdt = {"bf16": torch.bfloat16, "f16": torch.float16, "f32": torch.float32}[args.storage]
+    vol_s = vol32.to(sdt)
     tf = torch.from_numpy(w.tf).to(dev)
-    viewport = torch.from_numpy(w.viewport.astype(np.float32)).to(dev)
+    rays = spec["camera"] == "rays"
+    if rays:
+        cam = (torch.from_numpy(w.ray_start).to(dev), torch.from_numpy(w.ray_dir).to(dev))
+    else:
+        cam = (torch.from_numpy(w.viewport.astype(np.float32)).to(dev),)
 
-    def inputs(volume, tf_t, vp):
+    def inputs(volume, tf_t, cam_t):
         inp = pr.RendererInputs()
         inp.screen_size = pr.int2(W, H)
         inp.volume = volume
-        inp.volume_filter_mode = pr.VolumeFilterMode.Trilinear
+        inp.volume_filter_mode = pr.VolumeFilterMode(w.filter_mode)
         inp.box_min = pr.real3(*w.box_min)
         inp.box_size = pr.real3(*w.box_size)
-        inp.camera_mode = pr.CameraMode.ReferenceFrame
-        inp.camera = pr.CameraReferenceFrame(vp, float(w.fov_y))
+        if rays:
+            inp.camera_mode = pr.CameraMode.RayStartDir
+            inp.camera = pr.CameraPerPixelRays(cam_t[0], cam_t[1])
+        else:
+            inp.camera_mode = pr.CameraMode.ReferenceFrame
+            inp.camera = pr.CameraReferenceFrame(cam_t[0], float(w.fov_y))
         inp.step_size = float(w.step_size)
-        inp.tf_mode = pr.TFMode.Texture
+        inp.tf_mode = pr.TFMode(w.tf_mode)
         inp.tf = tf_t
-        inp.blend_mode = pr.BlendMode.BeerLambert
+        inp.blend_mode = pr.BlendMode(w.blend_mode)
         return inp
 
-    inp16 = inputs(vol16, tf, viewport)
-    K = args.interval
-    slots = pr.Renderer.checkpoint_slots(inp16, K)
+    inp_s = inputs(vol_s, tf, cam)
+    K = args.interval or spec["interval"]
+    slots = pr.Renderer.checkpoint_slots(inp_s, K)
     color = torch.empty(B, H, W, 4, device=dev)
     term = torch.empty(B, H, W, dtype=torch.int32, device=dev)
     ckpt = torch.empty(B, H, W, slots, device=dev)
     out = pr.RendererOutputs(color, term, ckpt, K)
-    if args.record == "full":
-        out.sample_density = torch.empty(pr.Renderer.sample_density_size(inp16, B), device=dev)
+    pool = 0
+    record_mode = "none"
+    if args.record != "none":
+        full = pr.Renderer.sample_density_size(inp_s, B)
+        pool = full
+        if args.record == "auto":
+            free, _ = torch.cuda.mem_get_info(dev)
+            pool = min(full, free // 4 // 4) // 4 * 4
+        record_mode = "full" if pool == full else "partial"
+        out.sample_density = torch.empty(pool, device=dev)
         out.sample_offset = torch.empty(B, H, W, dtype=torch.int32, device=dev)
-    adj_tf = torch.zeros_like(tf)
     adj = pr.AdjointOutputs()
-    adj.has_tf_derivatives = True
-    adj.tf_delayed_accumulation = True
-    adj.adj_tf = adj_tf
+    g_tensors = []
+    if "tf" in grads:
+        adj.has_tf_derivatives = True
+        adj.tf_delayed_accumulation = True
+        adj.adj_tf = torch.zeros(tf.shape, device=dev)
+        g_tensors.append(adj.adj_tf)
+    if "volume" in grads:
+        adj.has_volume_derivatives = True
+        adj.adj_volume = torch.zeros(vol32.shape, device=dev)
+        g_tensors.append(adj.adj_volume)
+    if "camera" in grads:
+        adj.has_camera_derivatives = True
+        adj.adj_camera_ray_start = torch.zeros(B, H, W, 3, device=dev)
+        adj.adj_camera_ray_dir = torch.zeros(B, H, W, 3, device=dev)
+        g_tensors += [adj.adj_camera_ray_start, adj.adj_camera_ray_dir]
     adj_color = torch.empty_like(color)
+    record_kernel = pool > 0 and grads == {"tf"} and w.tf_mode == 1
 
-    # target image: the same views rendered with the TF perturbed
-    g = torch.Generator(device="cpu").manual_seed(3)
-    tf_target = (tf.cpu() + 0.05 * torch.randn(tf.shape, generator=g)).clamp_min(0).to(dev)
+    # target image: the target volume (absorption reconstruction) or the TF perturbed
     target = torch.empty_like(color)
     pr.set_kernel_family("optimized")
-    pr.Renderer.render_forward(inputs(vol16, tf_target, viewport), pr.RendererOutputs(target, torch.empty_like(term)))
+    if spec["estimate"] == "const0.1":
+        t_inp = inputs(vol_target32.to(sdt), tf, cam)
+    else:
+        g = torch.Generator(device="cpu").manual_seed(3)
+        tf_target = (tf.cpu() + 0.05 * torch.randn(tf.shape, generator=g)).clamp_min(0).to(dev)
+        if w.tf_mode == 2:  # keep the linear TF's positions
+            tf_target[..., 4] = tf[..., 4]
+        t_inp = inputs(vol_s, tf_target, cam)
+    pr.Renderer.render_forward(t_inp, pr.RendererOutputs(target, torch.empty_like(term)))
     torch.cuda.synchronize()
     inv_n = 1.0 / color.numel()
 
@@ -214,19 +310,20 @@ def run_gpu(args):
     fwd_ev, adj_ev = [], []
 
     def step(record=False):
-        # forward + L2-loss gradient + adjoint of the TF
+        # forward + L2-loss gradient + adjoint
         if record:
             e = (ev(), ev(), ev(), ev())
             e[0].record()
-        pr.Renderer.render_forward(inp16, out)
+        pr.Renderer.render_forward(inp_s, out)
         if record:
             e[1].record()
         torch.sub(color, target, out=adj_color)
         adj_color.mul_(2 * inv_n)
-        adj_tf.zero_()
+        for t in g_tensors:
+            t.zero_()
         if record:
             e[2].record()
-        pr.Renderer.render_adjoint(inp16, out, adj_color, adj)
+        pr.Renderer.render_adjoint(inp_s, out, adj_color, adj)
         if record:
             e[3].record()
             fwd_ev.append((e[0], e[1]))
@@ -237,6 +334,7 @@ def run_gpu(args):
     torch.cuda.synchronize()
     samples = int(term.to(torch.int64).sum().item())
     rays_hit = int((term > 0).sum().item())
+    recorded_rays = int((out.sample_offset >= 0).sum().item()) if pool > 0 else 0
 
     # capture the step in a CUDA graph
     graph = torch.cuda.CUDAGraph()
@@ -290,53 +388,54 @@ def run_gpu(args):
     adj_ms = float(np.mean([a.elapsed_time(b) for a, b in adj_ev]))
 
     # ---- e2e: public API with host buffers
-    vol_host = vol16.cpu().pin_memory()
+    vol_host = vol_s.cpu().pin_memory()
     tf_host = tf.cpu().pin_memory()
-    vp_host = viewport.cpu().pin_memory()
+    cam_host = [c.cpu().pin_memory() for c in cam]
     target_host = target.cpu().pin_memory()
     loss_host = torch.empty(1, pin_memory=True)
-    grad_host = torch.empty_like(tf_host).pin_memory()
-    vol_d, tf_d, vp_d, tgt_d = torch.empty_like(vol16), torch.empty_like(tf), torch.empty_like(viewport), \
-        torch.empty_like(target)
-    inp_e2e = inputs(vol_d, tf_d, vp_d)
+    read_back = adj.adj_tf if "tf" in grads else None
+    grad_host = torch.empty_like(read_back, device="cpu").pin_memory() if read_back is not None else None
+    vol_d, tf_d, tgt_d = torch.empty_like(vol_s), torch.empty_like(tf), torch.empty_like(target)
+    cam_d = [torch.empty_like(c) for c in cam]
+    inp_e2e = inputs(vol_d, tf_d, cam_d)
     loss_d = torch.empty(1, device=dev)
 
     def e2e_step():
         vol_d.copy_(vol_host, non_blocking=True)
         tf_d.copy_(tf_host, non_blocking=True)
-        vp_d.copy_(vp_host, non_blocking=True)
+        for d, h in zip(cam_d, cam_host):
+            d.copy_(h, non_blocking=True)
         tgt_d.copy_(target_host, non_blocking=True)
         pr.Renderer.render_forward(inp_e2e, out)
         torch.sub(color, tgt_d, out=adj_color)
         loss_d.copy_((adj_color * adj_color).sum().view(1))
         adj_color.mul_(2 * inv_n)
-        adj_tf.zero_()
+        for t in g_tensors:
+            t.zero_()
         pr.Renderer.render_adjoint(inp_e2e, out, adj_color, adj)
         loss_host.copy_(loss_d, non_blocking=True)
-        grad_host.copy_(adj_tf, non_blocking=True)
+        if grad_host is not None:
+            grad_host.copy_(read_back, non_blocking=True)
 
     with torch.cuda.stream(stream):
         ms_e2e = timed(e2e_step, args.steps, args.warmup)
-    h2d = vol_host.numel() * vol_host.element_size() + tf_host.numel() * 4 + vp_host.numel() * 4 + \
+    h2d = vol_host.numel() * vol_host.element_size() + tf_host.numel() * 4 + sum(c.numel() * 4 for c in cam_host) + \
         target_host.numel() * 4
-    d2h = 4 + grad_host.numel() * 4
+    d2h = 4 + (grad_host.numel() * 4 if grad_host is not None else 0)
 
     # ---- plain FP32 arm (same workload, the reference's GPU algorithm)
     plain = None
     if not args.no_plain:
-        inp32 = inputs(vol32, tf, viewport)
+        inp32 = inputs(vol32, tf, cam)
         out32 = pr.RendererOutputs(torch.empty_like(color), torch.empty_like(term))
-        adj32 = pr.AdjointOutputs()
-        adj32.has_tf_derivatives = True
-        adj32.tf_delayed_accumulation = True
-        adj32.adj_tf = torch.zeros_like(tf)
 
         def plain_step():
             pr.Renderer.render_forward(inp32, out32)
             torch.sub(out32.color, target, out=adj_color)
             adj_color.mul_(2 * inv_n)
-            adj32.adj_tf.zero_()
-            pr.Renderer.render_adjoint(inp32, out32, adj_color, adj32)
+            for t in g_tensors:
+                t.zero_()
+            pr.Renderer.render_adjoint(inp32, out32, adj_color, adj)
 
         pr.set_kernel_family("plain")
         with torch.cuda.stream(stream):
@@ -356,25 +455,23 @@ def run_gpu(args):
 
     # ---- roofline of the dominant kernel (compulsory HBM bytes per launch)
     peak, peak_kind = measured_peaks()
-    V = args.res ** 3
+    V = int(np.prod(w.volume.shape[1:]))
     P = B * H * W
     ck_written = int(torch.clamp((term.to(torch.int64) - 1) // K, min=0).clamp_max(slots).sum().item())
-    if args.record == "full":
-        # forward: volume, colour + termination + offset, checkpoints, a (density, opacity) pair per sample;
-        # adjoint: termination + adj_color + offset, the pairs, TF in and out (no volume, no checkpoints)
-        fwd_bytes = V * 2 + P * (16 + 4 + 4) + ck_written * 4 + samples * 8
-        adj_bytes = P * (4 + 16 + 4) + samples * 8 + tf.numel() * 4 * 2
-    else:
-        fwd_bytes = V * 2 + P * (16 + 4) + ck_written * 4
-        adj_bytes = V * 2 + P * (4 + 16) + ck_written * 4 + tf.numel() * 4 * 2
+    s_v = vol_s.element_size()
+    fwd_bytes, adj_bytes = algorithmic_bytes(w, s_v, V, P, samples, ck_written, pool > 0, record_kernel, tf.numel())
     dominant = ("adjoint", adj_bytes, adj_ms) if adj_ms >= fwd_ms else ("forward", fwd_bytes, fwd_ms)
     achieved = dominant[1] / (dominant[2] / 1e3) / 1e9
     tr = profiled_traffic()
     traffic = None
-    if tr and tr.get("record") == args.record and tr.get("views") == B:
+    if tr and tr.get("workload") == args.workload and tr.get("record") == record_mode and tr.get("views") == B:
         traffic = tr.get("dram_bytes_per_launch", {}).get(dominant[0])
-    # 8 BF16 corner reads per sample in the forward, and in the adjoint unless it reads the record
-    gather_bytes = samples * 8 * 2 * (1 if args.record == "full" else 2)
+    # 8 corner reads per sample in the forward, and in the adjoint unless it reads the record
+    regather = pool == 0 or "camera" in grads
+    gather_bytes = samples * 8 * s_v * (2 if regather else 1)
+    # kernels of ours per step: forward = ray order (3) + march; adjoint = ray order (3) + the
+    # record kernel and the general kernel over its leftovers, or the general kernel alone
+    launches_per_step = 4 + (5 if record_kernel else 4)
 
     result = {
         "metric": METRIC,
@@ -387,18 +484,20 @@ def run_gpu(args):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "bf16-storage/f32-compute",
-        "data": "synthetic (seeded blobs + noise, random TF, Fibonacci views)",
-        "config": {"workload": WORKLOAD, "volume_storage": "bf16", "tf_storage": "f32", "views": B,
-                   "image": [H, W], "volume": [args.res] * 3, "samples_per_step": samples, "rays_hit": rays_hit,
-                   "checkpoint_interval": K, "sample_density_record": args.record,
+        "dtype": f"{args.storage}-storage/f32-compute",
+        "data": "synthetic (seeded, shapes and distributions of the workload)",
+        "config": {"workload": spec["desc"], "volume_storage": args.storage,
+                   "tf_storage": "f32", "views": B, "image": [H, W], "volume": list(w.volume.shape[1:]),
+                   "gradients": sorted(grads), "samples_per_step": samples, "rays_hit": rays_hit,
+                   "checkpoint_interval": K, "sample_record": record_mode,
+                   "recorded_rays": recorded_rays, "record_pool_MB": round(pool * 4 / 1e6, 1),
                    "l2": "flushed (256 MB write) before every timed step",
                    "graph": "forward+loss+adjoint captured in one CUDA graph",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": "samples/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": ms_e2e,
                 "path": "pyrenderer.Renderer.render_forward/render_adjoint, pinned host inputs"},
-        "gpu_launches": 2 * args.steps,
+        "gpu_launches": launches_per_step * args.steps,
         "kernel_ms": {"forward": fwd_ms, "adjoint": adj_ms},
         "roofline": {"bound": "hbm", "kernel": dominant[0], "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
@@ -409,7 +508,7 @@ def run_gpu(args):
         "clocks": clock_summary,
     }
     if rank == 0:
-        result["cpu_baseline"] = None if args.no_cpu else cpu_baseline(w, args, samples / P)
+        result["cpu_baseline"] = None if args.no_cpu else cpu_baseline(w, args, vol32.cpu().numpy())
         print(json.dumps(result))
     if world > 1:
         dist.barrier()
@@ -417,8 +516,8 @@ def run_gpu(args):
 
 
 # ------------------------------------------------------------------ CPU (reference) arm
-def cpu_sample_scene(w, n_rays: int, seed: int = 0):
-    """A bounded sample of the workload: n_rays rays of the 8 views, chosen
+def cpu_sample_scene(w, volume, n_rays: int, seed: int = 0):
+    """A bounded sample of the workload: n_rays rays of its views, chosen
     among rays that hit the volume, as one 1 x n_rays 'image'."""
     from oracle import oracle as O
     rng = np.random.default_rng(seed)
@@ -429,23 +528,25 @@ def cpu_sample_scene(w, n_rays: int, seed: int = 0):
     closest = rs + t[:, None] * rd
     hit = np.nonzero(np.linalg.norm(closest, axis=1) < 0.866)[0]
     idx = rng.choice(hit, size=min(n_rays, hit.size), replace=False)
-    sc = O.Scene(width=idx.size, height=1, volume=w.volume, tf=w.tf, step_size=np.full((1, 1, 1), w.step_size),
-                 box_min=np.array([w.box_min]), box_size=np.array([w.box_size]), filter_mode=1, camera_mode=0,
-                 tf_mode=1, blend_mode=0, ray_start=rs[idx][None, None], ray_dir=rd[idx][None, None])
+    sc = O.Scene(width=idx.size, height=1, volume=volume, tf=w.tf, step_size=np.full((1, 1, 1), w.step_size),
+                 box_min=np.array([w.box_min]), box_size=np.array([w.box_size]), filter_mode=w.filter_mode,
+                 camera_mode=0, tf_mode=w.tf_mode, blend_mode=w.blend_mode, ray_start=rs[idx][None, None],
+                 ray_dir=rd[idx][None, None])
     return sc
 
 
-def time_cpu(w, budget_s: float, kind: str):
-    """Forward + TF adjoint of a ray sample on the host cores; returns
-    (samples/s, description)."""
+def time_cpu(w, volume, budget_s: float, kind: str):
+    """Forward + adjoint (the workload's gradients) of a ray sample on the host
+    cores; returns (samples/s, description)."""
     from oracle import oracle as O
+    req = O.AdjointRequest(tf="tf" in w.grads, volume="volume" in w.grads, camera="camera" in w.grads)
     n = 512
     while True:
-        sc = cpu_sample_scene(w, n)
+        sc = cpu_sample_scene(w, volume, n)
         t0 = time.perf_counter()
         c, term = O.forward(sc, kind, "f32")
         adj = np.full(c.shape, 1e-3, np.float32)
-        O.adjoint(sc, c, term, adj, O.AdjointRequest(tf=True), kind, "f32")
+        O.adjoint(sc, c, term, adj, req, kind, "f32")
         dt = time.perf_counter() - t0
         if dt > budget_s / 6 or n >= 65536:
             break
@@ -454,18 +555,18 @@ def time_cpu(w, budget_s: float, kind: str):
     while total < budget_s * 0.7 or reps < 2:
         t0 = time.perf_counter()
         c, term = O.forward(sc, kind, "f32")
-        O.adjoint(sc, c, term, np.full(c.shape, 1e-3, np.float32), O.AdjointRequest(tf=True), kind, "f32")
+        O.adjoint(sc, c, term, np.full(c.shape, 1e-3, np.float32), req, kind, "f32")
         total += time.perf_counter() - t0
         samples += int(term.sum())
         reps += 1
     return samples / total, f"{sc.width} rays of the workload (hitting the volume), {reps} fwd+adj passes"
 
 
-def cpu_baseline(w, args, _samples_per_ray):
+def cpu_baseline(w, args, volume):
     from oracle import oracle as O
     O.build(reference=True)
     kind = "reference" if O.reference_available() else "port"
-    value, sample = time_cpu(w, args.cpu_seconds, kind)
+    value, sample = time_cpu(w, volume, args.cpu_seconds, kind)
     return {"value": value, "unit": "samples/s", "cores": os.cpu_count(), "kind": kind, "sample": sample}
 
 
@@ -477,19 +578,20 @@ def run_reference(args):
     O.build(reference=True)
     kind = "reference" if O.reference_available() else "port"
     w = make_workload(args)
+    volume = np.full_like(w.volume, 0.1) if WORKLOADS[args.workload]["estimate"] == "const0.1" else w.volume
     for _ in range(args.warmup):
-        time_cpu(w, 1.0, kind)
+        time_cpu(w, volume, 1.0, kind)
     vals = []
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        v, sample = time_cpu(w, max(1.0, args.cpu_seconds / max(args.steps, 1)), kind)
+        v, sample = time_cpu(w, volume, max(1.0, args.cpu_seconds / max(args.steps, 1)), kind)
         vals.append(v)
     wall = time.perf_counter() - t0
     value = float(np.median(vals))
     res = {"metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": wall * 1e3 / max(args.steps, 1), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-           "config": {"workload": WORKLOAD, "sample": sample}, "impl": "reference",
+           "config": {"workload": WORKLOADS[args.workload]["desc"], "sample": sample}, "impl": "reference",
            "cpu_baseline": {"value": value, "unit": "samples/s", "cores": os.cpu_count(), "kind": kind,
                             "sample": sample},
            "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

@@ -202,6 +202,38 @@ def absorption_recon_128(seed: int = 2, views: int = 64, image: int = 256) -> Wo
                     viewport=vp, fov_y=fov, grads=("volume",))
 
 
+def band_limited_noise(res: int, rng: np.random.Generator, cells: int = 64, dtype=np.float32) -> np.ndarray:
+    """Low-pass filtered white noise in [0, 1): U(0,1) on a cells^3 lattice,
+    trilinearly interpolated to res^3 (cell-centred); shape res*res*res."""
+    from scipy import ndimage
+    lattice = rng.uniform(0, 1, (cells, cells, cells)).astype(np.float32)
+    coords = (np.arange(res, dtype=np.float32) + 0.5) * (cells / res) - 0.5
+    out = np.empty((res, res, res), dtype=np.float32)
+    gy, gz = np.meshgrid(coords, coords, indexing="ij")
+    for i, cx in enumerate(coords):  # one x slice at a time keeps memory small
+        pts = np.stack([np.full_like(gy, cx), gy, gz])
+        out[i] = ndimage.map_coordinates(lattice, pts, order=1, mode="nearest")
+    return out.astype(dtype)
+
+
+def large_mixed_512(seed: int = 4, res: int = 512, views: int = 16, image: int = 1024,
+                    noise: float = 0.1) -> Workload:
+    """Large mixed-precision case: res^3 volume of 64 blobs plus band-limited
+    noise (stored BF16/FP16 by the caller), 16-point linear TF (absorption x10),
+    `views` Fibonacci views at image^2 on radius 3 as per-pixel rays, Beer-Lambert,
+    step 0.5 voxel; gradients with respect to the rays, the volume and the TF."""
+    rng = np.random.default_rng(seed)
+    vol = blob_volume(res, 64, rng)[0]
+    vol = np.clip(vol + noise * band_limited_noise(res, rng), 0, 1).astype(np.float32)[None]
+    tf = tf_linear(16, rng, 10.0)
+    lat, lon = fibonacci_sphere(views)
+    vp = viewport_from_sphere(lat, lon, 3.0)
+    fov = np.radians(45.0)
+    rs, rd = generate_rays(vp, fov, image, image)
+    return Workload("large_mixed_512", vol, tf, 2, 0, 1, rs, rd, 0.5 / (res - 1), image, image,
+                    viewport=vp, fov_y=fov, grads=("camera", "volume", "tf"))
+
+
 def small_scene(seed: int, shape=(9, 10, 11), W: int = 12, H: int = 10, B: int = 2,
                 tf_mode: int = 1, R: Optional[int] = None, opacity: float = 1.0, pad_faces: bool = False,
                 dtype=np.float32) -> Workload:
