@@ -670,16 +670,28 @@ struct VolGradCell {
         const int lx = clampi(cx, 0, X1), hx = clampi(cx + 1, 0, X1);
         const int ly = clampi(cy, 0, Y1), hy = clampi(cy + 1, 0, Y1);
         const int lz = clampi(cz, 0, Z1), hz = clampi(cz + 1, 0, Z1);
-        atomicAdd(adjv + lx * sx + ly * sy + lz * sz, g[0]);
-        atomicAdd(adjv + lx * sx + ly * sy + hz * sz, g[1]);
-        atomicAdd(adjv + lx * sx + hy * sy + lz * sz, g[2]);
-        atomicAdd(adjv + lx * sx + hy * sy + hz * sz, g[3]);
-        atomicAdd(adjv + hx * sx + ly * sy + lz * sz, g[4]);
-        atomicAdd(adjv + hx * sx + ly * sy + hz * sz, g[5]);
-        atomicAdd(adjv + hx * sx + hy * sy + lz * sz, g[6]);
-        atomicAdd(adjv + hx * sx + hy * sy + hz * sz, g[7]);
+        const bool pair = sz == 1 && hz == lz + 1;  // the two z corners are adjacent floats
+        add_z(adjv + lx * sx + ly * sy, lz, hz, sz, pair, g[0], g[1]);
+        add_z(adjv + lx * sx + hy * sy, lz, hz, sz, pair, g[2], g[3]);
+        add_z(adjv + hx * sx + ly * sy, lz, hz, sz, pair, g[4], g[5]);
+        add_z(adjv + hx * sx + hy * sy, lz, hz, sz, pair, g[6], g[7]);
       }
       reset();
+    }
+  }
+  // adds u at z = lz and v at z = hz of one (x, y) row of the gradient: one
+  // vector atomic when the two are adjacent floats inside an aligned 8- or
+  // 16-byte block, else two scalar atomics
+  __device__ __forceinline__ static void add_z(float* row, int lz, int hz, int64_t sz, bool pair, float u, float v) {
+    float* e = row + lz * sz;
+    const unsigned mis = static_cast<unsigned>(reinterpret_cast<uintptr_t>(e)) & 15u;
+    if (pair && (mis & 7u) == 0u) {
+      atomicAdd(reinterpret_cast<float2*>(e), make_float2(u, v));
+    } else if (pair && mis == 4u) {
+      atomicAdd(reinterpret_cast<float4*>(e - 1), make_float4(0.f, u, v, 0.f));
+    } else {
+      atomicAdd(e, u);
+      atomicAdd(row + hz * sz, v);
     }
   }
 };
