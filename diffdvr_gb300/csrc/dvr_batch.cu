@@ -1,11 +1,13 @@
-// Batched rendering of uneven instances in one launch.
+// Batched rendering of uneven instances.
 //
-// The host builds a work list of (instance, batch entry, tile) items ordered
-// by decreasing estimated cost (pixels of the tile times samples per ray), so
-// the block scheduler starts the longest tiles first and the tail of the
-// launch is made of short ones.  Instance descriptors and the list are copied
-// through a pinned staging buffer into a per-device workspace that the
-// library owns and grows on demand.
+// Instances are ordered by decreasing estimated cost (samples per ray), so the
+// block scheduler starts the longest tiles first and the tail of a launch is
+// made of short ones.  Up to kBatchMax instances go into one launch whose
+// kernel parameter carries their descriptors and item offsets
+// (BatchForwardTable / BatchAdjointTable): no staging copy, no device
+// workspace, nothing for a graph replay to go stale.  Also here: the
+// library's pools of work counters and per-stream scratch for the persistent
+// launches.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -17,51 +19,6 @@
 
 namespace dvr {
 namespace {
-
-struct Workspace {
-  void* dev = nullptr;
-  size_t dev_bytes = 0;
-  void* host = nullptr;       // pinned staging
-  size_t host_bytes = 0;
-  cudaEvent_t copied = nullptr;  // staging may be rewritten once this fired
-  std::mutex mutex;
-};
-Workspace g_ws[64];
-
-cudaError_t ensure(Workspace& w, size_t bytes) {
-  cudaError_t e = cudaSuccess;
-  if (!w.copied) {
-    e = cudaEventCreateWithFlags(&w.copied, cudaEventDisableTiming);
-    if (e != cudaSuccess) return e;
-  }
-  if (w.host_bytes < bytes) {
-    if (w.host) {
-      cudaEventSynchronize(w.copied);
-      cudaFreeHost(w.host);
-    }
-    w.host = nullptr;
-    w.host_bytes = 0;
-    e = cudaMallocHost(&w.host, bytes * 2);
-    if (e != cudaSuccess) return e;
-    w.host_bytes = bytes * 2;
-  }
-  if (w.dev_bytes < bytes) {
-    if (w.dev) {
-      // earlier launches may still read the old table
-      e = cudaDeviceSynchronize();
-      if (e != cudaSuccess) return e;
-      cudaFree(w.dev);
-    }
-    w.dev = nullptr;
-    w.dev_bytes = 0;
-    e = cudaMalloc(&w.dev, bytes * 2);
-    if (e != cudaSuccess) return e;
-    w.dev_bytes = bytes * 2;
-  }
-  return cudaSuccess;
-}
-
-size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 // Samples per ray, from the volume diagonal in voxels and the step in voxels
 // (step given by value; a step-size tensor counts as one voxel).
@@ -75,43 +32,21 @@ double cost_per_ray(const RenderParams& p) {
   return diag / std::max(step_vox, 1e-3);
 }
 
-std::vector<int4> build_items(const RenderParams* ps, int n) {
-  struct Inst {
-    int i;
-    double cost;
-  };
-  std::vector<Inst> order(n);
-  for (int i = 0; i < n; ++i) order[i] = {i, cost_per_ray(ps[i])};
-  std::stable_sort(order.begin(), order.end(), [](const Inst& a, const Inst& b) { return a.cost > b.cost; });
-  std::vector<int4> items;
-  for (const Inst& o : order) {
-    const RenderParams& p = ps[o.i];
-    const int tx = (p.W + kTileW - 1) / kTileW, ty = (p.H + kTileH - 1) / kTileH;
-    for (int b = 0; b < p.B; ++b)
-      for (int y = 0; y < ty; ++y)
-        for (int x = 0; x < tx; ++x) items.push_back(make_int4(o.i, b, x, y));
+// instances in decreasing cost order
+std::vector<int> cost_order(const RenderParams* ps, int n) {
+  std::vector<int> order(n);
+  std::vector<double> cost(n);
+  for (int i = 0; i < n; ++i) {
+    order[i] = i;
+    cost[i] = cost_per_ray(ps[i]);
   }
-  return items;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+  return order;
 }
 
-template <typename T>
-cudaError_t stage(Workspace& w, const std::vector<std::pair<const void*, size_t>>& parts, std::vector<size_t>& offs,
-                  cudaStream_t s) {
-  size_t total = 0;
-  offs.clear();
-  for (auto& pr : parts) {
-    offs.push_back(total);
-    total = align_up(total + pr.second, 256);
-  }
-  cudaError_t e = ensure(w, total);
-  if (e != cudaSuccess) return e;
-  e = cudaEventSynchronize(w.copied);  // the previous upload has left the staging buffer
-  if (e != cudaSuccess) return e;
-  for (size_t i = 0; i < parts.size(); ++i)
-    std::memcpy(static_cast<char*>(w.host) + offs[i], parts[i].first, parts[i].second);
-  e = cudaMemcpyAsync(w.dev, w.host, total, cudaMemcpyHostToDevice, s);
-  if (e != cudaSuccess) return e;
-  return cudaEventRecord(w.copied, s);
+// items (batch entries x tiles) of one instance
+int64_t instance_items(const RenderParams& p) {
+  return int64_t(p.B) * ((p.W + kTileW - 1) / kTileW) * ((p.H + kTileH - 1) / kTileH);
 }
 
 size_t max_tf_entries(const RenderParams* ps, int n) {
@@ -121,25 +56,22 @@ size_t max_tf_entries(const RenderParams* ps, int n) {
 }
 
 template <int TF>
-cudaError_t fwd_tf(const RenderParams* t, const int4* items, int n_items, size_t smem, int vst, int filter, int blend,
+cudaError_t fwd_tf(const BatchForwardTable& t, int n_items, size_t smem, int vst, int filter, int blend,
                    cudaStream_t s) {
   switch (vst) {
-    case kF16: return launch_fast_forward_batched_vt<TF, __half>(t, items, n_items, smem, filter, blend, s);
-    case kBF16: return launch_fast_forward_batched_vt<TF, __nv_bfloat16>(t, items, n_items, smem, filter, blend, s);
-    default: return launch_fast_forward_batched_vt<TF, float>(t, items, n_items, smem, filter, blend, s);
+    case kF16: return launch_fast_forward_batched_vt<TF, __half>(t, n_items, smem, filter, blend, s);
+    case kBF16: return launch_fast_forward_batched_vt<TF, __nv_bfloat16>(t, n_items, smem, filter, blend, s);
+    default: return launch_fast_forward_batched_vt<TF, float>(t, n_items, smem, filter, blend, s);
   }
 }
 
 template <int TF>
-cudaError_t adj_tf(const RenderParams* t, const AdjointParams* at, const int4* items, int n_items, size_t smem,
-                   int vst, int filter, int blend, bool vg, bool tg, cudaStream_t s) {
+cudaError_t adj_tf(const BatchAdjointTable& t, int n_items, size_t smem, int vst, int filter, int blend, bool vg,
+                   bool tg, cudaStream_t s) {
   switch (vst) {
-    case kF16:
-      return launch_fast_adjoint_batched_vt<TF, __half>(t, at, items, n_items, smem, filter, blend, vg, tg, s);
-    case kBF16:
-      return launch_fast_adjoint_batched_vt<TF, __nv_bfloat16>(t, at, items, n_items, smem, filter, blend, vg, tg, s);
-    default:
-      return launch_fast_adjoint_batched_vt<TF, float>(t, at, items, n_items, smem, filter, blend, vg, tg, s);
+    case kF16: return launch_fast_adjoint_batched_vt<TF, __half>(t, n_items, smem, filter, blend, vg, tg, s);
+    case kBF16: return launch_fast_adjoint_batched_vt<TF, __nv_bfloat16>(t, n_items, smem, filter, blend, vg, tg, s);
+    default: return launch_fast_adjoint_batched_vt<TF, float>(t, n_items, smem, filter, blend, vg, tg, s);
   }
 }
 
@@ -205,58 +137,66 @@ int* acquire_counter(int device, cudaStream_t s, cudaError_t& err) {
   return err == cudaSuccess ? c : nullptr;
 }
 
-cudaError_t launch_batched_forward(const RenderParams* ps, int n, int filter, int tf_mode, int blend, int device,
+cudaError_t launch_batched_forward(const RenderParams* ps, int n, int filter, int tf_mode, int blend, int,
                                    const LaunchInfo&, cudaStream_t s) {
-  std::vector<int4> items = build_items(ps, n);
-  if (items.empty()) return cudaSuccess;
-  if (items.size() > 0x7fffffffu) return cudaErrorInvalidConfiguration;
-  Workspace& w = g_ws[device & 63];
-  std::lock_guard<std::mutex> lock(w.mutex);
-  std::vector<size_t> offs;
-  cudaError_t e = stage<int>(w, {{ps, sizeof(RenderParams) * n}, {items.data(), sizeof(int4) * items.size()}}, offs, s);
-  if (e != cudaSuccess) return e;
-  const RenderParams* dt = reinterpret_cast<const RenderParams*>(static_cast<char*>(w.dev) + offs[0]);
-  const int4* di = reinterpret_cast<const int4*>(static_cast<char*>(w.dev) + offs[1]);
-  const size_t smem = max_tf_entries(ps, n) * sizeof(float);
-  const int ni = int(items.size()), vst = ps[0].vol_storage;
-  switch (tf_mode) {
-    case 0: return fwd_tf<0>(dt, di, ni, smem, vst, filter, blend, s);
-    case 1: return fwd_tf<1>(dt, di, ni, smem, vst, filter, blend, s);
-    case 2: return fwd_tf<2>(dt, di, ni, smem, vst, filter, blend, s);
-    default: return fwd_tf<3>(dt, di, ni, smem, vst, filter, blend, s);
+  const std::vector<int> order = cost_order(ps, n);
+  for (int first = 0; first < n; first += kBatchMax) {
+    BatchForwardTable t{};
+    t.n = std::min(kBatchMax, n - first);
+    int64_t items = 0;
+    size_t smem = 0;
+    for (int j = 0; j < t.n; ++j) {
+      const RenderParams& p = ps[order[first + j]];
+      t.p[j] = p;
+      items += instance_items(p);
+      if (items > 0x7fffffff) return cudaErrorInvalidConfiguration;
+      t.item_end[j] = int(items);
+      smem = std::max(smem, size_t(p.R) * p.C * sizeof(float));
+    }
+    if (items == 0) continue;
+    cudaError_t e;
+    switch (tf_mode) {
+      case 0: e = fwd_tf<0>(t, int(items), smem, t.p[0].vol_storage, filter, blend, s); break;
+      case 1: e = fwd_tf<1>(t, int(items), smem, t.p[0].vol_storage, filter, blend, s); break;
+      case 2: e = fwd_tf<2>(t, int(items), smem, t.p[0].vol_storage, filter, blend, s); break;
+      default: e = fwd_tf<3>(t, int(items), smem, t.p[0].vol_storage, filter, blend, s); break;
+    }
+    if (e != cudaSuccess) return e;
   }
+  return cudaSuccess;
 }
 
 cudaError_t launch_batched_adjoint(const RenderParams* ps, const AdjointParams* as, int n, int filter, int tf_mode,
-                                   int blend, int device, const LaunchInfo&, cudaStream_t s) {
-  std::vector<int4> items = build_items(ps, n);
-  if (items.empty()) return cudaSuccess;
-  if (items.size() > 0x7fffffffu) return cudaErrorInvalidConfiguration;
-  Workspace& w = g_ws[device & 63];
-  std::lock_guard<std::mutex> lock(w.mutex);
-  std::vector<size_t> offs;
-  cudaError_t e = stage<int>(w,
-                             {{ps, sizeof(RenderParams) * n},
-                              {as, sizeof(AdjointParams) * n},
-                              {items.data(), sizeof(int4) * items.size()}},
-                             offs, s);
-  if (e != cudaSuccess) return e;
-  const RenderParams* dt = reinterpret_cast<const RenderParams*>(static_cast<char*>(w.dev) + offs[0]);
-  const AdjointParams* da = reinterpret_cast<const AdjointParams*>(static_cast<char*>(w.dev) + offs[1]);
-  const int4* di = reinterpret_cast<const int4*>(static_cast<char*>(w.dev) + offs[2]);
+                                   int blend, int, const LaunchInfo&, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  const std::vector<int> order = cost_order(ps, n);
   const bool tg = as[0].has_tf != 0, vg = as[0].has_volume != 0;
-  size_t smem = 0;
-  for (int i = 0; i < n; ++i) {
-    const int seg = ps[i].ckpt.p ? ps[i].ckpt_interval : 0;
-    smem = std::max(smem, fast_adjoint_smem(tf_mode, ps[i].R, ps[i].C, tg, seg));
+  for (int first = 0; first < n; first += kBatchMax) {
+    BatchAdjointTable t{};
+    t.n = std::min(kBatchMax, n - first);
+    int64_t items = 0;
+    size_t smem = 0;
+    for (int j = 0; j < t.n; ++j) {
+      const int i = order[first + j];
+      t.p[j] = ps[i];
+      t.a[j] = as[i];
+      items += instance_items(ps[i]);
+      if (items > 0x7fffffff) return cudaErrorInvalidConfiguration;
+      t.item_end[j] = int(items);
+      const int seg = ps[i].ckpt.p ? ps[i].ckpt_interval : 0;
+      smem = std::max(smem, fast_adjoint_smem(tf_mode, ps[i].R, ps[i].C, tg, seg));
+    }
+    if (items == 0) continue;
+    cudaError_t e;
+    switch (tf_mode) {
+      case 0: e = adj_tf<0>(t, int(items), smem, t.p[0].vol_storage, filter, blend, vg, tg, s); break;
+      case 1: e = adj_tf<1>(t, int(items), smem, t.p[0].vol_storage, filter, blend, vg, tg, s); break;
+      case 2: e = adj_tf<2>(t, int(items), smem, t.p[0].vol_storage, filter, blend, vg, tg, s); break;
+      default: e = adj_tf<3>(t, int(items), smem, t.p[0].vol_storage, filter, blend, vg, tg, s); break;
+    }
+    if (e != cudaSuccess) return e;
   }
-  const int ni = int(items.size()), vst = ps[0].vol_storage;
-  switch (tf_mode) {
-    case 0: return adj_tf<0>(dt, da, di, ni, smem, vst, filter, blend, vg, tg, s);
-    case 1: return adj_tf<1>(dt, da, di, ni, smem, vst, filter, blend, vg, tg, s);
-    case 2: return adj_tf<2>(dt, da, di, ni, smem, vst, filter, blend, vg, tg, s);
-    default: return adj_tf<3>(dt, da, di, ni, smem, vst, filter, blend, vg, tg, s);
-  }
+  return cudaSuccess;
 }
 
 }  // namespace dvr

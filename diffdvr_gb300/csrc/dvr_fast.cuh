@@ -31,6 +31,38 @@
 namespace dvr {
 
 constexpr int kTileW = 16, kTileH = 8, kFastThreads = 128;
+
+// Batched launches carry their instance descriptors in the kernel parameter
+// (up to 32 KB since CUDA 12.1), so a batched call needs no staging copy and
+// no device workspace and can be captured into a CUDA graph.  One block per
+// (instance, batch entry, tile) item; instances are ordered by decreasing
+// cost and item_end[i] is the end of instance i's items.
+constexpr int kBatchMax = 24;  // instances per launch: 24 * (752 + 400) B of descriptors fit
+struct BatchForwardTable {
+  int n;
+  int item_end[kBatchMax];
+  RenderParams p[kBatchMax];
+};
+struct BatchAdjointTable {
+  int n;
+  int item_end[kBatchMax];
+  RenderParams p[kBatchMax];
+  AdjointParams a[kBatchMax];
+};
+static_assert(sizeof(BatchAdjointTable) <= 32764, "kernel parameter limit");
+
+__device__ __forceinline__ void batch_item(const int* item_end, int n, const RenderParams* ps, int item, int& inst,
+                                           int& b, int& tx, int& ty) {
+  inst = 0;
+  while (inst + 1 < n && item >= item_end[inst]) ++inst;
+  const int local = item - (inst > 0 ? item_end[inst - 1] : 0);
+  const int tiles_x = (ps[inst].W + kTileW - 1) / kTileW, tiles_y = (ps[inst].H + kTileH - 1) / kTileH;
+  const int per_b = tiles_x * tiles_y;
+  b = local / per_b;
+  const int r = local - b * per_b;
+  ty = r / tiles_x;
+  tx = r - ty * tiles_x;
+}
 constexpr int kMaxSegment = 64;  // largest checkpoint interval
 
 // Maps thread -> pixel within a 16x8 tile: warp w covers an 8x4 patch.
@@ -188,15 +220,15 @@ __global__ void __launch_bounds__(kFastThreads) fast_forward_kernel(const Render
 // a list ordered by decreasing estimated cost; the instance descriptors live
 // in device memory.
 template <int FILTER, int TF, int BLEND, typename VT>
-__global__ void __launch_bounds__(kFastThreads) fast_forward_batched_kernel(const RenderParams* __restrict__ table,
-                                                                             const int4* __restrict__ items) {
+__global__ void __launch_bounds__(kFastThreads) fast_forward_batched_kernel(const __grid_constant__ BatchForwardTable t) {
   extern __shared__ float4 fast_smem4[];
   float* s_tf = reinterpret_cast<float*>(fast_smem4);
-  const int4 it = items[blockIdx.x];
-  const RenderParams& p = table[it.x];
-  stage_tf(p, it.y, s_tf);
+  int inst, b, tx, ty;
+  batch_item(t.item_end, t.n, t.p, int(blockIdx.x), inst, b, tx, ty);
+  const RenderParams& p = t.p[inst];
+  stage_tf(p, b, s_tf);
   __syncthreads();
-  fast_forward_tile<FILTER, TF, BLEND, VT>(p, it.y, it.z, it.w, s_tf);
+  fast_forward_tile<FILTER, TF, BLEND, VT>(p, b, tx, ty, s_tf);
 }
 
 // ----------------------------------------------------------------- adjoint
@@ -927,11 +959,10 @@ __global__ void __launch_bounds__(kFastThreads) fast_adjoint_kernel(const Render
 }
 
 template <int FILTER, int TF, int BLEND, bool VOLGRAD, bool TFGRAD, typename VT>
-__global__ void __launch_bounds__(kFastThreads) fast_adjoint_batched_kernel(const RenderParams* __restrict__ table,
-                                                                             const AdjointParams* __restrict__ atable,
-                                                                             const int4* __restrict__ items) {
-  const int4 it = items[blockIdx.x];
-  fast_adjoint_block<FILTER, TF, BLEND, VOLGRAD, TFGRAD, VT>(table[it.x], atable[it.x], it.y, it.z, it.w);
+__global__ void __launch_bounds__(kFastThreads) fast_adjoint_batched_kernel(const __grid_constant__ BatchAdjointTable t) {
+  int inst, b, tx, ty;
+  batch_item(t.item_end, t.n, t.p, int(blockIdx.x), inst, b, tx, ty);
+  fast_adjoint_block<FILTER, TF, BLEND, VOLGRAD, TFGRAD, VT>(t.p[inst], t.a[inst], b, tx, ty);
 }
 
 }  // namespace dvr

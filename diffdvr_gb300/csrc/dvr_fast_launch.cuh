@@ -18,12 +18,11 @@ cudaError_t launch_fast_adjoint_vt(const RenderParams& p, const AdjointParams& a
                                    const LaunchInfo& li, cudaStream_t s);
 
 template <int TF, typename VT>
-cudaError_t launch_fast_forward_batched_vt(const RenderParams* table, const int4* items, int n_items, size_t smem,
-                                           int filter, int blend, cudaStream_t s);
-template <int TF, typename VT>
-cudaError_t launch_fast_adjoint_batched_vt(const RenderParams* table, const AdjointParams* atable, const int4* items,
-                                           int n_items, size_t smem, int filter, int blend, bool volgrad, bool tfgrad,
+cudaError_t launch_fast_forward_batched_vt(const BatchForwardTable& t, int n_items, size_t smem, int filter, int blend,
                                            cudaStream_t s);
+template <int TF, typename VT>
+cudaError_t launch_fast_adjoint_batched_vt(const BatchAdjointTable& t, int n_items, size_t smem, int filter, int blend,
+                                           bool volgrad, bool tfgrad, cudaStream_t s);
 template <int TF, typename VT>
 cudaError_t launch_fast_adjoint_into_vt(const RenderParams& p, const AdjointParams& a, int filter, int blend,
                                         const LaunchInfo& li, const CallerScratch& sc, cudaStream_t s);
@@ -36,13 +35,13 @@ static cudaError_t set_smem(K kernel, size_t smem) {
 }
 
 template <int TF, typename VT>
-cudaError_t launch_fast_forward_batched_vt(const RenderParams* table, const int4* items, int n_items, size_t smem,
-                                           int filter, int blend, cudaStream_t s) {
+cudaError_t launch_fast_forward_batched_vt(const BatchForwardTable& t, int n_items, size_t smem, int filter, int blend,
+                                           cudaStream_t s) {
   if (n_items == 0) return cudaSuccess;
   auto go = [&](auto kernel) {
     cudaError_t e = set_smem(kernel, smem);
     if (e != cudaSuccess) return e;
-    kernel<<<unsigned(n_items), kFastThreads, smem, s>>>(table, items);
+    kernel<<<unsigned(n_items), kFastThreads, smem, s>>>(t);
     return cudaGetLastError();
   };
   if (filter == kNearest)
@@ -53,12 +52,12 @@ cudaError_t launch_fast_forward_batched_vt(const RenderParams* table, const int4
 }
 
 template <int FILTER, int TF, int BLEND, typename VT>
-static cudaError_t fast_adjoint_batched_go(const RenderParams* table, const AdjointParams* atable, const int4* items,
-                                           int n_items, size_t smem, bool volgrad, bool tfgrad, cudaStream_t s) {
+static cudaError_t fast_adjoint_batched_go(const BatchAdjointTable& t, int n_items, size_t smem, bool volgrad,
+                                           bool tfgrad, cudaStream_t s) {
   auto go = [&](auto kernel) {
     cudaError_t e = set_smem(kernel, smem);
     if (e != cudaSuccess) return e;
-    kernel<<<unsigned(n_items), kFastThreads, smem, s>>>(table, atable, items);
+    kernel<<<unsigned(n_items), kFastThreads, smem, s>>>(t);
     return cudaGetLastError();
   };
   if (volgrad)
@@ -69,17 +68,16 @@ static cudaError_t fast_adjoint_batched_go(const RenderParams* table, const Adjo
 }
 
 template <int TF, typename VT>
-cudaError_t launch_fast_adjoint_batched_vt(const RenderParams* table, const AdjointParams* atable, const int4* items,
-                                           int n_items, size_t smem, int filter, int blend, bool volgrad, bool tfgrad,
-                                           cudaStream_t s) {
+cudaError_t launch_fast_adjoint_batched_vt(const BatchAdjointTable& t, int n_items, size_t smem, int filter, int blend,
+                                           bool volgrad, bool tfgrad, cudaStream_t s) {
   if (n_items == 0) return cudaSuccess;
   if (filter == kNearest)
     return blend == kBeerLambert
-               ? fast_adjoint_batched_go<kNearest, TF, kBeerLambert, VT>(table, atable, items, n_items, smem, volgrad, tfgrad, s)
-               : fast_adjoint_batched_go<kNearest, TF, kAlphaBlend, VT>(table, atable, items, n_items, smem, volgrad, tfgrad, s);
+               ? fast_adjoint_batched_go<kNearest, TF, kBeerLambert, VT>(t, n_items, smem, volgrad, tfgrad, s)
+               : fast_adjoint_batched_go<kNearest, TF, kAlphaBlend, VT>(t, n_items, smem, volgrad, tfgrad, s);
   return blend == kBeerLambert
-             ? fast_adjoint_batched_go<kTrilinear, TF, kBeerLambert, VT>(table, atable, items, n_items, smem, volgrad, tfgrad, s)
-             : fast_adjoint_batched_go<kTrilinear, TF, kAlphaBlend, VT>(table, atable, items, n_items, smem, volgrad, tfgrad, s);
+             ? fast_adjoint_batched_go<kTrilinear, TF, kBeerLambert, VT>(t, n_items, smem, volgrad, tfgrad, s)
+             : fast_adjoint_batched_go<kTrilinear, TF, kAlphaBlend, VT>(t, n_items, smem, volgrad, tfgrad, s);
 }
 
 // Grid of a persistent launch: every resident block slot, but no more
@@ -278,11 +276,10 @@ cudaError_t launch_fast_adjoint_into_vt(const RenderParams& p, const AdjointPara
                                                            cudaStream_t);                                    \
   template cudaError_t dvr::launch_fast_adjoint_vt<TF, VT>(const RenderParams&, const AdjointParams&, int, int, \
                                                            const LaunchInfo&, cudaStream_t);                 \
-  template cudaError_t dvr::launch_fast_forward_batched_vt<TF, VT>(const RenderParams*, const int4*, int, size_t, \
-                                                                   int, int, cudaStream_t);                  \
-  template cudaError_t dvr::launch_fast_adjoint_batched_vt<TF, VT>(const RenderParams*, const AdjointParams*,  \
-                                                                   const int4*, int, size_t, int, int, bool, bool, \
+  template cudaError_t dvr::launch_fast_forward_batched_vt<TF, VT>(const BatchForwardTable&, int, size_t, int, int, \
                                                                    cudaStream_t);                            \
+  template cudaError_t dvr::launch_fast_adjoint_batched_vt<TF, VT>(const BatchAdjointTable&, int, size_t, int, int, \
+                                                                   bool, bool, cudaStream_t);                            \
   template cudaError_t dvr::launch_fast_adjoint_into_vt<TF, VT>(const RenderParams&, const AdjointParams&, int,  \
                                                                 int, const LaunchInfo&, const CallerScratch&,  \
                                                                 cudaStream_t);

@@ -198,8 +198,9 @@ int dvr_render_adjoint_noalloc(const DvrRendererInputs* inputs, const DvrRendere
  * of (instance, view, tile) items.  All instances share the filter, TF and
  * blend modes and the volume storage dtype.  Extends the reference, whose
  * batches must share the volume and image sizes (renderer/renderer.cpp:59-70).
- * The per-instance descriptors are copied to a device workspace owned by the
- * library (grown on demand, reused across calls) on the same stream. */
+ * Up to 24 instances go into one launch whose kernel parameter carries their
+ * descriptors (more instances: several launches); nothing is copied or
+ * allocated, so the calls can be captured into a CUDA graph and replayed. */
 int dvr_render_forward_batched(const DvrRendererInputs* inputs, const DvrRendererOutputs* outputs, int32_t n,
                                void* cuda_stream);
 int dvr_render_adjoint_batched(const DvrRendererInputs* inputs, const DvrRendererOutputs* outputs_from_forward,

@@ -301,6 +301,84 @@ def test_batched_uneven_matches_single_instances(cuda_device):
         assert rel_l2(ao.adj_tf.cpu().numpy(), sg["adj_tf"]) <= 1e-4
 
 
+def _batched_setup(cases):
+    from diffdvr_gb300 import pyrenderer as pr
+    ins, outs, aos, adjs = [], [], [], []
+    g = torch.Generator(device="cuda").manual_seed(5)
+    for c in cases:
+        inp = c.inputs("cuda")
+        B = c.batch()
+        ck = torch.empty(B, c.height, c.width, pr.Renderer.checkpoint_slots(inp), device="cuda")
+        ins.append(inp)
+        outs.append(pr.RendererOutputs(torch.empty(B, c.height, c.width, 4, device="cuda"),
+                                       torch.empty(B, c.height, c.width, dtype=torch.int32, device="cuda"), ck, 16))
+        ao = pr.AdjointOutputs()
+        ao.has_volume_derivatives = True
+        ao.adj_volume = torch.zeros(c.volume.shape, device="cuda")
+        ao.has_tf_derivatives = True
+        ao.adj_tf = torch.zeros(c.tf.shape, device="cuda")
+        aos.append(ao)
+        adjs.append(torch.randn(B, c.height, c.width, 4, device="cuda", generator=g))
+    return ins, outs, aos, adjs
+
+
+def test_batched_calls_replay_in_a_cuda_graph(cuda_device):
+    """Batched forward + adjoint captured into one CUDA graph and replayed
+    twice give the eager batched results (the descriptors travel in the
+    kernel parameters, so nothing goes stale between replays)."""
+    from diffdvr_gb300 import pyrenderer as pr
+    cases = [make_case(71, tf_mode=3, shape=(9, 10, 11), W=20, H=12, B=1),
+             make_case(72, tf_mode=3, shape=(17, 13, 15), W=33, H=17, B=2)]
+    ins, outs, aos, adjs = _batched_setup(cases)
+
+    def step():
+        pr.Renderer.render_forward_batched(ins, outs)
+        for ao in aos:
+            ao.adj_volume.zero_()
+            ao.adj_tf.zero_()
+        pr.Renderer.render_adjoint_batched(ins, outs, adjs, aos)
+
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        step()
+    torch.cuda.synchronize()
+    ref = [(o.color.clone(), o.terminationIndex.clone(), a.adj_volume.clone(), a.adj_tf.clone())
+           for o, a in zip(outs, aos)]
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(stream):
+        with torch.cuda.graph(graph, stream=stream):
+            step()
+    for _ in range(2):
+        for o in outs:
+            o.color.fill_(float("nan"))
+            o.terminationIndex.fill_(-7)
+        graph.replay()
+        torch.cuda.synchronize()
+        for (c, t, gv, gt), o, a in zip(ref, outs, aos):
+            assert torch.equal(o.terminationIndex, t) and torch.equal(o.color, c)
+            assert rel_l2(a.adj_volume.cpu().numpy(), gv.cpu().numpy()) <= 1e-5
+            assert rel_l2(a.adj_tf.cpu().numpy(), gt.cpu().numpy()) <= 1e-5
+
+
+def test_batched_more_instances_than_one_launch_holds(cuda_device):
+    """26 instances (more than the 24 one launch carries) against single calls."""
+    from diffdvr_gb300 import pyrenderer as pr
+    cases = [make_case(200 + i, tf_mode=1, shape=(6 + i % 5, 7, 5 + i % 3), W=8 + i % 7, H=6 + i % 4, B=1 + i % 2)
+             for i in range(26)]
+    ins, outs, aos, adjs = _batched_setup(cases)
+    pr.Renderer.render_forward_batched(ins, outs)
+    pr.Renderer.render_adjoint_batched(ins, outs, adjs, aos)
+    torch.cuda.synchronize()
+    for c, o, a, adj in zip(cases, outs, aos, adjs):
+        si, so = gpu_forward(c, "optimized", checkpoints=True)
+        same = (so.terminationIndex == o.terminationIndex).cpu().numpy()
+        assert same.mean() >= 0.98
+        assert symmetric_error(so.color.cpu().numpy()[same], o.color.cpu().numpy()[same]) <= 1e-5
+        g = gpu_adjoint(c, si, so, adj.cpu().numpy(), volume=True, tf=True)
+        assert rel_l2(a.adj_volume.cpu().numpy(), g["adj_volume"]) <= 1e-4
+        assert rel_l2(a.adj_tf.cpu().numpy(), g["adj_tf"]) <= 1e-4
+
+
 def test_checkpointed_adjoint_is_exact_for_opaque_rays(oracle_built, cuda_device):
     """With high absorption the reference's blend inversion loses accuracy in
     FP32 (it divides by alpha - 1); the checkpointed adjoint does not."""
