@@ -84,6 +84,7 @@ constexpr unsigned kCounterInts = 4;  // 16 bytes per launch
 struct ScratchSlot {
   int device = -1;
   cudaStream_t stream = nullptr;
+  int slot = 0;
   void* ptr = nullptr;
   size_t bytes = 0;
 };
@@ -92,14 +93,14 @@ std::vector<ScratchSlot> g_scratch;
 
 }  // namespace
 
-void* acquire_scratch(int device, cudaStream_t s, size_t bytes, cudaError_t& err) {
+void* acquire_scratch(int device, cudaStream_t s, size_t bytes, cudaError_t& err, int which) {
   err = cudaSuccess;
   std::lock_guard<std::mutex> lock(g_scratch_mutex);
   ScratchSlot* slot = nullptr;
   for (auto& e : g_scratch)
-    if (e.device == device && e.stream == s) slot = &e;
+    if (e.device == device && e.stream == s && e.slot == which) slot = &e;
   if (!slot) {
-    g_scratch.push_back(ScratchSlot{device, s, nullptr, 0});
+    g_scratch.push_back(ScratchSlot{device, s, which, nullptr, 0});
     slot = &g_scratch.back();
   }
   if (slot->bytes < bytes) {

@@ -109,19 +109,44 @@ cudaError_t launch_fast_forward_vt(const RenderParams& p, int filter, int blend,
   if (!order_ints) return err;
   err = order_rays_by_work(p, nullptr, order_ints, li, s);
   if (err != cudaSuccess) return err;
+  // trilinear filtering reads the cell-corner volume, built here, when the
+  // cells fit in L2 with room to spare (64 MB of its 129 MB) or the volume
+  // itself is too large for L2 (one 16-byte sector per sample then replaces
+  // about four); in between (a volume that stays L2-resident, cells that
+  // would not) the corners are gathered directly.  Measured: 128^3 forward
+  // 2.38 -> 1.84 ms, 512^3 10.1 -> 9.4 ms; 256^3 BF16 0.84 ms direct, 0.96
+  // with cells.
+  const CellWords<VT>* cells = nullptr;
+  if (filter != kNearest) {
+    const int bv = p.volume.s[0] != 0 ? p.B : 1;
+    const size_t n = size_t(p.X) * p.Y * p.Z * bv;
+    const size_t cell_bytes = n * sizeof(CellWords<VT>), raw_bytes = n * sizeof(VT);
+    if (cell_bytes <= (size_t(64) << 20) || (raw_bytes > (size_t(64) << 20) && cell_bytes <= (size_t(8) << 30))) {
+      auto* c = static_cast<CellWords<VT>*>(acquire_scratch(li.device, s, cell_bytes, err, 1));
+      if (!c) return err;
+      const int blocks = int(std::min<size_t>((n + 255) / 256, size_t(li.num_sms) * 16));
+      build_cells_kernel<VT><<<blocks, 256, 0, s>>>(p, bv, c);
+      err = cudaGetLastError();
+      if (err != cudaSuccess) return err;
+      cells = c;
+    }
+  }
   auto go = [&](auto kernel) {
     cudaError_t e = set_smem(kernel, smem);
     if (e != cudaSuccess) return e;
     // one warp per ray: as many warps as fit, up to one per ray
     kernel<<<persistent_grid(kernel, smem, order.total() * 32, li), kFastThreads, smem, s>>>(
-        p, order, counter, order_ints + work_order_list_offset, order_ints + work_order_count_offset);
+        p, order, counter, order_ints + work_order_list_offset, order_ints + work_order_count_offset, cells);
     return cudaGetLastError();
   };
   if (filter == kNearest)
-    return blend == kBeerLambert ? go(fast_forward_warp_kernel<kNearest, TF, kBeerLambert, VT>)
-                                 : go(fast_forward_warp_kernel<kNearest, TF, kAlphaBlend, VT>);
-  return blend == kBeerLambert ? go(fast_forward_warp_kernel<kTrilinear, TF, kBeerLambert, VT>)
-                               : go(fast_forward_warp_kernel<kTrilinear, TF, kAlphaBlend, VT>);
+    return blend == kBeerLambert ? go(fast_forward_warp_kernel<kNearest, TF, kBeerLambert, VT, false>)
+                                 : go(fast_forward_warp_kernel<kNearest, TF, kAlphaBlend, VT, false>);
+  if (cells)
+    return blend == kBeerLambert ? go(fast_forward_warp_kernel<kTrilinear, TF, kBeerLambert, VT, true>)
+                                 : go(fast_forward_warp_kernel<kTrilinear, TF, kAlphaBlend, VT, true>);
+  return blend == kBeerLambert ? go(fast_forward_warp_kernel<kTrilinear, TF, kBeerLambert, VT, false>)
+                               : go(fast_forward_warp_kernel<kTrilinear, TF, kAlphaBlend, VT, false>);
 }
 
 // TF-gradient-only adjoint of a texture TF from the sample-density record:

@@ -21,8 +21,9 @@ int* acquire_counter(int device, cudaStream_t s, cudaError_t& err);
 
 // Scratch memory of at least `bytes` for launches on stream s, owned by the
 // library and reused by later launches on the same stream (grown on demand;
-// growing synchronises the stream).  Not zeroed.
-void* acquire_scratch(int device, cudaStream_t s, size_t bytes, cudaError_t& err);
+// growing synchronises the stream).  Not zeroed.  Slots are independent
+// buffers (0: ray order and TF-gradient slices, 1: cell-corner volume).
+void* acquire_scratch(int device, cudaStream_t s, size_t bytes, cudaError_t& err, int slot = 0);
 
 // Scratch handed in by the caller instead of the library's pools: `counter`
 // (one int, zeroed here on the stream before each launch) and `tf` (TF-gradient

@@ -17,6 +17,7 @@
 // so registers are few and many warps fit per SM.  Warps fetch one ray at a
 // time from the longest-first order of the rays with samples.
 #pragma once
+#include "dvr_cells.cuh"
 #include "dvr_persist.cuh"
 
 namespace dvr {
@@ -37,11 +38,13 @@ __device__ __forceinline__ float sample_density(const VolumeFast<VT>& v, float3 
 __device__ __forceinline__ float over(float a, float b) { return a + (1.f - a) * b; }
 
 // ray_list[0 .. *ray_count): the rays with samples (longest first); the
-// ordering pass has already finished the others.
-template <int FILTER, int TF, int BLEND, typename VT>
+// ordering pass has already finished the others.  CELLS: trilinear samples
+// read the cell-corner volume `cells`, else they gather the corners directly.
+template <int FILTER, int TF, int BLEND, typename VT, bool CELLS>
 __global__ void __launch_bounds__(kFastThreads) fast_forward_warp_kernel(const RenderParams p, const RayOrder order,
                                                                          int* counter, const int* ray_list,
-                                                                         const int* ray_count) {
+                                                                         const int* ray_count,
+                                                                         const CellWords<VT>* cells) {
   extern __shared__ float4 fast_smem4[];
   constexpr int C = TfChannels<TF>::C;
   float* s_tf = reinterpret_cast<float*>(fast_smem4);
@@ -81,6 +84,8 @@ __global__ void __launch_bounds__(kFastThreads) fast_forward_warp_kernel(const R
     }
     const VolumeFast<VT> vol{static_cast<const VT*>(p.volume.p) + b * p.volume.s[0], int(p.volume.s[1]),
                              int(p.volume.s[2]), int(p.volume.s[3]), p.X - 1, p.Y - 1, p.Z - 1};
+    const size_t vb = p.volume.s[0] != 0 ? size_t(b) * p.X * p.Y * p.Z : 0;
+    const CellVolume<VT> cv{cells ? cells + vb : nullptr, p.X - 1, p.Y - 1, p.Z - 1};
     const TfShared<C> tf{s_tf + (copies > 1 ? b : 0) * p.R * C, p.R};
     float* ck = p.ckpt.p ? static_cast<float*>(p.ckpt.p) + b * p.ckpt.s[0] + y * p.ckpt.s[1] + x * p.ckpt.s[2]
                          : nullptr;
@@ -95,7 +100,8 @@ __global__ void __launch_bounds__(kFastThreads) fast_forward_warp_kernel(const R
       float density = 0.f, a = 0.f;
       f4 c = mk4(0, 0, 0, 0);
       if (in_ray) {
-        density = sample_density<FILTER, VT>(vol, fast_pos(q, t));
+        if constexpr (CELLS) density = cv.sample(fast_pos(q, t));
+        else density = sample_density<FILTER, VT>(vol, fast_pos(q, t));
         c = tf_eval<TF>(tf, density);
         a = blend_alpha<BLEND>(c.w, q.step);
       }
