@@ -212,7 +212,7 @@ __global__ void __launch_bounds__(kFastThreads) fast_adjoint_persistent_kernel(c
         const int k = k0 + kk;
         if (active && ckpt_ray && k < k1) {
           if (drow) {  // recorded density and incoming opacity
-            const float2 v = __ldcs(drow + k);
+            const float2 v = __ldg(drow + k);
             seg_d[kk * blockDim.x] = v.x;
             seg_a[kk * blockDim.x] = v.y;
           } else {

@@ -182,7 +182,7 @@ __global__ void __launch_bounds__(kFastThreads) fast_adjoint_record_kernel(const
     {
       int k = s0;
       for (; k + 1 < s1; k += 2) {
-        const float2 v0 = __ldcs(rec + k), v1 = __ldcs(rec + k + 1);
+        const float2 v0 = __ldg(rec + k), v1 = __ldg(rec + k + 1);
         float A0, B0, A1, B1;
         record_sample_map<BLEND>(tf, step, v0.x, adj_col, A0, B0);
         record_sample_map<BLEND>(tf, step, v1.x, adj_col, A1, B1);
@@ -191,7 +191,7 @@ __global__ void __launch_bounds__(kFastThreads) fast_adjoint_record_kernel(const
       }
       if (k < s1) {
         float A0, B0;
-        record_sample_map<BLEND>(tf, step, __ldcs(rec + k).x, adj_col, A0, B0);
+        record_sample_map<BLEND>(tf, step, __ldg(rec + k).x, adj_col, A0, B0);
         compose(A, B, A0, B0);
       }
     }
@@ -209,11 +209,11 @@ __global__ void __launch_bounds__(kFastThreads) fast_adjoint_record_kernel(const
     // 3. reverse walk over the segment
     {
       int k = s1 - 1;
-      float2 v0 = k >= s0 ? __ldcs(rec + k) : make_float2(0.f, 0.f);
-      float2 v1 = k - 1 >= s0 ? __ldcs(rec + k - 1) : make_float2(0.f, 0.f);
+      float2 v0 = k >= s0 ? __ldg(rec + k) : make_float2(0.f, 0.f);
+      float2 v1 = k - 1 >= s0 ? __ldg(rec + k - 1) : make_float2(0.f, 0.f);
       for (; k - 1 >= s0; k -= 2) {
-        const float2 u0 = k - 2 >= s0 ? __ldcs(rec + k - 2) : make_float2(0.f, 0.f);  // next pair, in flight
-        const float2 u1 = k - 3 >= s0 ? __ldcs(rec + k - 3) : make_float2(0.f, 0.f);
+        const float2 u0 = k - 2 >= s0 ? __ldg(rec + k - 2) : make_float2(0.f, 0.f);  // next pair, in flight
+        const float2 u1 = k - 3 >= s0 ? __ldg(rec + k - 3) : make_float2(0.f, 0.f);
         record_reverse_step<BLEND>(tf, step, v0.x, v0.y, adj_acc, acc_tf);
         record_reverse_step<BLEND>(tf, step, v1.x, v1.y, adj_acc, acc_tf);
         v0 = u0;
