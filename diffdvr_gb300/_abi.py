@@ -94,6 +94,9 @@ class DvrAdjointOutputs(ctypes.Structure):
         ("adj_camera_ray_start", DvrTensor),
         ("adj_camera_ray_dir", DvrTensor),
         ("adj_tf", DvrTensor),
+        ("has_viewport_derivatives", ctypes.c_int32),
+        ("pad2_", ctypes.c_int32),
+        ("adj_viewport", DvrTensor),
     ]
 
 
@@ -139,7 +142,7 @@ def load() -> ctypes.CDLL:
             fn = getattr(lib, name)
             fn.restype = res
             fn.argtypes = args
-        if lib.dvr_abi_version() != 2:
+        if lib.dvr_abi_version() != 3:
             raise RuntimeError("libdvr_gb300.so has an unexpected ABI version")
         _LIB = lib
     return _LIB

@@ -84,6 +84,38 @@ __device__ __forceinline__ void compute_ray(const RenderParams& p, int x, int y,
   }
 }
 
+// Adjoint of the reference-frame ray generation (compute_ray, camera mode 2;
+// renderer/camera_impl.cu:17-36): adds the viewport gradient of one ray with
+// start/direction adjoints (adj_start, adj_dir) to g[0..8] (rows eye, right,
+// up).  start = eye; dir = d / |d|, d = front + ax right + ay up,
+// front = up x right.
+__device__ __forceinline__ void viewport_adjoint(const RenderParams& p, int x, int y, int b, f3 adj_start, f3 adj_dir,
+                                                 float* g) {
+  const float fovx = p.fov_y * float(p.W) / float(p.H);
+  const float tan_x = tanf(fovx / 2), tan_y = tanf(p.fov_y / 2);
+  const f3 right = mk3(mat_at(p.cam, b, 1, 0), mat_at(p.cam, b, 1, 1), mat_at(p.cam, b, 1, 2));
+  const f3 up = mk3(mat_at(p.cam, b, 2, 0), mat_at(p.cam, b, 2, 1), mat_at(p.cam, b, 2, 2));
+  const f3 front = cross3(up, right);
+  const float ax = (2 * (x + 0.5f) / float(p.W) - 1) * tan_x, ay = (2 * (y + 0.5f) / float(p.H) - 1) * tan_y;
+  const f3 d = mk3(front.x + ax * right.x + ay * up.x, front.y + ax * right.y + ay * up.y,
+                   front.z + ax * right.z + ay * up.z);
+  const float inv = 1.f / sqrtf(dot3(d, d));
+  const f3 dir = mk3(d.x * inv, d.y * inv, d.z * inv);
+  const float dd = dot3(dir, adj_dir);
+  const f3 ad = mk3((adj_dir.x - dir.x * dd) * inv, (adj_dir.y - dir.y * dd) * inv, (adj_dir.z - dir.z * dd) * inv);
+  const f3 af_x_up = cross3(ad, up);     // adjoint of right through front = up x right
+  const f3 right_x_af = cross3(right, ad);  // adjoint of up through front
+  atomicAdd(g + 0, adj_start.x);
+  atomicAdd(g + 1, adj_start.y);
+  atomicAdd(g + 2, adj_start.z);
+  atomicAdd(g + 3, ax * ad.x + af_x_up.x);
+  atomicAdd(g + 4, ax * ad.y + af_x_up.y);
+  atomicAdd(g + 5, ax * ad.z + af_x_up.z);
+  atomicAdd(g + 6, ay * ad.x + right_x_af.x);
+  atomicAdd(g + 7, ay * ad.y + right_x_af.y);
+  atomicAdd(g + 8, ay * ad.z + right_x_af.z);
+}
+
 // renderer/renderer_utils.cuh:60-74 (ternary min/max: NaN handling as the reference)
 __device__ __forceinline__ void ray_box(f3 s, f3 d, f3 bmin, f3 bsize, float& tmin, float& tmax) {
   const float ix = 1.0f / d.x, iy = 1.0f / d.y, iz = 1.0f / d.z;

@@ -200,8 +200,8 @@ static cudaError_t fast_adjoint_go(const RenderParams& p, const AdjointParams& a
   constexpr int C = TfChannels<TF>::C;
   const bool tfgrad = a.has_tf != 0, volgrad = a.has_volume != 0;
   const int copies = p.tf.s[0] == 0 ? 1 : p.B;
-  const size_t smem = size_t(AdjointSmem(TF, p.R, C, kFastThreads, tfgrad, p.ckpt.p ? p.ckpt_interval : 0, copies)
-                                 .total) * sizeof(float);
+  const size_t smem = (size_t(AdjointSmem(TF, p.R, C, kFastThreads, tfgrad, p.ckpt.p ? p.ckpt_interval : 0, copies)
+                                  .total) + (a.has_viewport ? size_t(p.B) * 9 : 0)) * sizeof(float);
   if (smem > size_t(li.max_smem_optin)) return cudaErrorInvalidConfiguration;
   cudaError_t err;
   int* counter = acquire_counter(li.device, s, err);
@@ -225,7 +225,7 @@ static cudaError_t fast_adjoint_go(const RenderParams& p, const AdjointParams& a
   };
   if constexpr (TF == kTfTexture) {
     // TF gradient only, from the sample-density record
-    if (tfgrad && !volgrad && !a.has_camera && !a.has_stepsize && p.dens && p.ckpt.p) {
+    if (tfgrad && !volgrad && !a.has_camera && !a.has_stepsize && !a.has_viewport && p.dens && p.ckpt.p) {
       const bool per_batch = a.adj_tf.s[0] != 0;
       (void)per_batch;
       const size_t rsmem = size_t(record_smem_floats(p.R, C, copies)) * sizeof(float);
@@ -261,8 +261,8 @@ static cudaError_t fast_adjoint_into_go(const RenderParams& p, const AdjointPara
   constexpr int C = TfChannels<TF>::C;
   const bool tfgrad = a.has_tf != 0, volgrad = a.has_volume != 0;
   const int copies = p.tf.s[0] == 0 ? 1 : p.B;
-  const size_t smem = size_t(AdjointSmem(TF, p.R, C, kFastThreads, tfgrad, p.ckpt.p ? p.ckpt_interval : 0, copies)
-                                 .total) * sizeof(float);
+  const size_t smem = (size_t(AdjointSmem(TF, p.R, C, kFastThreads, tfgrad, p.ckpt.p ? p.ckpt_interval : 0, copies)
+                                  .total) + (a.has_viewport ? size_t(p.B) * 9 : 0)) * sizeof(float);
   if (smem > size_t(li.max_smem_optin)) return cudaErrorInvalidConfiguration;
   const size_t slice = size_t(p.R) * C * sizeof(float);
   const int64_t fit = tfgrad ? int64_t(sc.tf_bytes / slice) : int64_t(1) << 30;

@@ -495,7 +495,22 @@ AdjointParams check_adjoint(const DvrTensor& adj_color, const DvrAdjointOutputs&
     check_dtype(t, "adj_tf", DVR_FLOAT32);
     a.adj_tf = out_view(t, true);
   }
-  if (!a.has_volume && !a.has_stepsize && !a.has_camera && !a.has_tf)
+  a.has_viewport = o.has_viewport_derivatives != 0;
+  if (a.has_viewport) {
+    const DvrTensor& t = o.adj_viewport;
+    check_dim(t, "adj_viewport", 3);
+    check_device(t, "adj_viewport", c.device);
+    check_batch(t, "adj_viewport", p.B);
+    check_size(t, "adj_viewport", 1, 3);
+    check_size(t, "adj_viewport", 2, 3);
+    check_dtype(t, "adj_viewport", DVR_FLOAT32);
+    if (p.camera_mode != DVR_CAMERA_REFERENCE_FRAME)
+      fail(DVR_E_INVALID_ARGUMENT, "viewport derivatives require cameraMode == ReferenceFrame");
+    if (p.B > kMaxViewportBatch)
+      fail(DVR_E_UNSUPPORTED, "viewport derivatives support batches of at most 256 views");
+    a.adj_viewport = out_view(t, true);
+  }
+  if (!a.has_volume && !a.has_stepsize && !a.has_camera && !a.has_tf && !a.has_viewport)
     fail(DVR_E_NO_GRADIENT, "At least one adjoint variable must be activated!");
   return a;
 }
@@ -511,8 +526,10 @@ void after_launch(cudaError_t e, cudaStream_t s, const char* what) {
   }
 }
 
-bool use_plain(const Checked& c) {
+bool use_plain(const Checked& c, const AdjointParams* a = nullptr) {
   if (g_family.load() == DVR_KERNELS_PLAIN) {
+    if (a && a->has_viewport)
+      fail(DVR_E_UNSUPPORTED, "viewport derivatives are computed by the optimized kernel family only");
     if (c.p.vol_storage != DVR_FLOAT32 || c.p.tf_storage != DVR_FLOAT32)
       fail(DVR_E_UNSUPPORTED, "the plain kernel family renders float32 volumes and TFs only");
     if (c.p.dens)
@@ -642,7 +659,7 @@ extern "C" int dvr_render_adjoint(const DvrRendererInputs* inputs, const DvrRend
     const AdjointParams a = check_adjoint(*adj_color, *adj_outputs, c);
     DeviceGuard guard(c.device);
     const LaunchInfo li = launch_info(c.device);
-    const bool plain = use_plain(c);
+    const bool plain = use_plain(c, &a);
     cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
     after_launch(dispatch_adjoint(c, a, plain, li, s), s, "adjoint");
   });
@@ -688,6 +705,8 @@ extern "C" int dvr_render_adjoint_batched(const DvrRendererInputs* inputs,
       check_outputs(outputs_from_forward[i], cs[i], false);
       if (cs[i].p.dens) fail(DVR_E_UNSUPPORTED, "the batched entry points do not record sample_density");
       as[i] = check_adjoint(adj_colors[i], adj_outputs[i], cs[i]);
+      if (as[i].has_viewport)
+        fail(DVR_E_UNSUPPORTED, "the batched entry points do not compute viewport derivatives");
       if (i > 0 && (cs[i].filter != cs[0].filter || cs[i].tf_mode != cs[0].tf_mode || cs[i].blend != cs[0].blend ||
                     cs[i].p.vol_storage != cs[0].p.vol_storage || cs[i].p.tf_storage != cs[0].p.tf_storage ||
                     cs[i].device != cs[0].device || as[i].has_volume != as[0].has_volume ||

@@ -7,6 +7,10 @@
 
 namespace dvr {
 
+// Viewport derivatives are summed per batch entry in shared memory: at most
+// this many entries (9 floats each).
+constexpr int kMaxViewportBatch = 256;
+
 struct LaunchInfo {
   int num_sms;
   int max_smem_optin;  // cudaDevAttrMaxSharedMemoryPerBlockOptin

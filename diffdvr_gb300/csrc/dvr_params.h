@@ -65,6 +65,8 @@ struct AdjointParams {
   OutView adj_step;             // [b][y][x]
   OutView adj_start, adj_dir;   // [b][y][x][i]
   OutView adj_tf;               // [b][r][c]
+  int32_t has_viewport, pad2_;
+  OutView adj_viewport;         // [b][row][c], reference-frame camera (broadcast strides allowed)
 };
 
 }  // namespace dvr

@@ -92,13 +92,19 @@ __global__ void __launch_bounds__(kFastThreads) fast_adjoint_persistent_kernel(c
   }
   __syncthreads();
 
+  // viewport gradient of the block, per batch entry, after the layout
+  float* s_vp = smem + L.total;
+  if (a.has_viewport)
+    for (int e = threadIdx.x; e < p.B * 9; e += blockDim.x) s_vp[e] = 0.f;
+  __syncthreads();
+
   const bool tf_per_batch = TFGRAD && a.adj_tf.s[0] != 0;
   float* s_grad_warp = smem + L.warp + (threadIdx.x >> 5) * p.R * C;
   TfGradAccum<TF, TFGRAD> tacc;
   tacc.bind(smem + L.lane, int(blockDim.x), int(threadIdx.x), L.slots, p.R);
   if (!tf_per_batch) tacc.set_evict_target(block_slice, C, 1);
   int cur_b = -1;  // batch entry of the accumulated TF gradient (per-batch outputs)
-  const bool need_pos = a.has_camera || a.has_stepsize;
+  const bool need_pos = a.has_camera || a.has_stepsize || a.has_viewport;
   float* seg_d = smem + L.seg + threadIdx.x;  // [offset][thread]
   float* seg_a = smem + L.seg + K * blockDim.x + threadIdx.x;
 
@@ -122,6 +128,7 @@ __global__ void __launch_bounds__(kFastThreads) fast_adjoint_persistent_kernel(c
   const float2* drow = nullptr;  // the ray's recorded (density, incoming opacity) pairs, if any
 
   auto write_ray_grads = [&]() {
+    if (a.has_viewport) viewport_adjoint(p, x, y, b, adj_start, adj_dir, s_vp + b * 9);
     if (a.has_stepsize) {
       float* ps = static_cast<float*>(a.adj_step.p) + b * a.adj_step.s[0] + y * a.adj_step.s[1] + x * a.adj_step.s[2];
       if (a.stepsize_broadcast) atomicAdd(ps, adj_step);
@@ -275,6 +282,18 @@ __global__ void __launch_bounds__(kFastThreads) fast_adjoint_persistent_kernel(c
       __syncthreads();
       reduce_tf_grad<TF>(L, smem, p.R, static_cast<float*>(a.adj_tf.p), 0, a.adj_tf.s[1], a.adj_tf.s[2], 0,
                          block_slice);
+    }
+  }
+  // viewport gradient of the block
+  if (a.has_viewport) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < p.B * 9; e += blockDim.x) {
+      const float v = s_vp[e];
+      const int bb = e / 9, r = (e - bb * 9) / 3, c = e - bb * 9 - r * 3;
+      if (v != 0.f)
+        atomicAdd(static_cast<float*>(a.adj_viewport.p) + bb * a.adj_viewport.s[0] + r * a.adj_viewport.s[1] +
+                      c * a.adj_viewport.s[2],
+                  v);
     }
   }
 }

@@ -184,6 +184,10 @@ class AdjointOutputs:
         self.has_tf_derivatives = False
         self.tf_delayed_accumulation = False
         self.adj_tf: Optional[torch.Tensor] = None
+        # extension: gradient of a CameraReferenceFrame viewport ((B) 3 3), the
+        # rays being generated inside the kernel
+        self.has_viewport_derivatives = False
+        self.adj_viewport: Optional[torch.Tensor] = None
 
 
 # --------------------------------------------------------------------- marshalling
@@ -292,6 +296,8 @@ def _adjoint_outputs(a: AdjointOutputs) -> _abi.DvrAdjointOutputs:
                                      "adj_camera_ray_start")
     c.adj_camera_ray_dir = _tensor(a.adj_camera_ray_dir if a.has_camera_derivatives else None, "adj_camera_ray_dir")
     c.adj_tf = _tensor(a.adj_tf if a.has_tf_derivatives else None, "adj_tf")
+    c.has_viewport_derivatives = int(bool(getattr(a, "has_viewport_derivatives", False)))
+    c.adj_viewport = _tensor(a.adj_viewport if c.has_viewport_derivatives else None, "adj_viewport")
     return c
 
 

@@ -93,7 +93,8 @@ class _RendererFunction(torch.autograd.Function):
         ctx.optimize = (optimize_camera, optimize_tf, optimize_volume)
         ctx.tf_delayed_accumulation = tf_delayed_accumulation
         ctx.profiling = profiling
-        assert _implies(optimize_camera, inputs.camera_mode == pyrenderer.CameraMode.RayStartDir)
+        assert _implies(optimize_camera, inputs.camera_mode in (pyrenderer.CameraMode.RayStartDir,
+                                                                pyrenderer.CameraMode.ReferenceFrame))
         if inputs.camera_mode == pyrenderer.CameraMode.RayStartDir:
             inputs.camera = pyrenderer.CameraPerPixelRays(camera_ray_start, camera_ray_dir)
         else:
@@ -138,9 +139,14 @@ class _RendererFunction(torch.autograd.Function):
             inputs.camera = pyrenderer.CameraReferenceFrame(camera_matrix, ctx.fov_y_radians)
         inputs.tf = tf
         inputs.volume = volume
-        g_start = g_dir = g_tf = g_volume = None
+        g_cam = g_start = g_dir = g_tf = g_volume = None
         adj = pyrenderer.AdjointOutputs()
-        if optimize_camera:
+        if optimize_camera and inputs.camera_mode == pyrenderer.CameraMode.ReferenceFrame:
+            # rays generated in the kernel: the viewport gradient directly
+            g_cam = torch.zeros(camera_matrix.shape, dtype=torch.float32, device=camera_matrix.device)
+            adj.has_viewport_derivatives = True
+            adj.adj_viewport = g_cam
+        elif optimize_camera:
             g_start = torch.zeros_like(ray_start)
             g_dir = torch.zeros_like(ray_dir)
             adj.has_camera_derivatives = True
@@ -164,7 +170,9 @@ class _RendererFunction(torch.autograd.Function):
             g_tf = g_tf.to(tf.dtype)
         if g_volume is not None and volume.dtype != torch.float32:
             g_volume = g_volume.to(volume.dtype)
-        return None, g_start, g_dir, g_tf, g_volume, None, None, None, None, None, None, None, None, None
+        if g_cam is not None and camera_matrix.dtype != torch.float32:
+            g_cam = g_cam.to(camera_matrix.dtype)
+        return g_cam, g_start, g_dir, g_tf, g_volume, None, None, None, None, None, None, None, None, None
 
 
 class Renderer(nn.Module):
@@ -173,7 +181,7 @@ class Renderer(nn.Module):
     def __init__(self, settings: Optional[pyrenderer.RendererInputs] = None, optimize_camera=False,
                  optimize_tf=False, optimize_volume=False, gradient_method="adjoint",
                  forward_delayed_gradients=False, tf_delayed_accumulation=True, checkpoint_interval: int = 16,
-                 sample_record="auto"):
+                 sample_record="auto", fused_camera: bool = True):
         super().__init__()
         self._settings = settings if settings is not None else pyrenderer.RendererInputs()
         self._optimize_camera = optimize_camera
@@ -187,6 +195,7 @@ class Renderer(nn.Module):
         self._tf_delayed_accumulation = tf_delayed_accumulation
         self._checkpoint_interval = int(checkpoint_interval)
         self._sample_record = sample_record
+        self._fused_camera = bool(fused_camera)
         self._renderer_function = _RendererFunction.apply
 
     def get_settings(self):
@@ -213,7 +222,7 @@ class Renderer(nn.Module):
         inputs = self._settings.clone()
         camera_matrix = ray_start = ray_dir = None
         if camera is not None:
-            if self._optimize_camera:
+            if self._optimize_camera and not self._fused_camera:
                 ray_start, ray_dir = Camera.generate_rays(camera, fov_y_radians, self._settings.screen_size.x,
                                                           self._settings.screen_size.y)
                 inputs.camera_mode = pyrenderer.CameraMode.RayStartDir

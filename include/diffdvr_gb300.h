@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define DVR_ABI_VERSION 2
+#define DVR_ABI_VERSION 3
 
 /* ---- status codes ---- */
 #define DVR_OK 0
@@ -157,6 +157,16 @@ typedef struct DvrAdjointOutputs {
   DvrTensor adj_camera_ray_start;/* (B) H W 3 */
   DvrTensor adj_camera_ray_dir;  /* (B) H W 3 */
   DvrTensor adj_tf;              /* (B) R C */
+  /* Gradient of the reference-frame camera's viewport (rows eye, right, up),
+   * (B) 3 3, accumulated: the rays are generated from the viewport inside the
+   * kernel (renderer/camera_impl.cu:17-36) and each ray's start/direction
+   * adjoint is carried back through that generation.  Needs cameraMode ==
+   * ReferenceFrame and the optimized single-instance entry points; the
+   * reference gets this gradient by materialising per-pixel rays and
+   * differentiating their generation separately. */
+  int32_t has_viewport_derivatives;
+  int32_t pad2_;
+  DvrTensor adj_viewport;
 } DvrAdjointOutputs;
 
 /* Forward rendering without gradients.

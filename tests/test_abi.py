@@ -26,7 +26,7 @@ def test_library_exports_every_header_symbol(dvr_lib):
     for n in names:
         assert hasattr(dvr_lib, n), n
     assert set(names) == set(_abi.SIGNATURES)
-    assert dvr_lib.dvr_abi_version() == 2
+    assert dvr_lib.dvr_abi_version() == 3
 
 
 def _fake(shape, dtype=_abi.DVR_FLOAT32, cuda=True, ptr=0x100000):
@@ -144,6 +144,26 @@ def test_adjoint_output_shape_checks(dvr_lib):
     code = dvr_lib.dvr_render_adjoint(ctypes.byref(i), ctypes.byref(o), ctypes.byref(adj), ctypes.byref(a), None)
     assert code == _abi.DVR_E_INVALID_ARGUMENT
     assert "adj_tf must have 8 entries at dimension 1" in dvr_lib.dvr_last_error().decode()
+
+
+@pytest.mark.parametrize("frame,shape,expect", [
+    (False, (1, 3, 3), "viewport derivatives require cameraMode == ReferenceFrame"),
+    (True, (1, 3, 4), "adj_viewport must have 3 entries at dimension 2"),
+])
+def test_viewport_derivative_checks(dvr_lib, frame, shape, expect):
+    i, o = _inputs(), _outputs()
+    if frame:
+        i.camera_mode = 2
+        i.camera_kind = _abi.DVR_CAMERA_REFERENCE_FRAME_KIND
+        i.camera_matrix = _fake((1, 3, 3))
+        i.camera_fov_y_radians = 0.7
+    a = _abi.DvrAdjointOutputs()
+    a.has_viewport_derivatives = 1
+    a.adj_viewport = _fake(shape)
+    adj = _fake((1, 7, 8, 4))
+    code = dvr_lib.dvr_render_adjoint(ctypes.byref(i), ctypes.byref(o), ctypes.byref(adj), ctypes.byref(a), None)
+    assert code == _abi.DVR_E_INVALID_ARGUMENT
+    assert expect in dvr_lib.dvr_last_error().decode()
 
 
 def test_checkpoint_slots(dvr_lib):
