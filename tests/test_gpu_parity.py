@@ -533,6 +533,38 @@ def test_fused_viewport_gradient_matches_generated_rays(views, viewports, cuda_d
     assert rel_l2(grads[True], grads[False]) <= 1e-3, rel_l2(grads[True], grads[False])
 
 
+def test_cvol_volume_renders_in_file_order(tmp_path, cuda_device):
+    """A Marschner-Lobb volume written to and read from a .cvol file keeps the
+    file's x-fastest layout (strides 1, X, X*Y); rendering it gives exactly
+    what its contiguous [x][y][z] copy gives, forward and TF gradient."""
+    from diffdvr_gb300 import pyrenderer as pr, volume_io as vio
+    path = str(tmp_path / "ml.cvol")
+    vio.save_cvol(path, vio.marschner_lobb(41), dtype="float32")
+    vol, world = vio.load_cvol(path)
+    case = make_case(97, tf_mode=1, shape=(41, 41, 41), W=32, H=24, B=2, opacity=0.5)
+    results = []
+    for t in (torch.from_numpy(vol).cuda(), torch.from_numpy(np.ascontiguousarray(vol)).cuda()):
+        assert t.is_contiguous() == (len(results) == 1)
+        case.volume = vol
+        inp = case.inputs("cuda")
+        inp.volume = t
+        B = case.batch()
+        out = pr.RendererOutputs(torch.empty(B, case.height, case.width, 4, device="cuda"),
+                                 torch.empty(B, case.height, case.width, dtype=torch.int32, device="cuda"),
+                                 torch.empty(B, case.height, case.width, pr.Renderer.checkpoint_slots(inp), device="cuda"),
+                                 16)
+        pr.Renderer.render_forward(inp, out)
+        a = pr.AdjointOutputs()
+        a.has_tf_derivatives = True
+        a.adj_tf = torch.zeros(case.tf.shape, device="cuda")
+        pr.Renderer.render_adjoint(inp, out, torch.ones_like(out.color) * 1e-2, a)
+        torch.cuda.synchronize()
+        results.append((out.color.clone(), out.terminationIndex.clone(), a.adj_tf.clone()))
+    (c0, t0, g0), (c1, t1, g1) = results
+    assert torch.equal(t0, t1) and torch.equal(c0, c1)
+    assert rel_l2(g0.cpu().numpy(), g1.cpu().numpy()) <= 1e-5
+
+
 def test_invalid_inputs_raise(cuda_device):
     from diffdvr_gb300 import pyrenderer as pr
     case = make_case(99)
