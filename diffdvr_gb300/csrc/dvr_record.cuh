@@ -52,25 +52,28 @@ struct TexelPairAtomic {
     put(i + 1, a1);
     i = -1;
   }
-  // adds k0 * v to texel i0 and k1 * v to texel i1 (i1 = i0 + 1, or i0 at the clamped ends)
+  __device__ __forceinline__ void red4(float* e, f4 v) const {
+    atomicAdd(e, v.x);
+    atomicAdd(e + sc, v.y);
+    atomicAdd(e + 2 * sc, v.z);
+    atomicAdd(e + 3 * sc, v.w);
+  }
+  // adds k0 * v to texel i0 and k1 * v to texel i1 (i1 = i0 + 1, or i0 at the
+  // clamped ends).  Branch-light: about one lane in ten moves to another texel
+  // per sample, so nearly every warp step has a mover; the moves are
+  // predicates and selects rather than nested branches.
   __device__ __forceinline__ void add(int i0, int i1, f4 v, float k0, float k1) {
-    if (i0 != i) {
-      const f4 z = mk4(0, 0, 0, 0);
-      if (i >= 0 && i0 == i + 1) {
-        put(i, a0);
-        a0 = a1;
-        a1 = z;
-      } else if (i >= 0 && i0 == i - 1) {
-        put(i + 1, a1);
-        a1 = a0;
-        a0 = z;
-      } else {
-        flush();
-        a0 = z;
-        a1 = z;
-      }
-      i = i0;
-    }
+    const bool moved = i0 != i, held = i >= 0;
+    const bool up = moved && held && i0 == i + 1, down = moved && held && i0 == i - 1;
+    const bool jump = moved && held && !up && !down;
+    if (up || jump) red4(dst + i * sr, a0);
+    if ((down || jump) && i + 1 < R) red4(dst + (i + 1) * sr, a1);
+    const f4 z = mk4(0, 0, 0, 0);
+    const f4 n0 = up ? a1 : (moved ? z : a0);
+    const f4 n1 = down ? a0 : (moved ? z : a1);
+    a0 = n0;
+    a1 = n1;
+    i = i0;
     const bool same = i1 == i0;
     const float q0 = same ? k0 + k1 : k0, q1 = same ? 0.f : k1;
     a0 = mk4(fmaf(v.x, q0, a0.x), fmaf(v.y, q0, a0.y), fmaf(v.z, q0, a0.z), fmaf(v.w, q0, a0.w));
