@@ -100,6 +100,18 @@ class DvrAdjointOutputs(ctypes.Structure):
     ]
 
 
+class DvrForwardDifferencesSettings(ctypes.Structure):
+    _fields_ = [
+        ("D", ctypes.c_int32),
+        ("d_stepsize", ctypes.c_int32),
+        ("d_ray_start", ctypes.c_int32 * 3),
+        ("d_ray_dir", ctypes.c_int32 * 3),
+        ("has_tf_derivatives", ctypes.c_int32),
+        ("pad_", ctypes.c_int32),
+        ("d_tf", DvrTensor),
+    ]
+
+
 # every exported symbol of the header, with its signature
 _P = ctypes.POINTER
 SIGNATURES = {
@@ -112,6 +124,11 @@ SIGNATURES = {
                                                   ctypes.c_void_p]),
     "dvr_render_adjoint_batched": (ctypes.c_int, [_P(DvrRendererInputs), _P(DvrRendererOutputs), _P(DvrTensor),
                                                   _P(DvrAdjointOutputs), ctypes.c_int32, ctypes.c_void_p]),
+    "dvr_render_forward_gradients": (ctypes.c_int, [_P(DvrRendererInputs), _P(DvrForwardDifferencesSettings),
+                                                    _P(DvrRendererOutputs), _P(DvrTensor), ctypes.c_void_p]),
+    "dvr_forward_variables_to_gradients": (ctypes.c_int, [_P(DvrTensor), _P(DvrTensor),
+                                                          _P(DvrForwardDifferencesSettings), _P(DvrAdjointOutputs),
+                                                          ctypes.c_void_p]),
     "dvr_checkpoint_slots": (ctypes.c_int64, [ctypes.c_double, ctypes.c_double, ctypes.c_int32]),
     "dvr_last_error": (ctypes.c_char_p, []),
     "dvr_set_kernel_family": (ctypes.c_int, [ctypes.c_int32]),
@@ -122,6 +139,7 @@ SIGNATURES = {
 }
 
 _LIB = None
+ABI_VERSION = 4
 
 
 def library_path() -> str:
@@ -142,7 +160,7 @@ def load() -> ctypes.CDLL:
             fn = getattr(lib, name)
             fn.restype = res
             fn.argtypes = args
-        if lib.dvr_abi_version() != 3:
+        if lib.dvr_abi_version() != ABI_VERSION:
             raise RuntimeError("libdvr_gb300.so has an unexpected ABI version")
         _LIB = lib
     return _LIB

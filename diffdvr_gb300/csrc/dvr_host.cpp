@@ -599,6 +599,43 @@ cudaError_t dispatch_adjoint_into(const Checked& c, const AdjointParams& a, cons
   }
 }
 
+// ---- forward-mode differentiation ----
+// Derivative indices of DvrForwardDifferencesSettings (host values) checked
+// against D; -1 (or any negative) = not traced.
+int checked_index(int32_t i, int D, const char* name) {
+  if (i < 0) return -1;
+  if (i >= D) {
+    std::ostringstream os;
+    os << name << " = " << i << " is not a derivative index: the number of derivatives D is " << D;
+    fail(DVR_E_INVALID_ARGUMENT, os.str());
+  }
+  return i;
+}
+
+void set_d_tf(const DvrForwardDifferencesSettings& fs, int device, const int32_t*& ptr, int64_t* strides) {
+  ptr = nullptr;
+  strides[0] = strides[1] = strides[2] = 0;
+  if (!fs.has_tf_derivatives) return;
+  const DvrTensor& t = fs.d_tf;
+  if (t.ndim < 0 || t.data == nullptr)
+    fail(DVR_E_INVALID_ARGUMENT, "d_tf not defined, hence hasTfDerivatives must be false but was set to true");
+  check_dim(t, "d_tf", 3);
+  check_device(t, "d_tf", device);
+  check_dtype(t, "d_tf", DVR_INT32);
+  ptr = static_cast<const int32_t*>(t.data);
+  for (int i = 0; i < 3; ++i) strides[i] = t.sizes[i] == 1 ? 0 : t.strides[i];
+}
+
+cudaError_t dispatch_forward_gradients(const Checked& c, const FwdGradParams& g, const LaunchInfo& li,
+                                       cudaStream_t s) {
+  switch (c.tf_mode) {
+    case DVR_TF_IDENTITY: return launch_forward_gradients<0>(c.p, g, c.filter, c.blend, li, s);
+    case DVR_TF_TEXTURE: return launch_forward_gradients<1>(c.p, g, c.filter, c.blend, li, s);
+    case DVR_TF_LINEAR: return launch_forward_gradients<2>(c.p, g, c.filter, c.blend, li, s);
+    default: return launch_forward_gradients<3>(c.p, g, c.filter, c.blend, li, s);
+  }
+}
+
 }  // namespace
 
 int render_adjoint_into(const DvrRendererInputs* inputs, const DvrRendererOutputs* outputs_from_forward,
@@ -722,6 +759,169 @@ extern "C" int dvr_render_adjoint_batched(const DvrRendererInputs* inputs,
     after_launch(launch_batched_adjoint(ps.data(), as.data(), n, cs[0].filter, cs[0].tf_mode, cs[0].blend,
                                         cs[0].device, li, s),
                  s, "batched adjoint");
+  });
+}
+
+// renderer::Renderer::renderForwardGradients (renderer/renderer.cpp:419-498)
+extern "C" int dvr_render_forward_gradients(const DvrRendererInputs* inputs,
+                                            const DvrForwardDifferencesSettings* settings,
+                                            const DvrRendererOutputs* outputs, const DvrTensor* gradients_out,
+                                            void* cuda_stream) {
+  return guarded([&] {
+    if (!inputs || !settings || !outputs || !gradients_out)
+      fail(DVR_E_INVALID_ARGUMENT, "arguments must not be NULL");
+    Checked c = check_inputs(*inputs);
+    const DvrForwardDifferencesSettings& fs = *settings;
+    if (fs.D <= 0) fail(DVR_E_INVALID_ARGUMENT, "number of derivatives must be positive");
+    FwdGradParams g{};
+    g.D = fs.D;
+    set_d_tf(fs, c.device, g.d_tf, g.dtf_s);
+    if (g.d_tf) {
+      check_size(fs.d_tf, "d_tf", 0, inputs->tf.sizes[0]);
+      check_size(fs.d_tf, "d_tf", 1, c.p.R);
+      check_size(fs.d_tf, "d_tf", 2, c.p.C);
+    }
+    g.has_tf = g.d_tf != nullptr;
+    g.d_step = checked_index(fs.d_stepsize, fs.D, "d_stepsize");
+    bool has_camera = false;
+    for (int i = 0; i < 3; ++i) {
+      g.d_start[i] = checked_index(fs.d_ray_start[i], fs.D, "d_rayStart");
+      g.d_dir[i] = checked_index(fs.d_ray_dir[i], fs.D, "d_rayDir");
+      has_camera |= g.d_start[i] >= 0 || g.d_dir[i] >= 0;
+    }
+    if (g.d_step < 0 && !has_camera && !g.has_tf) fail(DVR_E_INVALID_ARGUMENT, "at least one derivative must be activated");
+    DvrRendererOutputs plain_out = *outputs;  // color and termination index only
+    plain_out.checkpoints.ndim = -1;
+    plain_out.sample_density.ndim = -1;
+    plain_out.sample_offset.ndim = -1;
+    check_outputs(plain_out, c, true);
+    const DvrTensor& go = *gradients_out;
+    check_dim(go, "gradientsOut", 5);
+    check_device(go, "gradientsOut", c.device);
+    check_size(go, "gradientsOut", 0, c.p.B);
+    check_size(go, "gradientsOut", 1, c.p.H);
+    check_size(go, "gradientsOut", 2, c.p.W);
+    check_size(go, "gradientsOut", 3, fs.D);
+    check_size(go, "gradientsOut", 4, 4);
+    check_dtype(go, "gradientsOut", DVR_FLOAT32);
+    g.grad = static_cast<float*>(go.data);
+    for (int i = 0; i < 5; ++i) g.grad_s[i] = go.strides[i];
+    DeviceGuard guard(c.device);
+    const LaunchInfo li = launch_info(c.device);
+    const int copies = c.p.tf.s[0] == 0 ? 1 : c.p.B;
+    const size_t tf_bytes = size_t((int64_t(copies) * c.p.R * c.p.C + 3) / 4) * 16;
+    int pass = kFwdMaxPass;
+    while (pass > 32 && tf_bytes + size_t(kFwdThreads / 32) * pass * 16 > size_t(li.max_smem_optin)) pass /= 2;
+    if (tf_bytes + size_t(kFwdThreads / 32) * pass * 16 > size_t(li.max_smem_optin))
+      fail(DVR_E_UNSUPPORTED, "the TF (all batch entries) does not fit into shared memory for forward derivatives");
+    cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+    for (int d0 = 0; d0 < fs.D; d0 += pass) {
+      g.d0 = d0;
+      g.dn = std::min(pass, fs.D - d0);
+      after_launch(dispatch_forward_gradients(c, g, li, s), s, "forward gradients");
+    }
+  });
+}
+
+// renderer::Renderer::forwardVariablesToGradients (renderer/renderer.cpp:500-558)
+extern "C" int dvr_forward_variables_to_gradients(const DvrTensor* forward_variables, const DvrTensor* adj_color,
+                                                  const DvrForwardDifferencesSettings* settings,
+                                                  const DvrAdjointOutputs* adj_outputs, void* cuda_stream) {
+  return guarded([&] {
+    if (!forward_variables || !adj_color || !settings || !adj_outputs)
+      fail(DVR_E_INVALID_ARGUMENT, "arguments must not be NULL");
+    const DvrTensor& fv = *forward_variables;
+    check_dim(fv, "forwardVariables", 5);
+    if (fv.device_type != DVR_DEVICE_CUDA)
+      fail(DVR_E_INVALID_ARGUMENT, "forwardVariables is a CPU tensor: diffdvr_gb300 runs on CUDA devices only");
+    const int device = fv.device_index;
+    check_size(fv, "forwardVariables", 4, 4);
+    check_dtype(fv, "forwardVariables", DVR_FLOAT32);
+    FwdVarsParams v{};
+    v.B = int(fv.sizes[0]);
+    v.H = int(fv.sizes[1]);
+    v.W = int(fv.sizes[2]);
+    v.D = int(fv.sizes[3]);
+    v.fwd = static_cast<const float*>(fv.data);
+    for (int i = 0; i < 5; ++i) v.fwd_s[i] = fv.strides[i];
+    const DvrTensor& ac = *adj_color;
+    check_dim(ac, "gradientOutputColor", 4);
+    check_device(ac, "gradientOutputColor", device);
+    check_size(ac, "gradientOutputColor", 0, v.B);
+    check_size(ac, "gradientOutputColor", 1, v.H);
+    check_size(ac, "gradientOutputColor", 2, v.W);
+    check_size(ac, "gradientOutputColor", 3, 4);
+    check_dtype(ac, "gradientOutputColor", DVR_FLOAT32);
+    v.adj_color = static_cast<const float*>(ac.data);
+    for (int i = 0; i < 4; ++i) v.adj_s[i] = ac.strides[i];
+    const DvrForwardDifferencesSettings& fs = *settings;
+    set_d_tf(fs, device, v.d_tf, v.dtf_s);
+    v.d_step = checked_index(fs.d_stepsize, v.D, "d_stepsize");
+    for (int i = 0; i < 3; ++i) {
+      v.d_start[i] = checked_index(fs.d_ray_start[i], v.D, "d_rayStart");
+      v.d_dir[i] = checked_index(fs.d_ray_dir[i], v.D, "d_rayDir");
+    }
+    const DvrAdjointOutputs& o = *adj_outputs;
+    if (o.has_volume_derivatives)
+      fail(DVR_E_INVALID_ARGUMENT, "volume derivatives are not supported with forward variables");
+    if (o.has_viewport_derivatives)
+      fail(DVR_E_INVALID_ARGUMENT, "viewport derivatives are not supported with forward variables");
+    v.has_step = o.has_stepsize_derivatives != 0;
+    if (v.has_step) {
+      const DvrTensor& t = o.adj_stepsize;
+      check_dim(t, "adj_stepSize", 3);
+      check_device(t, "adj_stepSize", device);
+      check_batch(t, "adj_stepSize", v.B);
+      check_batch(t, "adj_stepSize", v.H, 1);
+      check_batch(t, "adj_stepSize", v.W, 2);
+      check_dtype(t, "adj_stepSize", DVR_FLOAT32);
+      v.adj_step = static_cast<float*>(t.data);
+      for (int i = 0; i < 3; ++i) v.step_s[i] = t.sizes[i] == 1 ? 0 : t.strides[i];
+      v.step_broadcast = v.B != t.sizes[0] || v.H != t.sizes[1] || v.W != t.sizes[2];
+    }
+    v.has_camera = o.has_camera_derivatives != 0;
+    if (v.has_camera) {
+      const DvrTensor* ts[2] = {&o.adj_camera_ray_start, &o.adj_camera_ray_dir};
+      const char* names[2] = {"adj_cameraRayStart", "adj_cameraRayDir"};
+      for (int k = 0; k < 2; ++k) {
+        const DvrTensor& t = *ts[k];
+        check_dim(t, names[k], 4);
+        check_device(t, names[k], device);
+        check_batch(t, names[k], v.B);
+        check_size(t, names[k], 1, v.H);
+        check_size(t, names[k], 2, v.W);
+        check_size(t, names[k], 3, 3);
+        check_dtype(t, names[k], DVR_FLOAT32);
+        v.camera_broadcast |= v.B != t.sizes[0];
+      }
+      v.adj_start = static_cast<float*>(o.adj_camera_ray_start.data);
+      v.adj_dir = static_cast<float*>(o.adj_camera_ray_dir.data);
+      for (int i = 0; i < 4; ++i) {
+        v.start_s[i] = (i == 0 && o.adj_camera_ray_start.sizes[0] == 1) ? 0 : o.adj_camera_ray_start.strides[i];
+        v.dir_s[i] = (i == 0 && o.adj_camera_ray_dir.sizes[0] == 1) ? 0 : o.adj_camera_ray_dir.strides[i];
+      }
+    }
+    v.has_tf = o.has_tf_derivatives != 0 && v.d_tf != nullptr;
+    if (o.has_tf_derivatives && !v.d_tf)
+      fail(DVR_E_INVALID_ARGUMENT, "TF derivatives need the TF derivative indices (d_tf, has_tf_derivatives)");
+    if (v.has_tf) {
+      const DvrTensor& t = o.adj_tf;
+      check_dim(t, "adj_tf", 3);
+      check_device(t, "adj_tf", device);
+      check_batch(t, "adj_tf", v.B);
+      check_size(t, "adj_tf", 1, fs.d_tf.sizes[1]);
+      check_size(t, "adj_tf", 2, fs.d_tf.sizes[2]);
+      check_dtype(t, "adj_tf", DVR_FLOAT32);
+      if (fs.d_tf.sizes[0] != 1 && fs.d_tf.sizes[0] != v.B)
+        fail(DVR_E_INVALID_ARGUMENT, "d_tf must have batch size 1 or B");
+      v.R = int(t.sizes[1]);
+      v.C = int(t.sizes[2]);
+      v.adj_tf = static_cast<float*>(t.data);
+      for (int i = 0; i < 3; ++i) v.tf_s[i] = t.sizes[i] == 1 ? 0 : t.strides[i];
+    }
+    DeviceGuard guard(device);
+    cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+    after_launch(launch_forward_variables_to_gradients(v, s), s, "forward variables to gradients");
   });
 }
 

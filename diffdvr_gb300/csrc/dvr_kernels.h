@@ -70,4 +70,15 @@ template <int TF>
 cudaError_t launch_fast_adjoint_into(const RenderParams& p, const AdjointParams& a, int filter, int blend,
                                      const LaunchInfo& li, const CallerScratch& sc, cudaStream_t s);
 
+// Forward-mode derivatives: blocks of kFwdThreads (one ray per warp at a
+// time), one launch per range of at most kFwdMaxPass derivative indices
+// (g.d0, g.dn); each warp holds its ray's dn x 4 Jacobian block in shared
+// memory.
+constexpr int kFwdThreads = 128;
+constexpr int kFwdMaxPass = 1024;
+template <int TF>
+cudaError_t launch_forward_gradients(const RenderParams& p, const FwdGradParams& g, int filter, int blend,
+                                     const LaunchInfo& li, cudaStream_t s);
+cudaError_t launch_forward_variables_to_gradients(const FwdVarsParams& v, cudaStream_t s);
+
 }  // namespace dvr

@@ -69,4 +69,44 @@ struct AdjointParams {
   OutView adj_viewport;         // [b][row][c], reference-frame camera (broadcast strides allowed)
 };
 
+// Forward-mode derivatives (renderForwardGradients): derivative indices
+// (-1 = not traced) and the forward-variable output of one launch, which
+// covers the indices [d0, d0 + dn) of D.
+struct FwdGradParams {
+  int32_t D, d0, dn;
+  int32_t d_step;
+  int32_t d_start[3], d_dir[3];
+  int32_t has_tf, pad_;
+  const int32_t* d_tf;          // [b][r][c] (broadcast strides); nullptr when !has_tf
+  int64_t dtf_s[3];
+  float* grad;                  // [b][y][x][d][c]
+  int64_t grad_s[5];
+};
+
+// forwardVariablesToGradients: forward variables and output adjoint in,
+// enabled gradients out.  Indices are -1 or in [0, D).
+constexpr int kFwdVarsSmemEntries = 8192;  // TF entries summed per block in shared memory
+struct FwdVarsParams {
+  int32_t B, H, W, D;
+  int32_t R, C;
+  int32_t has_step, has_camera, has_tf;
+  int32_t step_broadcast, camera_broadcast;
+  int32_t d_step, d_start[3], d_dir[3];
+  int32_t pad_;
+  const float* fwd;             // [b][y][x][d][c]
+  int64_t fwd_s[5];
+  const float* adj_color;       // [b][y][x][c]
+  int64_t adj_s[4];
+  float* adj_step;              // [b][y][x]
+  int64_t step_s[3];
+  float* adj_start;             // [b][y][x][i]
+  int64_t start_s[4];
+  float* adj_dir;
+  int64_t dir_s[4];
+  const int32_t* d_tf;          // [b][r][c]
+  int64_t dtf_s[3];
+  float* adj_tf;                // [b][r][c]
+  int64_t tf_s[3];
+};
+
 }  // namespace dvr

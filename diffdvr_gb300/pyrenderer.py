@@ -190,6 +190,21 @@ class AdjointOutputs:
         self.adj_viewport: Optional[torch.Tensor] = None
 
 
+class ForwardDifferencesSettings:
+    """Mirrors ForwardDifferencesSettingsHost (renderer/renderer.h:73-93,
+    bindings/bindings.cpp:423-436): the derivative index of each traced
+    variable, NOT_ENABLED (-1) for the others."""
+    NOT_ENABLED = -1
+
+    def __init__(self):
+        self.D = 0
+        self.d_stepsize = -1
+        self.d_rayStart = int3(-1, -1, -1)
+        self.d_rayDir = int3(-1, -1, -1)
+        self.d_tf: Optional[torch.Tensor] = None
+        self.has_tf_derivatives = False
+
+
 # --------------------------------------------------------------------- marshalling
 _DTYPES = {
     torch.float32: _abi.DVR_FLOAT32,
@@ -301,6 +316,19 @@ def _adjoint_outputs(a: AdjointOutputs) -> _abi.DvrAdjointOutputs:
     return c
 
 
+def _forward_settings(fs: ForwardDifferencesSettings) -> _abi.DvrForwardDifferencesSettings:
+    c = _abi.DvrForwardDifferencesSettings()
+    c.D = int(fs.D)
+    c.d_stepsize = int(fs.d_stepsize)
+    start, direction = list(fs.d_rayStart), list(fs.d_rayDir)
+    for i in range(3):
+        c.d_ray_start[i] = int(start[i])
+        c.d_ray_dir[i] = int(direction[i])
+    c.has_tf_derivatives = int(bool(fs.has_tf_derivatives))
+    c.d_tf = _tensor(fs.d_tf, "d_tf")
+    return c
+
+
 def _stream_of(t: Optional[torch.Tensor]) -> int:
     if t is not None and t.is_cuda:
         return torch.cuda.current_stream(t.device).cuda_stream
@@ -328,6 +356,30 @@ class Renderer:
         ca, cg = _tensor(adj_color, "adj_color"), _adjoint_outputs(adj_outputs)
         _abi.check(lib.dvr_render_adjoint(ctypes.byref(ci), ctypes.byref(co), ctypes.byref(ca), ctypes.byref(cg),
                                           _stream_of(inputs.volume)))
+
+    @staticmethod
+    def render_forward_gradients(inputs: RendererInputs, differences_settings: ForwardDifferencesSettings,
+                                 outputs: RendererOutputs, gradients_out: torch.Tensor) -> None:
+        """Forward rendering with forward-mode derivatives: fills outputs and
+        gradients_out (B*H*W*D*4, d color / d variable) for the variables
+        selected by differences_settings."""
+        lib = _abi.load()
+        ci, co = _inputs(inputs), _outputs(outputs)
+        cs, cg = _forward_settings(differences_settings), _tensor(gradients_out, "gradients_out")
+        _abi.check(lib.dvr_render_forward_gradients(ctypes.byref(ci), ctypes.byref(cs), ctypes.byref(co),
+                                                    ctypes.byref(cg), _stream_of(inputs.volume)))
+
+    @staticmethod
+    def forward_variables_to_gradients(forward_variables: torch.Tensor, adj_color: torch.Tensor,
+                                       differences_settings: ForwardDifferencesSettings,
+                                       adj_outputs: AdjointOutputs) -> None:
+        """Converts forward variables (B*H*W*D*4) to the gradients of the
+        step size, camera rays and TF for the colour adjoint adj_color."""
+        lib = _abi.load()
+        cf, ca = _tensor(forward_variables, "forward_variables"), _tensor(adj_color, "adj_color")
+        cs, cg = _forward_settings(differences_settings), _adjoint_outputs(adj_outputs)
+        _abi.check(lib.dvr_forward_variables_to_gradients(ctypes.byref(cf), ctypes.byref(ca), ctypes.byref(cs),
+                                                          ctypes.byref(cg), _stream_of(forward_variables)))
 
     @staticmethod
     def render_forward_batched(inputs: Sequence[RendererInputs], outputs: Sequence[RendererOutputs]) -> None:

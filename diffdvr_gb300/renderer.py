@@ -12,8 +12,15 @@ re-sampling the volume.  The record takes 8 bytes per sample; with
 quarter of the free device memory, else as large as that allows (rays that
 find it full are re-sampled).
 
-The reference's forward-mode differentiation (``gradient_method="forward"``)
-is not part of this renderer; requesting it raises ``NotImplementedError``.
+With ``gradient_method="forward"`` (pytests/diffdvr/renderer.py:63-80,
+:136-158, :218-253) the forward pass traces forward-mode derivatives of the
+colour with respect to the camera rays (6 variables) and every TF entry
+(``render_forward_gradients``), and ``backward`` contracts them with the
+colour gradient (``forward_variables_to_gradients``); with
+``forward_delayed_gradients=True`` the traced pass runs in ``backward``
+instead.  Camera optimisation in forward mode renders per-pixel rays
+generated by the differentiable ``Camera.generate_rays``.  Volume gradients
+need the adjoint method, as in the reference.
 """
 from __future__ import annotations
 
@@ -175,6 +182,101 @@ class _RendererFunction(torch.autograd.Function):
         return g_cam, g_start, g_dir, g_tf, g_volume, None, None, None, None, None, None, None, None, None
 
 
+def _forward_settings(optimize_camera, optimize_tf, tf) -> pyrenderer.ForwardDifferencesSettings:
+    """Derivative indices of the forward method: the six ray components
+    first, then the TF entries in row-major order
+    (pytests/diffdvr/renderer.py:63-80)."""
+    s = pyrenderer.ForwardDifferencesSettings()
+    D = 0
+    if optimize_camera:
+        s.d_rayStart = pyrenderer.int3(D, D + 1, D + 2)
+        s.d_rayDir = pyrenderer.int3(D + 3, D + 4, D + 5)
+        D += 6
+    if optimize_tf:
+        B, R, C = tf.shape
+        idx = torch.arange(D, D + R * C, dtype=torch.int32, device=tf.device).reshape(1, R, C)
+        s.d_tf = idx.expand(B, R, C).contiguous()
+        s.has_tf_derivatives = True
+        D += R * C
+    s.D = D
+    return s
+
+
+class _ForwardModeFunction(torch.autograd.Function):
+    """The forward method: forward-mode derivatives traced by the renderer,
+    contracted with the colour gradient in backward."""
+
+    @staticmethod
+    def forward(ctx, ray_start, ray_dir, tf, volume, inputs: pyrenderer.RendererInputs, optimize_camera,
+                optimize_tf, delayed, profiling: Optional[ProfileRenderer]):
+        ctx.inputs = inputs
+        ctx.optimize = (optimize_camera, optimize_tf)
+        ctx.delayed = delayed
+        ctx.profiling = profiling
+        if inputs.camera_mode == pyrenderer.CameraMode.RayStartDir:
+            inputs.camera = pyrenderer.CameraPerPixelRays(ray_start, ray_dir)
+        inputs.tf = tf
+        inputs.volume = volume
+        B = max([(1 if t is None else t.shape[0]) for t in (ray_start, ray_dir, tf, volume)])
+        W, H = inputs.screen_size.x, inputs.screen_size.y
+        color = torch.empty(B, H, W, 4, dtype=torch.float32, device=volume.device)
+        term = torch.empty(B, H, W, dtype=torch.int32, device=volume.device)
+        outputs = pyrenderer.RendererOutputs(color, term)
+        settings = _forward_settings(optimize_camera, optimize_tf, tf)
+        ctx.settings = settings
+        grads = None
+        with _Timer(profiling is not None) as timer:
+            if delayed or settings.D == 0:
+                pyrenderer.Renderer.render_forward(inputs, outputs)
+            else:
+                grads = torch.empty(B, H, W, settings.D, 4, dtype=torch.float32, device=volume.device)
+                pyrenderer.Renderer.render_forward_gradients(inputs, settings, outputs, grads)
+        if profiling is not None:
+            profiling.forward_ms += timer.elapsed_ms()
+            profiling.forward_bytes += _size_of(ray_start, ray_dir, tf, volume, color, term, grads)
+        ctx.save_for_backward(ray_start, ray_dir, tf, volume, grads)
+        return color
+
+    @staticmethod
+    def backward(ctx, grad_color):
+        ray_start, ray_dir, tf, volume, grads = ctx.saved_tensors
+        optimize_camera, optimize_tf = ctx.optimize
+        settings = ctx.settings
+        inputs = ctx.inputs
+        if settings.D == 0:
+            return None, None, None, None, None, None, None, None, None
+        with _Timer(ctx.profiling is not None) as timer:
+            if grads is None:
+                if inputs.camera_mode == pyrenderer.CameraMode.RayStartDir:
+                    inputs.camera = pyrenderer.CameraPerPixelRays(ray_start, ray_dir)
+                inputs.tf = tf
+                inputs.volume = volume
+                B, H, W = grad_color.shape[:3]
+                color = torch.empty(B, H, W, 4, dtype=torch.float32, device=volume.device)
+                term = torch.empty(B, H, W, dtype=torch.int32, device=volume.device)
+                grads = torch.empty(B, H, W, settings.D, 4, dtype=torch.float32, device=volume.device)
+                pyrenderer.Renderer.render_forward_gradients(inputs, settings, pyrenderer.RendererOutputs(color, term),
+                                                             grads)
+            adj = pyrenderer.AdjointOutputs()
+            g_start = g_dir = g_tf = None
+            if optimize_camera:
+                g_start = torch.zeros(ray_start.shape, dtype=torch.float32, device=ray_start.device)
+                g_dir = torch.zeros(ray_dir.shape, dtype=torch.float32, device=ray_dir.device)
+                adj.has_camera_derivatives = True
+                adj.adj_camera_ray_start = g_start
+                adj.adj_camera_ray_dir = g_dir
+            if optimize_tf:
+                g_tf = torch.zeros(tf.shape, dtype=torch.float32, device=tf.device)
+                adj.has_tf_derivatives = True
+                adj.adj_tf = g_tf
+            pyrenderer.Renderer.forward_variables_to_gradients(grads, grad_color.contiguous().float(), settings, adj)
+        if ctx.profiling is not None:
+            ctx.profiling.backward_ms += timer.elapsed_ms()
+        if g_tf is not None and tf.dtype != torch.float32:
+            g_tf = g_tf.to(tf.dtype)
+        return g_start, g_dir, g_tf, None, None, None, None, None, None
+
+
 class Renderer(nn.Module):
     """Mirrors diffdvr.Renderer (pytests/diffdvr/renderer.py:264-359)."""
 
@@ -189,9 +291,10 @@ class Renderer(nn.Module):
         self._optimize_volume = optimize_volume
         self._has_parameters_to_optimize = optimize_camera or optimize_tf or optimize_volume
         assert gradient_method in ["adjoint", "forward"]
-        if gradient_method != "adjoint":
-            raise NotImplementedError("forward-mode differentiation is not provided by diffdvr_gb300; "
-                                      "use gradient_method='adjoint'")
+        assert _implies(optimize_volume, gradient_method == "adjoint"), \
+            "if volume densities should be optimized, the gradient method must be 'adjoint'"
+        self._use_adjoint_method = gradient_method == "adjoint"
+        self._forward_delayed_gradients = bool(forward_delayed_gradients)
         self._tf_delayed_accumulation = tf_delayed_accumulation
         self._checkpoint_interval = int(checkpoint_interval)
         self._sample_record = sample_record
@@ -221,6 +324,8 @@ class Renderer(nn.Module):
         assert _implies(self._optimize_volume, volume is not None)
         inputs = self._settings.clone()
         camera_matrix = ray_start = ray_dir = None
+        if not self._use_adjoint_method:
+            return self._forward_method(inputs, camera, fov_y_radians, tf, volume, profiling)
         if camera is not None:
             if self._optimize_camera and not self._fused_camera:
                 ray_start, ray_dir = Camera.generate_rays(camera, fov_y_radians, self._settings.screen_size.x,
@@ -241,3 +346,20 @@ class Renderer(nn.Module):
                                        self._optimize_camera, self._optimize_tf, self._optimize_volume,
                                        self._tf_delayed_accumulation, self._checkpoint_interval,
                                        self._sample_record, profiling)
+
+    def _forward_method(self, inputs, camera, fov_y_radians, tf, volume, profiling):
+        ray_start = ray_dir = None
+        if camera is not None:
+            # forward variables are taken with respect to per-pixel rays
+            ray_start, ray_dir = Camera.generate_rays(camera, fov_y_radians, self._settings.screen_size.x,
+                                                      self._settings.screen_size.y)
+            inputs.camera_mode = pyrenderer.CameraMode.RayStartDir
+        elif isinstance(inputs.camera, pyrenderer.CameraPerPixelRays):
+            ray_start, ray_dir = inputs.camera.ray_start, inputs.camera.ray_dir
+        assert _implies(self._optimize_camera, inputs.camera_mode == pyrenderer.CameraMode.RayStartDir)
+        if tf is None:
+            tf = inputs.tf
+        if volume is None:
+            volume = inputs.volume
+        return _ForwardModeFunction.apply(ray_start, ray_dir, tf, volume, inputs, self._optimize_camera,
+                                          self._optimize_tf, self._forward_delayed_gradients, profiling)

@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define DVR_ABI_VERSION 3
+#define DVR_ABI_VERSION 4
 
 /* ---- status codes ---- */
 #define DVR_OK 0
@@ -217,6 +217,38 @@ int dvr_render_adjoint_batched(const DvrRendererInputs* inputs, const DvrRendere
                                const DvrTensor* adj_colors, const DvrAdjointOutputs* adj_outputs, int32_t n,
                                void* cuda_stream);
 
+/* Mirrors renderer::ForwardDifferencesSettingsHost (renderer/renderer.h:73-93):
+ * which variables forward-mode differentiation traces, each given the index
+ * of its derivative in [0, D); -1 = not traced. */
+typedef struct DvrForwardDifferencesSettings {
+  int32_t D;                     /* number of derivatives */
+  int32_t d_stepsize;            /* the step size */
+  int32_t d_ray_start[3];        /* ray start x, y, z (after ray generation, any camera mode) */
+  int32_t d_ray_dir[3];          /* ray direction x, y, z */
+  int32_t has_tf_derivatives;    /* nonzero: d_tf holds TF derivative indices */
+  int32_t pad_;
+  DvrTensor d_tf;                /* int32, the TF's shape (B) R C: index of each TF entry, -1 = not traced */
+} DvrForwardDifferencesSettings;
+/* Forward rendering with forward-mode derivatives: writes color, termination
+ * index and gradients_out (B*H*W*D*4 float32, d color / d variable; no
+ * zeroing needed).  Any D; volume derivatives are not available in forward
+ * mode.  The checkpoint and sample-record fields of outputs are ignored.
+ * Replaces renderer::Renderer::renderForwardGradients
+ * (renderer/renderer.h:192-196, renderer/renderer.cpp:419-498). */
+int dvr_render_forward_gradients(const DvrRendererInputs* inputs, const DvrForwardDifferencesSettings* settings,
+                                 const DvrRendererOutputs* outputs, const DvrTensor* gradients_out,
+                                 void* cuda_stream);
+/* Contracts forward variables (B*H*W*D*4, from dvr_render_forward_gradients)
+ * with the colour adjoint (B*H*W*4): per pixel, the gradient of each traced
+ * variable is dot(adj_color, d color / d variable).  Step-size and camera
+ * gradients are written per pixel (accumulated where the output broadcasts
+ * over a dimension), TF gradients are accumulated (zero-initialise adj_tf).
+ * Volume and viewport derivatives are rejected.
+ * Replaces renderer::Renderer::forwardVariablesToGradients
+ * (renderer/renderer.h:212-216, renderer/renderer.cpp:500-558). */
+int dvr_forward_variables_to_gradients(const DvrTensor* forward_variables, const DvrTensor* adj_color,
+                                       const DvrForwardDifferencesSettings* settings,
+                                       const DvrAdjointOutputs* adj_outputs, void* cuda_stream);
 /* Number of checkpoint slots per ray (the C of DvrRendererOutputs.checkpoints)
  * for rays of at most max_ray_length world units inside the box (the box
  * diagonal bounds it) marched with steps of at least min_step_size, at the

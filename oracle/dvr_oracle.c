@@ -18,6 +18,7 @@
 
 #include <math.h>
 #include <stddef.h>
+#include <stdlib.h>
 
 #if DVR_ORACLE_DOUBLE
 typedef double real_t;
@@ -584,6 +585,284 @@ int oracle_adjoint(const OracleInputs* in, const OracleTensor* color, const Orac
         else { *ps[c] = vs[c]; *pd[c] = vd[c]; }
       }
     }
+  }
+  return 0;
+}
+
+/* ---- forward-mode differentiation (renderer/renderer_kernels.cuh:131-240) ----
+ * Every traced quantity carries, next to its value, its D partial derivatives
+ * with respect to the variables the settings select: the step size, the
+ * components of the ray start and direction (after ray generation), and TF
+ * entries (each with its own index, renderer/renderer_settings.cuh:189-206).
+ * The values are computed by the same functions as oracle_forward, so colour
+ * and termination index are identical; the derivatives follow the chain rule
+ * through the position, the density (trilinear gradient; nearest sampling
+ * has none), the TF and the blend.  The entry and exit distances are not
+ * traced (:201-207).  The reference's dual-number type (cudAD) is not part of
+ * the reference sources, so this restates the derivatives directly. */
+
+static inline real_t* at5(const OracleTensor* t, int64_t i0, int64_t i1, int64_t i2, int64_t i3, int64_t i4) {
+  return (real_t*)t->data + i0 * bstride(t, 0) + i1 * bstride(t, 1) + i2 * bstride(t, 2) + i3 * bstride(t, 3) +
+         i4 * bstride(t, 4);
+}
+
+/* derivative index of TF entry (r, c), or -1 */
+static inline int tf_index(const OracleForwardSettings* fs, int b, int r, int c) {
+  if (!fs->has_tf) return -1;
+  const int i = *iat3(&fs->d_tf, b, r, c);
+  return (i >= 0 && i < fs->D) ? i : -1;
+}
+
+static inline int var_index(int i, int D) { return (i >= 0 && i < D) ? i : -1; }
+
+/* Derivatives of the TF colour: dc[ch * D + j] = d c_ch / d var_j, given the
+ * density's derivatives dden (renderer/renderer_tf.cuh:122-150, :256-290,
+ * :437-486, :522-560).  Clamps select an operand together with its
+ * derivatives: the identity TF's density clamp passes the derivative only
+ * strictly inside (0, 1), like its adjoint; the linear TF's density clamp to
+ * [p0, p1] takes the derivative of the bound it clamps to. */
+static void tf_dual(const OracleInputs* in, const OracleForwardSettings* fs, int b, real_t density,
+                    const real_t* dden, real_t* dc) {
+  const OracleTensor* tf = &in->tf;
+  const int R = (int)tf->sizes[1];
+  const int D = fs->D;
+  for (int j = 0; j < 4 * D; ++j) dc[j] = 0;
+  switch (in->tf_mode) {
+    case 0: {
+      const real_t dcl = clampr(density, 0, 1);
+      const int inside = density > 0 && density < 1;
+      const real_t sa = *at3(tf, b, 0, 0), sc = *at3(tf, b, 0, 1);
+      if (inside)
+        for (int j = 0; j < D; ++j) {
+          dc[0 * D + j] = dden[j] * sc;
+          dc[1 * D + j] = dden[j] * sc;
+          dc[2 * D + j] = dden[j] * sc;
+          dc[3 * D + j] = dden[j] * sa;
+        }
+      const int isa = tf_index(fs, b, 0, 0), isc = tf_index(fs, b, 0, 1);
+      if (isa >= 0) dc[3 * D + isa] += dcl;
+      if (isc >= 0) { dc[0 * D + isc] += dcl; dc[1 * D + isc] += dcl; dc[2 * D + isc] += dcl; }
+      break;
+    }
+    case 1: {
+      const real_t d = density * R - (real_t)0.5;
+      const int di = (int)floorf((float)d);
+      const real_t df = d - di;
+      const int i0 = clampi(di, 0, R - 1), i1 = clampi(di + 1, 0, R - 1);
+      const v4 a = tf4(tf, b, i0), c = tf4(tf, b, i1);
+      const real_t dv[4] = {c.x - a.x, c.y - a.y, c.z - a.z, c.w - a.w};
+      for (int ch = 0; ch < 4; ++ch)
+        for (int j = 0; j < D; ++j) dc[ch * D + j] = dv[ch] * (R * dden[j]);
+      for (int ch = 0; ch < 4; ++ch) {
+        const int k0 = tf_index(fs, b, i0, ch), k1 = tf_index(fs, b, i1, ch);
+        if (k0 >= 0) dc[ch * D + k0] += 1 - df;
+        if (k1 >= 0) dc[ch * D + k1] += df;
+      }
+      break;
+    }
+    case 2: {
+      const int i = linear_interval(tf, b, R, density);
+      const v4 a = tf4(tf, b, i), c = tf4(tf, b, i + 1);
+      const real_t p0 = *at3(tf, b, i, 4), p1 = *at3(tf, b, i + 1, 4);
+      const int lo = density < p0, hi = !lo && density > p1;
+      const real_t d2 = lo ? p0 : (hi ? p1 : density);
+      const real_t den = p1 - p0;
+      const real_t fr = (d2 - p0) / den;
+      const real_t dv[4] = {c.x - a.x, c.y - a.y, c.z - a.z, c.w - a.w};
+      const int ip0 = tf_index(fs, b, i, 4), ip1 = tf_index(fs, b, i + 1, 4);
+      for (int j = 0; j < D; ++j) {
+        const real_t dp0 = j == ip0 ? 1 : 0, dp1 = j == ip1 ? 1 : 0;
+        const real_t dd2 = lo ? dp0 : (hi ? dp1 : dden[j]);
+        const real_t dfr = ((dd2 - dp0) * den - (d2 - p0) * (dp1 - dp0)) / (den * den);
+        for (int ch = 0; ch < 4; ++ch) dc[ch * D + j] = dv[ch] * dfr;
+      }
+      for (int ch = 0; ch < 4; ++ch) {
+        const int k0 = tf_index(fs, b, i, ch), k1 = tf_index(fs, b, i + 1, ch);
+        if (k0 >= 0) dc[ch * D + k0] += 1 - fr;
+        if (k1 >= 0) dc[ch * D + k1] += fr;
+      }
+      break;
+    }
+    default: {
+      for (int i = 0; i < R; ++i) {
+        const v4 ci = tf4(tf, b, i);
+        const real_t cv[4] = {ci.x, ci.y, ci.z, ci.w};
+        const real_t mu = *at3(tf, b, i, 4), sigma = *at3(tf, b, i, 5);
+        const real_t ni = gauss(density, mu, sigma);
+        const real_t s2 = sigma * sigma;
+        const int imu = tf_index(fs, b, i, 4), isg = tf_index(fs, b, i, 5);
+        for (int j = 0; j < D; ++j) {
+          const real_t dmu = j == imu ? 1 : 0, dsg = j == isg ? 1 : 0;
+          const real_t dn = ni * (-(density - mu) * (dden[j] - dmu) / s2 +
+                                  (density - mu) * (density - mu) * dsg / (s2 * sigma));
+          for (int ch = 0; ch < 4; ++ch) dc[ch * D + j] += cv[ch] * dn;
+        }
+        for (int ch = 0; ch < 4; ++ch) {
+          const int k = tf_index(fs, b, i, ch);
+          if (k >= 0) dc[ch * D + k] += ni;
+        }
+      }
+      break;
+    }
+  }
+}
+
+/* trilinear density and its gradient with respect to the volume position */
+static real_t trilerp_grad(const real_t* d, const real_t* f, v3* g) {
+  const real_t ay0 = lerp1(d[0], d[4], f[0]), ay1 = lerp1(d[2], d[6], f[0]);
+  const real_t by0 = lerp1(d[1], d[5], f[0]), by1 = lerp1(d[3], d[7], f[0]);
+  g->x = lerp1(lerp1(d[4] - d[0], d[6] - d[2], f[1]), lerp1(d[5] - d[1], d[7] - d[3], f[1]), f[2]);
+  g->y = lerp1(ay1 - ay0, by1 - by0, f[2]);
+  g->z = lerp1(by0, by1, f[1]) - lerp1(ay0, ay1, f[1]);
+  return lerp1(lerp1(ay0, ay1, f[1]), lerp1(by0, by1, f[1]), f[2]);
+}
+
+int oracle_forward_gradients(const OracleInputs* in, const OracleForwardSettings* fs, OracleTensor* color,
+                             OracleTensor* termination, OracleTensor* grads) {
+  if (check_modes(in)) return 2;
+  const int D = fs->D;
+  if (D <= 0) return 3;
+  const int W = in->width, H = in->height, B = in->batch;
+  const int64_t count = (int64_t)W * H * B;
+  const real_t early_out = (real_t)in->blending_early_out;
+  const int istep = var_index(fs->d_stepsize, D);
+  int istart[3], idir[3];
+  for (int c = 0; c < 3; ++c) {
+    istart[c] = var_index(fs->d_ray_start[c], D);
+    idir[c] = var_index(fs->d_ray_dir[c], D);
+  }
+  int failed = 0;
+#pragma omp parallel for schedule(guided)
+  for (int64_t i = 0; i < count; ++i) {
+    const int b = (int)(i / ((int64_t)W * H));
+    const int y = (int)((i - (int64_t)b * W * H) / W);
+    const int x = (int)(i - (int64_t)W * (y + (int64_t)H * b));
+    /* derivative arrays of one ray: start, dir, step, volume position,
+     * density, TF colour, alpha, accumulator */
+    real_t* buf = (real_t*)calloc((size_t)D * 21, sizeof(real_t));
+    if (!buf) {
+#pragma omp atomic write
+      failed = 1;
+      continue;
+    }
+    real_t *dstart = buf, *ddir = buf + 3 * D, *dstep = buf + 6 * D, *dvp = buf + 7 * D, *dden = buf + 10 * D;
+    real_t *dc = buf + 11 * D, *dalpha = buf + 15 * D, *dacc = buf + 16 * D;
+    RaySetup r;
+    ray_setup(in, x, y, b, &r);
+    for (int c = 0; c < 3; ++c) {
+      if (istart[c] >= 0) dstart[c * D + istart[c]] = 1;
+      if (idir[c] >= 0) ddir[c * D + idir[c]] = 1;
+    }
+    if (istep >= 0) dstep[istep] = 1;
+    const real_t dirv[3] = {r.dir.x, r.dir.y, r.dir.z};
+    const real_t vox3[3] = {r.voxel.x, r.voxel.y, r.voxel.z};
+    Sampler s = {b, (int)in->volume.sizes[1], (int)in->volume.sizes[2], (int)in->volume.sizes[3], &in->volume};
+    v4 acc = mk4(0, 0, 0, 0);
+    int k;
+    for (k = 0;; ++k) {
+      const real_t t = r.tmin + k * r.step;
+      if (t > r.tmax) break;
+      if (acc.w > early_out) break;
+      const v3 p = volume_pos(&r, t);
+      /* volumePos = (start + t dir - boxMin) / voxelSize, t = tmin + k step */
+      for (int c = 0; c < 3; ++c)
+        for (int j = 0; j < D; ++j)
+          dvp[c * D + j] = (dstart[c * D + j] + k * dstep[j] * dirv[c] + t * ddir[c * D + j]) / vox3[c];
+      real_t density;
+      if (in->filter_mode == 0) {
+        density = sample_forward(&s, 0, p);
+        for (int j = 0; j < D; ++j) dden[j] = 0;
+      } else {
+        int ip[3] = {(int)p.x, (int)p.y, (int)p.z};
+        real_t d8[8], f[3] = {p.x - (real_t)ip[0], p.y - (real_t)ip[1], p.z - (real_t)ip[2]};
+        cell_corners(&s, ip, d8);
+        v3 g;
+        trilerp_grad(d8, f, &g);
+        density = trilerp(d8, f);
+        for (int j = 0; j < D; ++j) dden[j] = g.x * dvp[j] + g.y * dvp[D + j] + g.z * dvp[2 * D + j];
+      }
+      const v4 cur = tf_eval(in, b, density);
+      tf_dual(in, fs, b, density, dden, dc);
+      const real_t a = blend_alpha(in->blend_mode, cur.w, r.step);
+      if (in->blend_mode == 0) {
+        const real_t e = R_EXP(-cur.w * r.step);
+        for (int j = 0; j < D; ++j) dalpha[j] = e * (dc[3 * D + j] * r.step + cur.w * dstep[j]);
+      } else {
+        const int lin = cur.w * r.step < 1;
+        for (int j = 0; j < D; ++j) dalpha[j] = lin ? dc[3 * D + j] * r.step + cur.w * dstep[j] : 0;
+      }
+      /* colorOut = acc + (1 - acc.w) c alpha, alphaOut = acc.w + (1 - acc.w) alpha
+       * (renderer/renderer_blending.cuh:40-52) */
+      const real_t T = 1 - acc.w;
+      const real_t cv[3] = {cur.x, cur.y, cur.z};
+      for (int j = 0; j < D; ++j) {
+        const real_t dT = -dacc[3 * D + j];
+        for (int c = 0; c < 3; ++c)
+          dacc[c * D + j] += dT * cv[c] * a + T * dc[c * D + j] * a + T * cv[c] * dalpha[j];
+        dacc[3 * D + j] += dT * a + T * dalpha[j];
+      }
+      acc = blend(in->blend_mode, acc, cur, r.step);
+    }
+    *at4(color, b, y, x, 0) = acc.x;
+    *at4(color, b, y, x, 1) = acc.y;
+    *at4(color, b, y, x, 2) = acc.z;
+    *at4(color, b, y, x, 3) = acc.w;
+    *iat3(termination, b, y, x) = k;
+    for (int j = 0; j < D; ++j)
+      for (int c = 0; c < 4; ++c) *at5(grads, b, y, x, j, c) = dacc[c * D + j];
+    free(buf);
+  }
+  return failed ? 4 : 0;
+}
+
+/* renderer/renderer_kernels.cuh:505-560: per pixel, each enabled variable's
+ * gradient is dot(adj_color, d color / d variable); step size and camera
+ * gradients are per pixel (accumulated where their output broadcasts), TF
+ * gradients accumulate over the pixels. */
+int oracle_forward_variables_to_gradients(const OracleTensor* fwd, const OracleTensor* adj_color,
+                                          const OracleForwardSettings* fs, OracleAdjointOutputs* out) {
+  const int B = (int)fwd->sizes[0], H = (int)fwd->sizes[1], W = (int)fwd->sizes[2], D = (int)fwd->sizes[3];
+  if (D != fs->D) return 3;
+  const int64_t count = (int64_t)W * H * B;
+  const int istep = var_index(fs->d_stepsize, D);
+  const int R = fs->has_tf ? (int)fs->d_tf.sizes[1] : 0, C = fs->has_tf ? (int)fs->d_tf.sizes[2] : 0;
+#pragma omp parallel for schedule(guided)
+  for (int64_t i = 0; i < count; ++i) {
+    const int b = (int)(i / ((int64_t)W * H));
+    const int y = (int)((i - (int64_t)b * W * H) / W);
+    const int x = (int)(i - (int64_t)W * (y + (int64_t)H * b));
+    const v4 g = mk4(*at4(adj_color, b, y, x, 0), *at4(adj_color, b, y, x, 1), *at4(adj_color, b, y, x, 2),
+                     *at4(adj_color, b, y, x, 3));
+#define FWD4(j) mk4(*at5(fwd, b, y, x, j, 0), *at5(fwd, b, y, x, j, 1), *at5(fwd, b, y, x, j, 2), *at5(fwd, b, y, x, j, 3))
+    if (out->has_stepsize && istep >= 0) {
+      real_t* p = at3(&out->adj_stepsize, b, y, x);
+      const real_t v = dot4(g, FWD4(istep));
+      if (out->stepsize_broadcast) atomic_add(p, v);
+      else *p = v;
+    }
+    if (out->has_camera)
+      for (int c = 0; c < 3; ++c) {
+        const int is = var_index(fs->d_ray_start[c], D), id = var_index(fs->d_ray_dir[c], D);
+        if (is >= 0) {
+          real_t* p = at4(&out->adj_ray_start, b, y, x, c);
+          const real_t v = dot4(g, FWD4(is));
+          if (out->camera_broadcast) atomic_add(p, v);
+          else *p = v;
+        }
+        if (id >= 0) {
+          real_t* p = at4(&out->adj_ray_dir, b, y, x, c);
+          const real_t v = dot4(g, FWD4(id));
+          if (out->camera_broadcast) atomic_add(p, v);
+          else *p = v;
+        }
+      }
+    if (out->has_tf && fs->has_tf)
+      for (int r = 0; r < R; ++r)
+        for (int c = 0; c < C; ++c) {
+          const int k = tf_index(fs, b, r, c);
+          if (k >= 0) atomic_add(at3(&out->adj_tf, b, r, c), dot4(g, FWD4(k)));
+        }
+#undef FWD4
   }
   return 0;
 }

@@ -69,11 +69,31 @@ typedef struct OracleAdjointOutputs {
   OracleTensor adj_tf;         /* (B) R C */
 } OracleAdjointOutputs;
 
+/* Forward-mode derivative indices (renderer/renderer_settings.cuh:189-206):
+ * -1 = not traced, else an index in [0, D). */
+typedef struct OracleForwardSettings {
+  int32_t D;
+  int32_t d_stepsize;
+  int32_t d_ray_start[3];
+  int32_t d_ray_dir[3];
+  int32_t has_tf;
+  int32_t pad_;
+  OracleTensor d_tf;           /* int32 (B) R C */
+} OracleForwardSettings;
+
 /* Returns 0 on success, nonzero for an unsupported mode combination. */
 int oracle_forward(const OracleInputs* in, OracleTensor* color, OracleTensor* termination);
 int oracle_adjoint(const OracleInputs* in, const OracleTensor* color,
                    const OracleTensor* termination, const OracleTensor* adj_color,
                    OracleAdjointOutputs* out);
+/* Forward march with forward-mode derivatives: color, termination and
+ * gradients B H W D 4 (d color / d variable) — renderForwardGradients. */
+int oracle_forward_gradients(const OracleInputs* in, const OracleForwardSettings* fs, OracleTensor* color,
+                             OracleTensor* termination, OracleTensor* gradients);
+/* Contracts forward variables B H W D 4 with adj_color B H W 4 into the
+ * enabled adjoint outputs (stepsize, camera, TF) — forwardVariablesToGradients. */
+int oracle_forward_variables_to_gradients(const OracleTensor* forward_variables, const OracleTensor* adj_color,
+                                          const OracleForwardSettings* fs, OracleAdjointOutputs* out);
 /* Size of real_t in this build (4 or 8). */
 int oracle_real_size(void);
 

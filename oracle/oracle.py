@@ -65,6 +65,15 @@ class OracleAdjointOutputs(ctypes.Structure):
     ]
 
 
+class OracleForwardSettings(ctypes.Structure):
+    _fields_ = [
+        ("D", ctypes.c_int32), ("d_stepsize", ctypes.c_int32),
+        ("d_ray_start", ctypes.c_int32 * 3), ("d_ray_dir", ctypes.c_int32 * 3),
+        ("has_tf", ctypes.c_int32), ("pad_", ctypes.c_int32),
+        ("d_tf", OracleTensor),
+    ]
+
+
 def build(reference: bool = True, quiet: bool = True) -> None:
     """Builds the port libraries (and the reference harness when its sources exist)."""
     out = subprocess.DEVNULL if quiet else None
@@ -101,6 +110,15 @@ def load(kind: str = "port", precision: str = "f64") -> ctypes.CDLL:
         lib.oracle_forward.restype = ctypes.c_int
         lib.oracle_adjoint.restype = ctypes.c_int
         lib.oracle_real_size.restype = ctypes.c_int
+        if hasattr(lib, "oracle_forward_gradients"):  # the port only: the reference's needs cudAD
+            lib.oracle_forward_gradients.argtypes = [
+                ctypes.POINTER(OracleInputs), ctypes.POINTER(OracleForwardSettings), ctypes.POINTER(OracleTensor),
+                ctypes.POINTER(OracleTensor), ctypes.POINTER(OracleTensor)]
+            lib.oracle_forward_gradients.restype = ctypes.c_int
+            lib.oracle_forward_variables_to_gradients.argtypes = [
+                ctypes.POINTER(OracleTensor), ctypes.POINTER(OracleTensor), ctypes.POINTER(OracleForwardSettings),
+                ctypes.POINTER(OracleAdjointOutputs)]
+            lib.oracle_forward_variables_to_gradients.restype = ctypes.c_int
         _LIBS[key] = lib
     return _LIBS[key]
 
@@ -247,4 +265,88 @@ def adjoint(scene: Scene, color: np.ndarray, term: np.ndarray, adj_color: np.nda
                             ctypes.byref(out))
     if rc != 0:
         raise RuntimeError(f"oracle_adjoint failed with code {rc}")
+    return res
+
+
+@dataclass
+class ForwardSettings:
+    """Forward-mode derivative indices (-1 = not traced); d_tf is an int array
+    of the TF's shape ((B) R C) or None."""
+    D: int
+    d_stepsize: int = -1
+    d_ray_start: tuple = (-1, -1, -1)
+    d_ray_dir: tuple = (-1, -1, -1)
+    d_tf: Optional[np.ndarray] = None
+
+
+def _forward_settings(fs: ForwardSettings, keep: list) -> OracleForwardSettings:
+    o = OracleForwardSettings()
+    o.D = int(fs.D)
+    o.d_stepsize = int(fs.d_stepsize)
+    for c in range(3):
+        o.d_ray_start[c] = int(fs.d_ray_start[c])
+        o.d_ray_dir[c] = int(fs.d_ray_dir[c])
+    o.has_tf = int(fs.d_tf is not None)
+    o.d_tf = _tensor(None if fs.d_tf is None else np.asarray(fs.d_tf, dtype=np.int32), keep)
+    return o
+
+
+def forward_gradients(scene: Scene, fs: ForwardSettings, precision: str = "f64"):
+    """Forward march with forward-mode derivatives; returns (color B*H*W*4,
+    termination B*H*W, gradients B*H*W*D*4)."""
+    lib = load("port", precision)
+    dt = _dtype(lib)
+    keep: list = []
+    inp = _inputs(scene, dt, keep)
+    B, H, W = inp.batch, scene.height, scene.width
+    color = np.zeros((B, H, W, 4), dtype=dt)
+    term = np.zeros((B, H, W), dtype=np.int32)
+    grads = np.zeros((B, H, W, fs.D, 4), dtype=dt)
+    tc, tt, tg = _tensor(color, keep), _tensor(term, keep), _tensor(grads, keep)
+    ofs = _forward_settings(fs, keep)
+    rc = lib.oracle_forward_gradients(ctypes.byref(inp), ctypes.byref(ofs), ctypes.byref(tc), ctypes.byref(tt),
+                                      ctypes.byref(tg))
+    if rc != 0:
+        raise RuntimeError(f"oracle_forward_gradients failed with code {rc}")
+    return color, term, grads
+
+
+def forward_variables_to_gradients(forward_variables: np.ndarray, adj_color: np.ndarray, fs: ForwardSettings,
+                                   req: AdjointRequest, tf_shape: Optional[tuple] = None,
+                                   precision: str = "f64") -> dict:
+    """Contracts forward variables with adj_color into the requested
+    stepsize / camera / TF gradients (zero-initialised)."""
+    lib = load("port", precision)
+    dt = _dtype(lib)
+    keep: list = []
+    fv = np.asarray(forward_variables, dtype=dt)
+    B, H, W = fv.shape[:3]
+    out = OracleAdjointOutputs()
+    res = {}
+    if req.tf:
+        shp = tf_shape if tf_shape is not None else fs.d_tf.shape
+        res["adj_tf"] = np.zeros(shp, dtype=dt)
+        out.has_tf = 1
+        out.adj_tf = _tensor(res["adj_tf"], keep)
+    if req.camera:
+        cb = req.camera_batch or B
+        res["adj_ray_start"] = np.zeros((cb, H, W, 3), dtype=dt)
+        res["adj_ray_dir"] = np.zeros((cb, H, W, 3), dtype=dt)
+        out.has_camera = 1
+        out.camera_broadcast = int(cb != B)
+        out.adj_ray_start = _tensor(res["adj_ray_start"], keep)
+        out.adj_ray_dir = _tensor(res["adj_ray_dir"], keep)
+    if req.stepsize:
+        shp = req.stepsize_shape or (B, H, W)
+        res["adj_stepsize"] = np.zeros(shp, dtype=dt)
+        out.has_stepsize = 1
+        out.stepsize_broadcast = int(tuple(shp) != (B, H, W))
+        out.adj_stepsize = _tensor(res["adj_stepsize"], keep)
+    ofs = _forward_settings(fs, keep)
+    tf_ = _tensor(fv, keep)
+    ta = _tensor(np.asarray(adj_color, dtype=dt), keep)
+    rc = lib.oracle_forward_variables_to_gradients(ctypes.byref(tf_), ctypes.byref(ta), ctypes.byref(ofs),
+                                                   ctypes.byref(out))
+    if rc != 0:
+        raise RuntimeError(f"oracle_forward_variables_to_gradients failed with code {rc}")
     return res

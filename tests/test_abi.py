@@ -26,7 +26,7 @@ def test_library_exports_every_header_symbol(dvr_lib):
     for n in names:
         assert hasattr(dvr_lib, n), n
     assert set(names) == set(_abi.SIGNATURES)
-    assert dvr_lib.dvr_abi_version() == 3
+    assert dvr_lib.dvr_abi_version() == 4
 
 
 def _fake(shape, dtype=_abi.DVR_FLOAT32, cuda=True, ptr=0x100000):
@@ -201,7 +201,17 @@ def test_python_api_mirrors_reference_names():
     assert abs(inp.blending_early_out - (1 - 1e-5)) < 1e-12
 
 
-def test_forward_mode_differentiation_is_reported_missing():
+def test_forward_mode_interface():
+    """The forward method's names (bindings/bindings.cpp:423-436, :455, :496;
+    pytests/diffdvr/renderer.py:271-311)."""
     from diffdvr_gb300 import Renderer
-    with pytest.raises(NotImplementedError):
-        Renderer(optimize_tf=True, gradient_method="forward")
+    s = pr.ForwardDifferencesSettings()
+    for f in ("D", "d_stepsize", "d_rayStart", "d_rayDir", "d_tf", "has_tf_derivatives"):
+        assert hasattr(s, f), f
+    assert s.NOT_ENABLED == -1 and s.d_stepsize == -1 and tuple(s.d_rayStart) == (-1, -1, -1)
+    assert callable(pr.Renderer.render_forward_gradients)
+    assert callable(pr.Renderer.forward_variables_to_gradients)
+    Renderer(optimize_tf=True, gradient_method="forward")
+    Renderer(optimize_camera=True, gradient_method="forward", forward_delayed_gradients=True)
+    with pytest.raises(AssertionError):
+        Renderer(optimize_volume=True, gradient_method="forward")
