@@ -25,6 +25,12 @@ absorption_recon_128 (volume gradient, 64 views into 128^3), large_mixed_512
 (512^3 BF16, 16 views at 1024^2, ray + volume + TF gradients) and
 plain_cpu_64 (the CPU-sized case).
 
+--method forward times the forward method of the same workload instead
+(render_forward_gradients tracing one derivative per TF entry, and camera
+rays where the workload optimises them, + L2-loss gradient +
+forward_variables_to_gradients); its CPU baseline is the oracle's forward
+mode (the reference's forward mode needs cudAD, absent from its sources).
+
 Multi-GPU: rays and views shard without any exchange in a TF-only step except
 the TF-gradient sum, so N GPUs run N replicas ("scaling": "weak").
 """
@@ -43,6 +49,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "fwd+adjoint samples/sec: batched-BF16 vs plain FP32, grad rel err ≤1e-3"
+METRIC_FORWARD = "forward-mode samples/sec: render_forward_gradients + forward_variables_to_gradients"
 # the headline workload (the default) and the other configurations of the metric
 WORKLOADS = {
     "tf_reconstruction_256": {
@@ -77,6 +84,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline budget")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--interval", type=int, default=0, help="transmittance checkpoint interval (workload default)")
+    ap.add_argument("--method", choices=["adjoint", "forward"], default="adjoint",
+                    help="gradient method: adjoint (the headline) or forward-mode derivatives")
     ap.add_argument("--record", choices=["full", "auto", "none"], default="auto",
                     help="sample record: a pool for every ray; one for every ray if that fits in a quarter of "
                          "the free device memory, else as large as that; or none")
@@ -262,7 +271,7 @@ def run_gpu(args):
     out = pr.RendererOutputs(color, term, ckpt, K)
     pool = 0
     record_mode = "none"
-    if args.record != "none":
+    if args.record != "none" and args.method == "adjoint":
         full = pr.Renderer.sample_density_size(inp_s, B)
         pool = full
         if args.record == "auto":
@@ -289,6 +298,25 @@ def run_gpu(args):
         g_tensors += [adj.adj_camera_ray_start, adj.adj_camera_ray_dir]
     adj_color = torch.empty_like(color)
     record_kernel = pool > 0 and grads == {"tf"} and w.tf_mode == 1
+    forward_method = args.method == "forward"
+    fs = J = out_fg = None
+    if forward_method:
+        if "volume" in grads:
+            raise SystemExit(f"the forward method has no volume derivatives ({args.workload} optimises the volume)")
+        fs = pr.ForwardDifferencesSettings()
+        D = 0
+        if "camera" in grads:
+            fs.d_rayStart, fs.d_rayDir = pr.int3(0, 1, 2), pr.int3(3, 4, 5)
+            D = 6
+        if "tf" in grads:
+            _, R, C = tf.shape
+            fs.d_tf = torch.arange(D, D + R * C, dtype=torch.int32, device=dev).reshape(1, R, C)
+            fs.has_tf_derivatives = True
+            D += R * C
+        fs.D = D
+        J = torch.empty(B, H, W, D, 4, device=dev)
+        out_fg = pr.RendererOutputs(color, term)
+        record_kernel = False
 
     # target image: the target volume (absorption reconstruction) or the TF perturbed
     target = torch.empty_like(color)
@@ -314,7 +342,10 @@ def run_gpu(args):
         if record:
             e = (ev(), ev(), ev(), ev())
             e[0].record()
-        pr.Renderer.render_forward(inp_s, out)
+        if forward_method:
+            pr.Renderer.render_forward_gradients(inp_s, fs, out_fg, J)
+        else:
+            pr.Renderer.render_forward(inp_s, out)
         if record:
             e[1].record()
         torch.sub(color, target, out=adj_color)
@@ -323,7 +354,10 @@ def run_gpu(args):
             t.zero_()
         if record:
             e[2].record()
-        pr.Renderer.render_adjoint(inp_s, out, adj_color, adj)
+        if forward_method:
+            pr.Renderer.forward_variables_to_gradients(J, adj_color, fs, adj)
+        else:
+            pr.Renderer.render_adjoint(inp_s, out, adj_color, adj)
         if record:
             e[3].record()
             fwd_ev.append((e[0], e[1]))
@@ -406,13 +440,19 @@ def run_gpu(args):
         for d, h in zip(cam_d, cam_host):
             d.copy_(h, non_blocking=True)
         tgt_d.copy_(target_host, non_blocking=True)
-        pr.Renderer.render_forward(inp_e2e, out)
+        if forward_method:
+            pr.Renderer.render_forward_gradients(inp_e2e, fs, out_fg, J)
+        else:
+            pr.Renderer.render_forward(inp_e2e, out)
         torch.sub(color, tgt_d, out=adj_color)
         loss_d.copy_((adj_color * adj_color).sum().view(1))
         adj_color.mul_(2 * inv_n)
         for t in g_tensors:
             t.zero_()
-        pr.Renderer.render_adjoint(inp_e2e, out, adj_color, adj)
+        if forward_method:
+            pr.Renderer.forward_variables_to_gradients(J, adj_color, fs, adj)
+        else:
+            pr.Renderer.render_adjoint(inp_e2e, out, adj_color, adj)
         loss_host.copy_(loss_d, non_blocking=True)
         if grad_host is not None:
             grad_host.copy_(read_back, non_blocking=True)
@@ -425,7 +465,7 @@ def run_gpu(args):
 
     # ---- plain FP32 arm (same workload, the reference's GPU algorithm)
     plain = None
-    if not args.no_plain:
+    if not args.no_plain and not forward_method:
         inp32 = inputs(vol32, tf, cam)
         out32 = pr.RendererOutputs(torch.empty_like(color), torch.empty_like(term))
 
@@ -459,12 +499,21 @@ def run_gpu(args):
     P = B * H * W
     ck_written = int(torch.clamp((term.to(torch.int64) - 1) // K, min=0).clamp_max(slots).sum().item())
     s_v = vol_s.element_size()
-    fwd_bytes, adj_bytes = algorithmic_bytes(w, s_v, V, P, samples, ck_written, pool > 0, record_kernel, tf.numel())
-    dominant = ("adjoint", adj_bytes, adj_ms) if adj_ms >= fwd_ms else ("forward", fwd_bytes, fwd_ms)
+    if forward_method:
+        # volume once, colour + termination, the forward variables written once and read once
+        fwd_bytes = V * s_v + P * (16 + 4) + P * fs.D * 16
+        adj_bytes = P * fs.D * 16 + P * 16 + tf.numel() * 4 * 2 + (P * 24 if "camera" in grads else 0)
+        names = ("contraction", "forward gradients")
+    else:
+        fwd_bytes, adj_bytes = algorithmic_bytes(w, s_v, V, P, samples, ck_written, pool > 0, record_kernel,
+                                                 tf.numel())
+        names = ("adjoint", "forward")
+    dominant = (names[0], adj_bytes, adj_ms) if adj_ms >= fwd_ms else (names[1], fwd_bytes, fwd_ms)
     achieved = dominant[1] / (dominant[2] / 1e3) / 1e9
     tr = profiled_traffic()
     traffic = None
-    if tr and tr.get("workload") == args.workload and tr.get("record") == record_mode and tr.get("views") == B:
+    if tr and tr.get("workload") == args.workload and tr.get("record") == record_mode and tr.get("views") == B \
+            and tr.get("method", "adjoint") == args.method:
         traffic = tr.get("dram_bytes_per_launch", {}).get(dominant[0])
     # 8 corner reads per sample in the forward, and in the adjoint unless it reads the record
     regather = pool == 0 or "camera" in grads
@@ -472,9 +521,11 @@ def run_gpu(args):
     # kernels of ours per step: forward = ray order (3) + march; adjoint = ray order (3) + the
     # record kernel and the general kernel over its leftovers, or the general kernel alone
     launches_per_step = 4 + (5 if record_kernel else 4)
+    if forward_method:
+        launches_per_step = 2  # forward-gradient march + contraction
 
     result = {
-        "metric": METRIC,
+        "metric": METRIC_FORWARD if forward_method else METRIC,
         "value": value,
         "unit": "samples/s",
         "n_gpus": world,
@@ -489,6 +540,7 @@ def run_gpu(args):
         "config": {"workload": spec["desc"], "volume_storage": args.storage,
                    "tf_storage": "f32", "views": B, "image": [H, W], "volume": list(w.volume.shape[1:]),
                    "gradients": sorted(grads), "samples_per_step": samples, "rays_hit": rays_hit,
+                   "method": args.method, "forward_derivatives": fs.D if forward_method else None,
                    "checkpoint_interval": K, "sample_record": record_mode,
                    "recorded_rays": recorded_rays, "record_pool_MB": round(pool * 4 / 1e6, 1),
                    "l2": "flushed (256 MB write) before every timed step",
@@ -496,9 +548,11 @@ def run_gpu(args):
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": "samples/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": ms_e2e,
-                "path": "pyrenderer.Renderer.render_forward/render_adjoint, pinned host inputs"},
+                "path": ("pyrenderer.Renderer.render_forward_gradients/forward_variables_to_gradients"
+                         if forward_method else "pyrenderer.Renderer.render_forward/render_adjoint")
+                + ", pinned host inputs"},
         "gpu_launches": launches_per_step * args.steps,
-        "kernel_ms": {"forward": fwd_ms, "adjoint": adj_ms},
+        "kernel_ms": {names[1]: fwd_ms, names[0]: adj_ms},
         "roofline": {"bound": "hbm", "kernel": dominant[0], "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_launch": int(dominant[1]),
@@ -508,7 +562,7 @@ def run_gpu(args):
         "clocks": clock_summary,
     }
     if rank == 0:
-        result["cpu_baseline"] = None if args.no_cpu else cpu_baseline(w, args, vol32.cpu().numpy())
+        result["cpu_baseline"] = None if args.no_cpu else cpu_baseline(w, args, vol32.cpu().numpy(), args.method)
         print(json.dumps(result))
     if world > 1:
         dist.barrier()
@@ -535,18 +589,37 @@ def cpu_sample_scene(w, volume, n_rays: int, seed: int = 0):
     return sc
 
 
-def time_cpu(w, volume, budget_s: float, kind: str):
+def time_cpu(w, volume, budget_s: float, kind: str, method: str = "adjoint"):
     """Forward + adjoint (the workload's gradients) of a ray sample on the host
-    cores; returns (samples/s, description)."""
+    cores, or the forward method (forward-mode derivatives + contraction);
+    returns (samples/s, description)."""
     from oracle import oracle as O
     req = O.AdjointRequest(tf="tf" in w.grads, volume="volume" in w.grads, camera="camera" in w.grads)
+    fs = None
+    if method == "forward":
+        req.volume = False
+        D = 6 if "camera" in w.grads else 0
+        kw = {"d_ray_start": (0, 1, 2), "d_ray_dir": (3, 4, 5)} if D else {}
+        if "tf" in w.grads:
+            _, R, C = w.tf.shape
+            kw["d_tf"] = np.arange(D, D + R * C, dtype=np.int32).reshape(1, R, C)
+            D += R * C
+        fs = O.ForwardSettings(D=D, **kw)
+
+    def one_pass(sc):
+        if fs is not None:
+            c, term, J = O.forward_gradients(sc, fs, "f32")
+            O.forward_variables_to_gradients(J, np.full(c.shape, 1e-3, np.float32), fs, req, precision="f32")
+        else:
+            c, term = O.forward(sc, kind, "f32")
+            O.adjoint(sc, c, term, np.full(c.shape, 1e-3, np.float32), req, kind, "f32")
+        return term
+
     n = 512
     while True:
         sc = cpu_sample_scene(w, volume, n)
         t0 = time.perf_counter()
-        c, term = O.forward(sc, kind, "f32")
-        adj = np.full(c.shape, 1e-3, np.float32)
-        O.adjoint(sc, c, term, adj, req, kind, "f32")
+        one_pass(sc)
         dt = time.perf_counter() - t0
         if dt > budget_s / 6 or n >= 65536:
             break
@@ -554,19 +627,20 @@ def time_cpu(w, volume, budget_s: float, kind: str):
     reps, total, samples = 0, 0.0, 0
     while total < budget_s * 0.7 or reps < 2:
         t0 = time.perf_counter()
-        c, term = O.forward(sc, kind, "f32")
-        O.adjoint(sc, c, term, np.full(c.shape, 1e-3, np.float32), req, kind, "f32")
+        term = one_pass(sc)
         total += time.perf_counter() - t0
         samples += int(term.sum())
         reps += 1
-    return samples / total, f"{sc.width} rays of the workload (hitting the volume), {reps} fwd+adj passes"
+    what = "forward-mode + contraction" if fs is not None else "fwd+adj"
+    return samples / total, f"{sc.width} rays of the workload (hitting the volume), {reps} {what} passes"
 
 
-def cpu_baseline(w, args, volume):
+def cpu_baseline(w, args, volume, method: str = "adjoint"):
     from oracle import oracle as O
     O.build(reference=True)
-    kind = "reference" if O.reference_available() else "port"
-    value, sample = time_cpu(w, volume, args.cpu_seconds, kind)
+    # the reference's forward mode needs cudAD, which its sources do not include: the oracle port times it
+    kind = "reference" if O.reference_available() and method == "adjoint" else "port"
+    value, sample = time_cpu(w, volume, args.cpu_seconds, kind, method)
     return {"value": value, "unit": "samples/s", "cores": os.cpu_count(), "kind": kind, "sample": sample}
 
 
@@ -576,19 +650,19 @@ def run_reference(args):
         return
     from oracle import oracle as O
     O.build(reference=True)
-    kind = "reference" if O.reference_available() else "port"
+    kind = "reference" if O.reference_available() and args.method == "adjoint" else "port"
     w = make_workload(args)
     volume = np.full_like(w.volume, 0.1) if WORKLOADS[args.workload]["estimate"] == "const0.1" else w.volume
     for _ in range(args.warmup):
-        time_cpu(w, volume, 1.0, kind)
+        time_cpu(w, volume, 1.0, kind, args.method)
     vals = []
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        v, sample = time_cpu(w, volume, max(1.0, args.cpu_seconds / max(args.steps, 1)), kind)
+        v, sample = time_cpu(w, volume, max(1.0, args.cpu_seconds / max(args.steps, 1)), kind, args.method)
         vals.append(v)
     wall = time.perf_counter() - t0
     value = float(np.median(vals))
-    res = {"metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
+    res = {"metric": METRIC_FORWARD if args.method == "forward" else METRIC, "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": wall * 1e3 / max(args.steps, 1), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
            "config": {"workload": WORKLOADS[args.workload]["desc"], "sample": sample}, "impl": "reference",

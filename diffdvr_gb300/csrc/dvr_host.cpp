@@ -920,8 +920,9 @@ extern "C" int dvr_forward_variables_to_gradients(const DvrTensor* forward_varia
       for (int i = 0; i < 3; ++i) v.tf_s[i] = t.sizes[i] == 1 ? 0 : t.strides[i];
     }
     DeviceGuard guard(device);
+    const LaunchInfo li = launch_info(device);
     cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
-    after_launch(launch_forward_variables_to_gradients(v, s), s, "forward variables to gradients");
+    after_launch(launch_forward_variables_to_gradients(v, li, s), s, "forward variables to gradients");
   });
 }
 

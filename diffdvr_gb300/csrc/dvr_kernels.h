@@ -79,6 +79,6 @@ constexpr int kFwdMaxPass = 1024;
 template <int TF>
 cudaError_t launch_forward_gradients(const RenderParams& p, const FwdGradParams& g, int filter, int blend,
                                      const LaunchInfo& li, cudaStream_t s);
-cudaError_t launch_forward_variables_to_gradients(const FwdVarsParams& v, cudaStream_t s);
+cudaError_t launch_forward_variables_to_gradients(const FwdVarsParams& v, const LaunchInfo& li, cudaStream_t s);
 
 }  // namespace dvr
