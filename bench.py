@@ -63,6 +63,10 @@ WORKLOADS = {
         "desc": "large_mixed_512: 512^3 blobs+band-limited noise, linear TF R=16, 16 views 1024x1024 as per-pixel "
                 "rays, step 0.5 voxel, ray + volume + TF grads",
         "camera": "rays", "interval": 16, "estimate": "target", "res": 512, "views": 16, "image": 1024},
+    "preshaded_256": {
+        "desc": "preshaded_256: the tf_reconstruction_256 scene pre-shaded into a 4x256^3 colour volume, "
+                "8 views 256x256, step 0.25 voxel, colour-volume grad against the full volume from half of it",
+        "camera": "frame", "interval": 16, "estimate": "half", "res": 256, "views": 8, "image": 256},
     "plain_cpu_64": {
         "desc": "plain_cpu_64: 64^3 blobs, linear TF R=8, one 128x128 view, step 0.5 voxel, TF + volume grads",
         "camera": "frame", "interval": 16, "estimate": "target", "res": 64, "views": 1, "image": 128},
@@ -170,6 +174,8 @@ def make_workload(args):
         return scenes.large_mixed_512(seed=4, res=args.res, views=args.views, image=args.image)
     if args.workload == "plain_cpu_64":
         return scenes.plain_cpu_64(seed=0)
+    if args.workload == "preshaded_256":
+        return scenes.preshaded_256(seed=1, res=args.res, views=args.views, image=args.image)
     return scenes.tf_reconstruction_256(seed=1, res=args.res, views=args.views, image=args.image)
 
 
@@ -233,7 +239,12 @@ def run_gpu(args):
     B, H, W = w.ray_start.shape[0], w.height, w.width
     vol_target32 = torch.from_numpy(w.volume).to(dev)
     # the absorption reconstruction renders its estimate (0.1 everywhere) against the target's images
-    vol32 = torch.full_like(vol_target32, 0.1) if spec["estimate"] == "const0.1" else vol_target32
+    if spec["estimate"] == "const0.1":
+        vol32 = torch.full_like(vol_target32, 0.1)
+    elif spec["estimate"] == "half":  # the pre-shaded estimate: half the target's colour and absorption
+        vol32 = vol_target32 * 0.5
+    else:
+        vol32 = vol_target32
     sdt = {"bf16": torch.bfloat16, "f16": torch.float16, "f32": torch.float32}[args.storage]
     vol_s = vol32.to(sdt)
     tf = torch.from_numpy(w.tf).to(dev)
@@ -271,7 +282,7 @@ def run_gpu(args):
     out = pr.RendererOutputs(color, term, ckpt, K)
     pool = 0
     record_mode = "none"
-    if args.record != "none" and args.method == "adjoint":
+    if args.record != "none" and args.method == "adjoint" and w.filter_mode != 3:
         full = pr.Renderer.sample_density_size(inp_s, B)
         pool = full
         if args.record == "auto":
@@ -321,7 +332,7 @@ def run_gpu(args):
     # target image: the target volume (absorption reconstruction) or the TF perturbed
     target = torch.empty_like(color)
     pr.set_kernel_family("optimized")
-    if spec["estimate"] == "const0.1":
+    if spec["estimate"] in ("const0.1", "half"):
         t_inp = inputs(vol_target32.to(sdt), tf, cam)
     else:
         g = torch.Generator(device="cpu").manual_seed(3)
@@ -495,7 +506,7 @@ def run_gpu(args):
 
     # ---- roofline of the dominant kernel (compulsory HBM bytes per launch)
     peak, peak_kind = measured_peaks()
-    V = int(np.prod(w.volume.shape[1:]))
+    V = int(np.prod(w.volume.shape[1:])) * (4 if w.filter_mode == 3 else 1)  # pre-shaded: 4 channels
     P = B * H * W
     ck_written = int(torch.clamp((term.to(torch.int64) - 1) // K, min=0).clamp_max(slots).sum().item())
     s_v = vol_s.element_size()
@@ -523,6 +534,8 @@ def run_gpu(args):
     launches_per_step = 4 + (5 if record_kernel else 4)
     if forward_method:
         launches_per_step = 2  # forward-gradient march + contraction
+    elif w.filter_mode == 3:
+        launches_per_step = 2  # pre-shaded forward + adjoint
 
     result = {
         "metric": METRIC_FORWARD if forward_method else METRIC,
@@ -652,7 +665,8 @@ def run_reference(args):
     O.build(reference=True)
     kind = "reference" if O.reference_available() and args.method == "adjoint" else "port"
     w = make_workload(args)
-    volume = np.full_like(w.volume, 0.1) if WORKLOADS[args.workload]["estimate"] == "const0.1" else w.volume
+    est = WORKLOADS[args.workload]["estimate"]
+    volume = np.full_like(w.volume, 0.1) if est == "const0.1" else (w.volume * 0.5 if est == "half" else w.volume)
     for _ in range(args.warmup):
         time_cpu(w, volume, 1.0, kind, args.method)
     vals = []

@@ -129,6 +129,10 @@ SIGNATURES = {
     "dvr_forward_variables_to_gradients": (ctypes.c_int, [_P(DvrTensor), _P(DvrTensor),
                                                           _P(DvrForwardDifferencesSettings), _P(DvrAdjointOutputs),
                                                           ctypes.c_void_p]),
+    "dvr_preshade_volume": (ctypes.c_int, [_P(DvrTensor), _P(DvrTensor), ctypes.c_int32, _P(DvrTensor),
+                                           ctypes.c_void_p]),
+    "dvr_preshade_volume_adjoint": (ctypes.c_int, [_P(DvrTensor), _P(DvrTensor), ctypes.c_int32, _P(DvrTensor),
+                                                   _P(DvrTensor), ctypes.c_void_p]),
     "dvr_checkpoint_slots": (ctypes.c_int64, [ctypes.c_double, ctypes.c_double, ctypes.c_int32]),
     "dvr_last_error": (ctypes.c_char_p, []),
     "dvr_set_kernel_family": (ctypes.c_int, [ctypes.c_int32]),

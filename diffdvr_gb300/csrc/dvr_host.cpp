@@ -193,10 +193,19 @@ Checked check_inputs(const DvrRendererInputs& in) {
   p.X = int(volume.sizes[1]);
   p.Y = int(volume.sizes[2]);
   p.Z = int(volume.sizes[3]);
-  if (in.volume_filter_mode == DVR_FILTER_PRESHADED || in.tf_mode == DVR_TF_PRESHADED)
-    fail(DVR_E_UNSUPPORTED, "pre-shaded volumes are not supported by diffdvr_gb300");
-  if (in.volume_filter_mode != DVR_FILTER_NEAREST && in.volume_filter_mode != DVR_FILTER_TRILINEAR)
+  if (in.volume_filter_mode != DVR_FILTER_NEAREST && in.volume_filter_mode != DVR_FILTER_TRILINEAR &&
+      in.volume_filter_mode != DVR_FILTER_PRESHADED)
     fail(DVR_E_INVALID_ARGUMENT, "unknown volume filter enum value");
+  // renderer/renderer.cpp:72-80
+  if ((in.volume_filter_mode == DVR_FILTER_PRESHADED) != (in.tf_mode == DVR_TF_PRESHADED))
+    fail(DVR_E_INVALID_ARGUMENT, "if pre-shading is selected, both the filter mode and TF mode must be set to preshaded");
+  if (in.volume_filter_mode == DVR_FILTER_PRESHADED) {
+    if (volume.sizes[0] != 4)
+      fail(DVR_E_INVALID_ARGUMENT,
+           "In pre-shaded mode, the volume colors are encoded in the batch dimension of the volume. It must be 4, "
+           "but is " + std::to_string(volume.sizes[0]));
+    B = 1;
+  }
   if (p.X < 1 || p.Y < 1 || p.Z < 1) fail(DVR_E_INVALID_ARGUMENT, "volume must have at least one voxel per axis");
   {
     // offsets inside one batch entry are 32-bit, as the reference's accessors
@@ -327,6 +336,8 @@ Checked check_inputs(const DvrRendererInputs& in) {
     case DVR_TF_GAUSSIAN:
       check_size(tf, "tf", 2, 6);
       break;
+    case DVR_TF_PRESHADED:
+      break;  // any size, the TF is not read
     case DVR_TF_GAUSSIAN_LOG:
       fail(DVR_E_UNSUPPORTED, "TFGaussianLog is not supported by diffdvr_gb300");
     default:
@@ -398,6 +409,8 @@ void check_outputs(const DvrRendererOutputs& out, Checked& c, bool forward) {
   const bool has_off = out.sample_offset.ndim >= 0 && out.sample_offset.data != nullptr;
   if (has_dens != has_off) fail(DVR_E_INVALID_ARGUMENT, "sample_density and sample_offset go together");
   if (has_dens) {
+    if (c.filter == DVR_FILTER_PRESHADED)
+      fail(DVR_E_UNSUPPORTED, "sample_density records densities; pre-shaded volumes have none");
     if (!p.ckpt.p) fail(DVR_E_INVALID_ARGUMENT, "sample_density needs a checkpoint buffer");
     const DvrTensor& d = out.sample_density;
     check_dim(d, "sample_density", 1);
@@ -440,7 +453,8 @@ AdjointParams check_adjoint(const DvrTensor& adj_color, const DvrAdjointOutputs&
     const DvrTensor& t = o.adj_volume;
     check_dim(t, "adj_volume", 4);
     check_device(t, "adj_volume", c.device);
-    check_batch(t, "adj_volume", p.B);
+    if (c.filter == DVR_FILTER_PRESHADED) check_size(t, "adj_volume", 0, 4);  // renderer/renderer.cpp:277-279
+    else check_batch(t, "adj_volume", p.B);
     check_size(t, "adj_volume", 1, p.X);
     check_size(t, "adj_volume", 2, p.Y);
     check_size(t, "adj_volume", 3, p.Z);
@@ -506,6 +520,8 @@ AdjointParams check_adjoint(const DvrTensor& adj_color, const DvrAdjointOutputs&
     check_dtype(t, "adj_viewport", DVR_FLOAT32);
     if (p.camera_mode != DVR_CAMERA_REFERENCE_FRAME)
       fail(DVR_E_INVALID_ARGUMENT, "viewport derivatives require cameraMode == ReferenceFrame");
+    if (c.filter == DVR_FILTER_PRESHADED)
+      fail(DVR_E_UNSUPPORTED, "viewport derivatives are not available for pre-shaded volumes");
     if (p.B > kMaxViewportBatch)
       fail(DVR_E_UNSUPPORTED, "viewport derivatives support batches of at most 256 views");
     a.adj_viewport = out_view(t, true);
@@ -555,6 +571,7 @@ int guarded(F&& fn) {
 }
 
 cudaError_t dispatch_forward(const Checked& c, bool plain, const LaunchInfo& li, cudaStream_t s) {
+  if (c.filter == DVR_FILTER_PRESHADED) return launch_preshaded_forward(c.p, c.blend, plain, li, s);
   switch (c.tf_mode) {
     case DVR_TF_IDENTITY:
       return plain ? launch_plain_forward<0>(c.p, c.filter, c.blend, li, s)
@@ -573,6 +590,8 @@ cudaError_t dispatch_forward(const Checked& c, bool plain, const LaunchInfo& li,
 
 cudaError_t dispatch_adjoint(const Checked& c, const AdjointParams& a, bool plain, const LaunchInfo& li,
                              cudaStream_t s) {
+  // the plain family keeps the reference's position and step-size adjoints
+  if (c.filter == DVR_FILTER_PRESHADED) return launch_preshaded_adjoint(c.p, a, c.blend, !plain, li, s);
   switch (c.tf_mode) {
     case DVR_TF_IDENTITY:
       return plain ? launch_plain_adjoint<0>(c.p, a, c.filter, c.blend, li, s)
@@ -591,6 +610,7 @@ cudaError_t dispatch_adjoint(const Checked& c, const AdjointParams& a, bool plai
 
 cudaError_t dispatch_adjoint_into(const Checked& c, const AdjointParams& a, const LaunchInfo& li,
                                   const CallerScratch& sc, cudaStream_t s) {
+  if (c.filter == DVR_FILTER_PRESHADED) return launch_preshaded_adjoint(c.p, a, c.blend, true, li, s);
   switch (c.tf_mode) {
     case DVR_TF_IDENTITY: return launch_fast_adjoint_into<0>(c.p, a, c.filter, c.blend, li, sc, s);
     case DVR_TF_TEXTURE: return launch_fast_adjoint_into<1>(c.p, a, c.filter, c.blend, li, sc, s);
@@ -710,6 +730,8 @@ extern "C" int dvr_render_forward_batched(const DvrRendererInputs* inputs, const
     std::vector<Checked> cs(n);
     for (int i = 0; i < n; ++i) {
       cs[i] = check_inputs(inputs[i]);
+      if (cs[i].filter == DVR_FILTER_PRESHADED)
+        fail(DVR_E_UNSUPPORTED, "pre-shaded volumes are rendered by the single-instance entry points");
       check_outputs(outputs[i], cs[i], true);
       if (cs[i].p.dens) fail(DVR_E_UNSUPPORTED, "the batched entry points do not record sample_density");
       if (i > 0 && (cs[i].filter != cs[0].filter || cs[i].tf_mode != cs[0].tf_mode || cs[i].blend != cs[0].blend ||
@@ -739,6 +761,8 @@ extern "C" int dvr_render_adjoint_batched(const DvrRendererInputs* inputs,
     std::vector<AdjointParams> as(n);
     for (int i = 0; i < n; ++i) {
       cs[i] = check_inputs(inputs[i]);
+      if (cs[i].filter == DVR_FILTER_PRESHADED)
+        fail(DVR_E_UNSUPPORTED, "pre-shaded volumes are rendered by the single-instance entry points");
       check_outputs(outputs_from_forward[i], cs[i], false);
       if (cs[i].p.dens) fail(DVR_E_UNSUPPORTED, "the batched entry points do not record sample_density");
       as[i] = check_adjoint(adj_colors[i], adj_outputs[i], cs[i]);
@@ -771,6 +795,8 @@ extern "C" int dvr_render_forward_gradients(const DvrRendererInputs* inputs,
     if (!inputs || !settings || !outputs || !gradients_out)
       fail(DVR_E_INVALID_ARGUMENT, "arguments must not be NULL");
     Checked c = check_inputs(*inputs);
+    if (c.filter == DVR_FILTER_PRESHADED)
+      fail(DVR_E_UNSUPPORTED, "forward derivatives are not available for pre-shaded volumes");
     const DvrForwardDifferencesSettings& fs = *settings;
     if (fs.D <= 0) fail(DVR_E_INVALID_ARGUMENT, "number of derivatives must be positive");
     FwdGradParams g{};
@@ -923,6 +949,102 @@ extern "C" int dvr_forward_variables_to_gradients(const DvrTensor* forward_varia
     const LaunchInfo li = launch_info(device);
     cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
     after_launch(launch_forward_variables_to_gradients(v, li, s), s, "forward variables to gradients");
+  });
+}
+
+// ---- TFUtils::preshadeVolume (renderer/tf_utils.cpp:173-249) ----
+namespace dvr {
+namespace {
+PreshadeParams check_preshade(const DvrTensor& density, const DvrTensor& tf, int tf_mode, int& device) {
+  PreshadeParams q{};
+  check_dim(density, "densityVolume", 4);
+  if (density.device_type != DVR_DEVICE_CUDA)
+    fail(DVR_E_INVALID_ARGUMENT, "densityVolume is a CPU tensor: diffdvr_gb300 runs on CUDA devices only");
+  device = density.device_index;
+  check_dtype(density, "densityVolume", DVR_FLOAT32);
+  check_size(density, "densityVolume", 0, 1);
+  q.X = int(density.sizes[1]);
+  q.Y = int(density.sizes[2]);
+  q.Z = int(density.sizes[3]);
+  check_dim(tf, "tf", 3);
+  check_device(tf, "tf", device);
+  check_size(tf, "tf", 0, 1);
+  check_dtype(tf, "tf", DVR_FLOAT32);
+  switch (tf_mode) {
+    case DVR_TF_IDENTITY:
+      check_size(tf, "tf", 1, 1);
+      check_size(tf, "tf", 2, 2);
+      break;
+    case DVR_TF_TEXTURE:
+      check_size(tf, "tf", 2, 4);
+      break;
+    case DVR_TF_LINEAR:
+      check_size(tf, "tf", 2, 5);
+      if (tf.sizes[1] <= 1) fail(DVR_E_INVALID_ARGUMENT, "tensor 'tf' must have at least two control points in TFLinear-mode");
+      break;
+    case DVR_TF_GAUSSIAN:
+      check_size(tf, "tf", 2, 6);
+      break;
+    case DVR_TF_GAUSSIAN_LOG:
+      fail(DVR_E_UNSUPPORTED, "TFGaussianLog is not supported by diffdvr_gb300");
+    default:
+      fail(DVR_E_INVALID_ARGUMENT, "unknown tf enum value: " + std::to_string(tf_mode));
+  }
+  if (tf.sizes[1] < 1) fail(DVR_E_INVALID_ARGUMENT, "tensor 'tf' must have at least one control point");
+  q.R = int(tf.sizes[1]);
+  q.C = int(tf.sizes[2]);
+  q.density = static_cast<const float*>(density.data);
+  for (int i = 0; i < 4; ++i) q.d_s[i] = density.strides[i];
+  q.tf = static_cast<const float*>(tf.data);
+  for (int i = 0; i < 3; ++i) q.tf_s[i] = tf.strides[i];
+  return q;
+}
+
+void check_volume_like(const DvrTensor& t, const char* name, int channels, const PreshadeParams& q, int device) {
+  check_dim(t, name, 4);
+  check_device(t, name, device);
+  check_size(t, name, 0, channels);
+  check_size(t, name, 1, q.X);
+  check_size(t, name, 2, q.Y);
+  check_size(t, name, 3, q.Z);
+  check_dtype(t, name, DVR_FLOAT32);
+}
+}  // namespace
+}  // namespace dvr
+
+extern "C" int dvr_preshade_volume(const DvrTensor* density, const DvrTensor* tf, int32_t tf_mode,
+                                   const DvrTensor* color_out, void* cuda_stream) {
+  return guarded([&] {
+    if (!density || !tf || !color_out) fail(DVR_E_INVALID_ARGUMENT, "arguments must not be NULL");
+    int device = 0;
+    PreshadeParams q = check_preshade(*density, *tf, tf_mode, device);
+    check_volume_like(*color_out, "color", 4, q, device);
+    q.out = static_cast<float*>(color_out->data);
+    for (int i = 0; i < 4; ++i) q.o_s[i] = color_out->strides[i];
+    DeviceGuard guard(device);
+    const LaunchInfo li = launch_info(device);
+    cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+    after_launch(launch_preshade_volume(q, tf_mode, false, li, s), s, "preshade volume");
+  });
+}
+
+extern "C" int dvr_preshade_volume_adjoint(const DvrTensor* density, const DvrTensor* tf, int32_t tf_mode,
+                                           const DvrTensor* adj_color, const DvrTensor* adj_density,
+                                           void* cuda_stream) {
+  return guarded([&] {
+    if (!density || !tf || !adj_color || !adj_density) fail(DVR_E_INVALID_ARGUMENT, "arguments must not be NULL");
+    int device = 0;
+    PreshadeParams q = check_preshade(*density, *tf, tf_mode, device);
+    check_volume_like(*adj_color, "adj_color", 4, q, device);
+    check_volume_like(*adj_density, "adj_density", 1, q, device);
+    q.adj_color = static_cast<const float*>(adj_color->data);
+    for (int i = 0; i < 4; ++i) q.a_s[i] = adj_color->strides[i];
+    q.out = static_cast<float*>(adj_density->data);
+    for (int i = 0; i < 4; ++i) q.o_s[i] = adj_density->strides[i];
+    DeviceGuard guard(device);
+    const LaunchInfo li = launch_info(device);
+    cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+    after_launch(launch_preshade_volume(q, tf_mode, true, li, s), s, "preshade volume adjoint");
   });
 }
 

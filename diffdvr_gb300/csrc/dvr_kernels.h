@@ -70,6 +70,18 @@ template <int TF>
 cudaError_t launch_fast_adjoint_into(const RenderParams& p, const AdjointParams& a, int filter, int blend,
                                      const LaunchInfo& li, const CallerScratch& sc, cudaStream_t s);
 
+// Pre-shaded volumes (4 x X x Y x Z colour/absorption).  Forward: the
+// reference's one thread per ray (plain) or one warp per ray; adjoint: one
+// thread per ray with blend inversion, the reference's position and
+// step-size adjoints (exact = false) or the exact ones (exact = true).
+cudaError_t launch_preshaded_forward(const RenderParams& p, int blend, bool plain, const LaunchInfo& li,
+                                     cudaStream_t s);
+cudaError_t launch_preshaded_adjoint(const RenderParams& p, const AdjointParams& a, int blend, bool exact,
+                                     const LaunchInfo& li, cudaStream_t s);
+
+cudaError_t launch_preshade_volume(const PreshadeParams& q, int tf_mode, bool adjoint, const LaunchInfo& li,
+                                   cudaStream_t s);
+
 // Forward-mode derivatives: blocks of kFwdThreads (one ray per warp at a
 // time), one launch per range of at most kFwdMaxPass derivative indices
 // (g.d0, g.dn); each warp holds its ray's dn x 4 Jacobian block in shared

@@ -110,4 +110,19 @@ struct FwdVarsParams {
   int64_t tf_s[3];
 };
 
+// TFUtils::preshadeVolume: density [0][x][y][z] -> colour [c][x][y][z]
+// (forward), or adj_color [c][x][y][z] -> d loss / d density [0][x][y][z]
+// (adjoint, written to out).  TF [0][r][c] in float32.
+struct PreshadeParams {
+  int32_t X, Y, Z, R, C, pad_;
+  const float* density;
+  int64_t d_s[4];
+  const float* tf;
+  int64_t tf_s[3];
+  const float* adj_color;
+  int64_t a_s[4];
+  float* out;
+  int64_t o_s[4];
+};
+
 }  // namespace dvr

@@ -1,0 +1,80 @@
+// Launchers of the pre-shaded kernels (all blend modes and volume storage types).
+#include "dvr_preshaded.cuh"
+
+namespace dvr {
+
+namespace {
+template <typename K>
+int grid_for(K kernel, int block, int64_t work, const LaunchInfo& li) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0) != cudaSuccess || per_sm < 1) per_sm = 1;
+  const int64_t need = (work + block - 1) / block;
+  const int64_t cap = int64_t(per_sm) * li.num_sms;
+  return int(need < cap ? (need > 0 ? need : 1) : cap);
+}
+
+template <int BLEND, typename VT>
+cudaError_t forward_go(const RenderParams& p, const LaunchInfo& li, cudaStream_t s) {
+  auto kernel = preshaded_forward_kernel<BLEND, VT>;
+  cudaError_t err = cudaSuccess;
+  int* counter = acquire_counter(li.device, s, err);
+  if (err != cudaSuccess) return err;
+  const int64_t rays = int64_t(p.B) * p.H * p.W;
+  // one warp per ray: rays x 32 threads of work
+  kernel<<<grid_for(kernel, kFastThreads, rays * 32, li), kFastThreads, 0, s>>>(p, counter);
+  return cudaGetLastError();
+}
+
+template <int BLEND, typename VT, bool EXACT>
+cudaError_t adjoint_go(const RenderParams& p, const AdjointParams& a, const LaunchInfo& li, cudaStream_t s) {
+  const int64_t rays = int64_t(p.B) * p.H * p.W;
+  auto run = [&](auto kernel) {
+    kernel<<<grid_for(kernel, 256, rays, li), 256, 0, s>>>(p, a);
+    return cudaGetLastError();
+  };
+  return a.has_volume ? run(preshaded_adjoint_kernel<BLEND, VT, true, EXACT>)
+                      : run(preshaded_adjoint_kernel<BLEND, VT, false, EXACT>);
+}
+
+template <typename VT>
+cudaError_t adjoint_vt(const RenderParams& p, const AdjointParams& a, int blend, bool exact, const LaunchInfo& li,
+                       cudaStream_t s) {
+  if (blend == kBeerLambert)
+    return exact ? adjoint_go<kBeerLambert, VT, true>(p, a, li, s) : adjoint_go<kBeerLambert, VT, false>(p, a, li, s);
+  return exact ? adjoint_go<kAlphaBlend, VT, true>(p, a, li, s) : adjoint_go<kAlphaBlend, VT, false>(p, a, li, s);
+}
+}  // namespace
+
+cudaError_t launch_preshaded_forward(const RenderParams& p, int blend, bool plain, const LaunchInfo& li,
+                                     cudaStream_t s) {
+  const int64_t rays = int64_t(p.B) * p.H * p.W;
+  if (rays == 0) return cudaSuccess;
+  if (plain) {
+    auto run = [&](auto kernel) {
+      kernel<<<grid_for(kernel, 256, rays, li), 256, 0, s>>>(p);
+      return cudaGetLastError();
+    };
+    return blend == kBeerLambert ? run(preshaded_plain_forward_kernel<kBeerLambert>)
+                                 : run(preshaded_plain_forward_kernel<kAlphaBlend>);
+  }
+  switch (p.vol_storage) {
+    case kF16: return blend == kBeerLambert ? forward_go<kBeerLambert, __half>(p, li, s)
+                                            : forward_go<kAlphaBlend, __half>(p, li, s);
+    case kBF16: return blend == kBeerLambert ? forward_go<kBeerLambert, __nv_bfloat16>(p, li, s)
+                                             : forward_go<kAlphaBlend, __nv_bfloat16>(p, li, s);
+    default: return blend == kBeerLambert ? forward_go<kBeerLambert, float>(p, li, s)
+                                          : forward_go<kAlphaBlend, float>(p, li, s);
+  }
+}
+
+cudaError_t launch_preshaded_adjoint(const RenderParams& p, const AdjointParams& a, int blend, bool exact,
+                                     const LaunchInfo& li, cudaStream_t s) {
+  if (int64_t(p.B) * p.H * p.W == 0) return cudaSuccess;
+  switch (p.vol_storage) {
+    case kF16: return adjoint_vt<__half>(p, a, blend, exact, li, s);
+    case kBF16: return adjoint_vt<__nv_bfloat16>(p, a, blend, exact, li, s);
+    default: return adjoint_vt<float>(p, a, blend, exact, li, s);
+  }
+}
+
+}  // namespace dvr

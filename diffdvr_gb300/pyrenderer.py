@@ -432,6 +432,42 @@ class Renderer:
 
 
 # --------------------------------------------------------------------- module functions
+class _PreshadeFunction(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, density, tf, tf_mode):
+        lib = _abi.load()
+        out = torch.empty((4,) + tuple(density.shape[1:]), dtype=torch.float32, device=density.device)
+        cd, ct, co = _tensor(density, "density"), _tensor(tf, "tf"), _tensor(out, "color")
+        _abi.check(lib.dvr_preshade_volume(ctypes.byref(cd), ctypes.byref(ct), int(tf_mode), ctypes.byref(co),
+                                           _stream_of(density)))
+        ctx.save_for_backward(density, tf)
+        ctx.tf_mode = int(tf_mode)
+        return out
+
+    @staticmethod
+    def backward(ctx, grad_color):
+        density, tf = ctx.saved_tensors
+        lib = _abi.load()
+        adj = torch.empty_like(density)
+        cd, ct = _tensor(density, "density"), _tensor(tf, "tf")
+        ca, co = _tensor(grad_color.contiguous().float(), "adj_color"), _tensor(adj, "adj_density")
+        _abi.check(lib.dvr_preshade_volume_adjoint(ctypes.byref(cd), ctypes.byref(ct), ctx.tf_mode, ctypes.byref(ca),
+                                                   ctypes.byref(co), _stream_of(density)))
+        return adj, None, None
+
+
+class TFUtils:
+    """The pre-shading entry of the reference's TFUtils (renderer/tf_utils.h:125-140,
+    bindings/bindings.cpp:570-581)."""
+
+    @staticmethod
+    def preshade_volume(density: torch.Tensor, tf: torch.Tensor, tfMode) -> torch.Tensor:
+        """Pre-shades a density volume of shape 1*X*Y*Z with the transfer
+        function into a colour volume of shape 4*X*Y*Z (r, g, b, opacity),
+        differentiable with respect to the density."""
+        return _PreshadeFunction.apply(density, tf, int(tfMode))
+
+
 def set_kernel_family(family: str) -> str:
     """'optimized' (default) or 'plain' (one thread per ray, reference semantics)."""
     code = {"plain": _abi.DVR_KERNELS_PLAIN, "optimized": _abi.DVR_KERNELS_OPTIMIZED}[family]

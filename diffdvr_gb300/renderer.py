@@ -109,14 +109,20 @@ class _RendererFunction(torch.autograd.Function):
         inputs.tf = tf
         inputs.volume = volume
 
-        B = max([(1 if t is None else t.shape[0]) for t in (camera_matrix, camera_ray_start, camera_ray_dir, tf,
-                                                            volume)])
+        # a pre-shaded volume holds its four channels in the first dimension
+        # (pytests/diffdvr/renderer.py:110-112)
+        batched = [camera_matrix, camera_ray_start, camera_ray_dir, tf]
+        if inputs.volume_filter_mode != pyrenderer.VolumeFilterMode.Preshaded:
+            batched.append(volume)
+        B = max([(1 if t is None else t.shape[0]) for t in batched])
         W, H = inputs.screen_size.x, inputs.screen_size.y
         color = torch.empty(B, H, W, 4, dtype=torch.float32, device=volume.device)
         term = torch.empty(B, H, W, dtype=torch.int32, device=volume.device)
         needs_grad = any(ctx.needs_input_grad[:5])
         ckpt = None
-        if needs_grad and checkpoint_interval > 0:
+        # pre-shaded volumes take the adjoint that inverts the blend: no checkpoints, no record
+        preshaded = inputs.volume_filter_mode == pyrenderer.VolumeFilterMode.Preshaded
+        if needs_grad and checkpoint_interval > 0 and not preshaded:
             slots = pyrenderer.Renderer.checkpoint_slots(inputs, checkpoint_interval)
             ckpt = torch.empty(B, H, W, slots, dtype=torch.float32, device=volume.device)
         outputs = pyrenderer.RendererOutputs(color, term, ckpt, checkpoint_interval)

@@ -141,11 +141,11 @@ def generate_rays(viewport: np.ndarray, fov_y: float, W: int, H: int, dtype=np.f
 class Workload:
     """A complete set of renderer inputs in the reference layout."""
     name: str
-    volume: np.ndarray          # B*X*Y*Z
+    volume: np.ndarray          # B*X*Y*Z (pre-shaded: 4*X*Y*Z colour and absorption)
     tf: np.ndarray              # B*R*C
-    tf_mode: int                # 0 identity, 1 texture, 2 linear, 3 gaussian
+    tf_mode: int                # 0 identity, 1 texture, 2 linear, 3 gaussian, 5 pre-shaded
     blend_mode: int             # 0 Beer-Lambert, 1 alpha
-    filter_mode: int            # 0 nearest, 1 trilinear
+    filter_mode: int            # 0 nearest, 1 trilinear, 3 pre-shaded
     ray_start: np.ndarray       # B*H*W*3
     ray_dir: np.ndarray         # B*H*W*3
     step_size: float
@@ -171,6 +171,32 @@ def tf_reconstruction_256(seed: int = 1, res: int = 256, views: int = 8, image: 
     rs, rd = generate_rays(vp, fov, image, image)
     return Workload("tf_reconstruction_256", vol, tf, 1, 0, 1, rs, rd, 0.25 / (res - 1), image, image,
                     viewport=vp, fov_y=fov, grads=("tf",))
+
+
+def preshade_texture(density: np.ndarray, tf: np.ndarray) -> np.ndarray:
+    """Colour volume 4*X*Y*Z of a density volume 1*X*Y*Z through a texture TF
+    (batch entry 0): texel centres at (i + 0.5) / R, clamped neighbours, as
+    the texture TF evaluates a sample (renderer/renderer_tf.cuh:160-171)."""
+    R = tf.shape[1]
+    d = density[0].astype(np.float32) * np.float32(R) - np.float32(0.5)
+    di = np.floor(d).astype(np.int64)
+    f = (d - di).astype(np.float32)
+    t = tf[0].astype(np.float32)
+    a = t[np.clip(di, 0, R - 1)]
+    b = t[np.clip(di + 1, 0, R - 1)]
+    out = a + f[..., None] * (b - a)
+    return np.ascontiguousarray(np.moveaxis(out, -1, 0)).astype(np.float32)
+
+
+def preshaded_256(seed: int = 1, res: int = 256, views: int = 8, image: int = 256) -> Workload:
+    """The TF-reconstruction scene pre-shaded: its density volume through its
+    texture TF gives a 4*256^3 colour volume (r, g, b, absorption), rendered
+    with the pre-shaded filter and TF modes; 8 views at 256^2, step 0.25
+    voxel, gradient with respect to the colour volume."""
+    w = tf_reconstruction_256(seed, res, views, image)
+    rgba = preshade_texture(w.volume, w.tf)
+    return Workload("preshaded_256", rgba, np.zeros((1, 1, 1), np.float32), 5, 0, 3, w.ray_start, w.ray_dir,
+                    w.step_size, image, image, viewport=w.viewport, fov_y=w.fov_y, grads=("volume",))
 
 
 def plain_cpu_64(seed: int = 0) -> Workload:

@@ -17,6 +17,9 @@
  *                     (B) 3 3 reference frame (eye, right, up) + fovY
  *   step_size         (B) (H) (W)
  *   tf                (B) R C, C = 2 identity, 4 texture, 5 linear, 6 Gaussian
+ *   pre-shaded volume 4 X Y Z              (filter and TF mode Preshaded: r, g,
+ *                     b, absorption per voxel, shared by all batch entries;
+ *                     the TF is not read; volume gradient 4 X Y Z)
  *   color             B H W 4              output (r, g, b, alpha)
  *   termination_index B H W int32          output
  * Gradient outputs are accumulated with atomics and must be zero-initialised
@@ -249,6 +252,18 @@ int dvr_render_forward_gradients(const DvrRendererInputs* inputs, const DvrForwa
 int dvr_forward_variables_to_gradients(const DvrTensor* forward_variables, const DvrTensor* adj_color,
                                        const DvrForwardDifferencesSettings* settings,
                                        const DvrAdjointOutputs* adj_outputs, void* cuda_stream);
+/* Pre-shading: the colour volume color_out (4*X*Y*Z float32: r, g, b,
+ * absorption) of a density volume (1*X*Y*Z float32) through the TF (1*R*C
+ * float32) of mode tf_mode, for rendering with the pre-shaded filter and TF
+ * modes (volume = color_out).  The adjoint writes d loss / d density
+ * (1*X*Y*Z) for the colour-volume adjoint adj_color (4*X*Y*Z); there is no
+ * TF gradient, as in the reference.
+ * Replace renderer::TFUtils::preshadeVolume and its autograd backward
+ * (renderer/tf_utils.h:125-140, renderer/tf_utils.cpp:173-249). */
+int dvr_preshade_volume(const DvrTensor* density, const DvrTensor* tf, int32_t tf_mode, const DvrTensor* color_out,
+                        void* cuda_stream);
+int dvr_preshade_volume_adjoint(const DvrTensor* density, const DvrTensor* tf, int32_t tf_mode,
+                                const DvrTensor* adj_color, const DvrTensor* adj_density, void* cuda_stream);
 /* Number of checkpoint slots per ray (the C of DvrRendererOutputs.checkpoints)
  * for rays of at most max_ray_length world units inside the box (the box
  * diagonal bounds it) marched with steps of at least min_step_size, at the

@@ -484,11 +484,108 @@ static inline v3 volume_pos(const RaySetup* r, real_t t) {
 }
 
 static int check_modes(const OracleInputs* in) {
-  if (in->filter_mode < 0 || in->filter_mode > 1) return 2;
+  /* pre-shaded: filter 3 together with TF 5 (renderer/renderer.cpp:72-80) */
+  const int preshaded = in->filter_mode == 3;
+  if (preshaded != (in->tf_mode == 5)) return 2;
+  if (!preshaded && (in->filter_mode < 0 || in->filter_mode > 1)) return 2;
   if (in->camera_mode < 0 || in->camera_mode > 2) return 2;
-  if (in->tf_mode < 0 || in->tf_mode > 3) return 2;
+  if (!preshaded && (in->tf_mode < 0 || in->tf_mode > 3)) return 2;
   if (in->blend_mode < 0 || in->blend_mode > 1) return 2;
+  if (preshaded && in->volume.sizes[0] != 4) return 2;
   return 0;
+}
+
+/* ---- pre-shaded volumes (renderer/renderer_interpolation.cuh:393-579,
+ *      renderer/renderer_tf.cuh:818-854): the volume is 4 X Y Z, the colour
+ *      and absorption channels in its first dimension, shared by all batch
+ *      entries; each channel is interpolated trilinearly and the TF passes
+ *      the result through. ---- */
+static int g_exact_preshaded = 0;
+/* 0 (default): the reference's position adjoint, whose z term is summed
+ * with the y weights' selector (renderer/renderer_interpolation.cuh:543-548);
+ * 1: the exact trilinear z derivative. */
+void oracle_set_exact_preshaded(int exact) { g_exact_preshaded = exact; }
+
+typedef struct {
+  const OracleTensor* vol;
+  OracleTensor* adj;
+  int has_adj;
+  int X, Y, Z;
+  int li[3];
+  real_t dens[4][8];
+  real_t acc[4][8];
+  real_t fpos[3];
+} RgbaSampler;
+
+static void rgba_corners(const RgbaSampler* s, const int* ip, real_t d[4][8]) {
+  const int lx = clampi(ip[0], 0, s->X - 1), hx = clampi(ip[0] + 1, 0, s->X - 1);
+  const int ly = clampi(ip[1], 0, s->Y - 1), hy = clampi(ip[1] + 1, 0, s->Y - 1);
+  const int lz = clampi(ip[2], 0, s->Z - 1), hz = clampi(ip[2] + 1, 0, s->Z - 1);
+  for (int c = 0; c < 4; ++c) {
+    d[c][0] = *at4(s->vol, c, lx, ly, lz); d[c][1] = *at4(s->vol, c, lx, ly, hz);
+    d[c][2] = *at4(s->vol, c, lx, hy, lz); d[c][3] = *at4(s->vol, c, lx, hy, hz);
+    d[c][4] = *at4(s->vol, c, hx, ly, lz); d[c][5] = *at4(s->vol, c, hx, ly, hz);
+    d[c][6] = *at4(s->vol, c, hx, hy, lz); d[c][7] = *at4(s->vol, c, hx, hy, hz);
+  }
+}
+
+static v4 rgba_forward(const RgbaSampler* s, v3 p) {
+  int ip[3] = {(int)p.x, (int)p.y, (int)p.z};
+  real_t d[4][8], f[3] = {p.x - (real_t)ip[0], p.y - (real_t)ip[1], p.z - (real_t)ip[2]};
+  rgba_corners(s, ip, d);
+  return mk4(trilerp(d[0], f), trilerp(d[1], f), trilerp(d[2], f), trilerp(d[3], f));
+}
+
+static void rgba_flush(RgbaSampler* s) {
+  if (!s->has_adj || s->li[0] < 0) return;
+  const int lx = clampi(s->li[0], 0, s->X - 1), hx = clampi(s->li[0] + 1, 0, s->X - 1);
+  const int ly = clampi(s->li[1], 0, s->Y - 1), hy = clampi(s->li[1] + 1, 0, s->Y - 1);
+  const int lz = clampi(s->li[2], 0, s->Z - 1), hz = clampi(s->li[2] + 1, 0, s->Z - 1);
+  for (int c = 0; c < 4; ++c) {
+    atomic_add(at4(s->adj, c, lx, ly, lz), s->acc[c][0]);
+    atomic_add(at4(s->adj, c, lx, ly, hz), s->acc[c][1]);
+    atomic_add(at4(s->adj, c, lx, hy, lz), s->acc[c][2]);
+    atomic_add(at4(s->adj, c, lx, hy, hz), s->acc[c][3]);
+    atomic_add(at4(s->adj, c, hx, ly, lz), s->acc[c][4]);
+    atomic_add(at4(s->adj, c, hx, ly, hz), s->acc[c][5]);
+    atomic_add(at4(s->adj, c, hx, hy, lz), s->acc[c][6]);
+    atomic_add(at4(s->adj, c, hx, hy, hz), s->acc[c][7]);
+    for (int i = 0; i < 8; ++i) s->acc[c][i] = 0;
+  }
+}
+
+static v4 rgba_adjoint_fetch(RgbaSampler* s, v3 p) {
+  int ip[3] = {(int)p.x, (int)p.y, (int)p.z};
+  if (ip[0] != s->li[0] || ip[1] != s->li[1] || ip[2] != s->li[2]) {
+    rgba_flush(s);
+    s->li[0] = ip[0]; s->li[1] = ip[1]; s->li[2] = ip[2];
+    rgba_corners(s, ip, s->dens);
+  }
+  s->fpos[0] = p.x - (real_t)ip[0];
+  s->fpos[1] = p.y - (real_t)ip[1];
+  s->fpos[2] = p.z - (real_t)ip[2];
+  return mk4(trilerp(s->dens[0], s->fpos), trilerp(s->dens[1], s->fpos), trilerp(s->dens[2], s->fpos),
+             trilerp(s->dens[3], s->fpos));
+}
+
+/* adjoint of the four trilinear channels; returns d(colour)/d(volumePos) . adj */
+static v3 rgba_adjoint(RgbaSampler* s, v4 adj) {
+  const real_t c[3] = {s->fpos[0], s->fpos[1], s->fpos[2]};
+  const real_t f[3] = {1 - c[0], 1 - c[1], 1 - c[2]};
+  real_t adj_c[3] = {0, 0, 0}, adj_f[3] = {0, 0, 0};
+  const real_t a[4] = {adj.x, adj.y, adj.z, adj.w};
+  static const int order[8] = {0, 4, 2, 6, 1, 5, 3, 7};
+  for (int ch = 0; ch < 4; ++ch)
+    for (int k = 0; k < 8; ++k) {
+      const int idx = order[k];
+      const int hx = (idx >> 2) & 1, hy = (idx >> 1) & 1, hz = idx & 1;
+      const real_t wx = hx ? c[0] : f[0], wy = hy ? c[1] : f[1], wz = hz ? c[2] : f[2];
+      if (s->has_adj) s->acc[ch][idx] += a[ch] * (wx * wy * wz);
+      (hx ? adj_c : adj_f)[0] += a[ch] * s->dens[ch][idx] * wy * wz;
+      (hy ? adj_c : adj_f)[1] += a[ch] * s->dens[ch][idx] * wx * wz;
+      (g_exact_preshaded ? (hz ? adj_c : adj_f) : (hy ? adj_c : adj_f))[2] += a[ch] * s->dens[ch][idx] * wx * wy;
+    }
+  return mk3(adj_c[0] - adj_f[0], adj_c[1] - adj_f[1], adj_c[2] - adj_f[2]);
 }
 
 int oracle_real_size(void) { return (int)sizeof(real_t); }
@@ -507,14 +604,21 @@ int oracle_forward(const OracleInputs* in, OracleTensor* color, OracleTensor* te
     RaySetup r;
     ray_setup(in, x, y, b, &r);
     Sampler s = {b, (int)in->volume.sizes[1], (int)in->volume.sizes[2], (int)in->volume.sizes[3], &in->volume};
+    RgbaSampler rs = {&in->volume, NULL, 0, s.X, s.Y, s.Z};
     v4 acc = mk4(0, 0, 0, 0);
     int k;
     for (k = 0;; ++k) {
       const real_t t = r.tmin + k * r.step;
       if (t > r.tmax) break;
       if (acc.w > early_out) break;
-      const real_t density = sample_forward(&s, in->filter_mode, volume_pos(&r, t));
-      acc = blend(in->blend_mode, acc, tf_eval(in, b, density), r.step);
+      v4 cur;
+      if (in->filter_mode == 3) {
+        cur = rgba_forward(&rs, volume_pos(&r, t));
+      } else {
+        const real_t density = sample_forward(&s, in->filter_mode, volume_pos(&r, t));
+        cur = tf_eval(in, b, density);
+      }
+      acc = blend(in->blend_mode, acc, cur, r.step);
     }
     *at4(color, b, y, x, 0) = acc.x;
     *at4(color, b, y, x, 1) = acc.y;
@@ -551,15 +655,31 @@ int oracle_adjoint(const OracleInputs* in, const OracleTensor* color, const Orac
     s.li[0] = s.li[1] = s.li[2] = -1;
     for (int q = 0; q < 8; ++q) s.acc[q] = s.dens[q] = 0;
     s.nearest_val = s.nearest_acc = 0;
+    RgbaSampler rs;
+    rs.vol = &in->volume;
+    rs.adj = &out->adj_volume;
+    rs.has_adj = out->has_volume;
+    rs.X = s.X; rs.Y = s.Y; rs.Z = s.Z;
+    rs.li[0] = rs.li[1] = rs.li[2] = -1;
+    for (int c = 0; c < 4; ++c)
+      for (int q = 0; q < 8; ++q) rs.acc[c][q] = rs.dens[c][q] = 0;
     /* the last blended sample has index terminationIndex-1 (:374-376) */
     for (--k; k >= 0; --k) {
       const real_t t = r.tmin + k * r.step;
-      const real_t density = sample_adjoint_fetch(&s, in->filter_mode, volume_pos(&r, t));
-      const v4 cur = tf_eval(in, b, density);
+      v3 adj_vp;
       v4 adj_cur;
-      acc = blend_adjoint(in->blend_mode, acc, cur, r.step, &adj_acc, &adj_cur, &adj_step);
-      const real_t adj_density = tf_adjoint(in, b, density, adj_cur, out);
-      const v3 adj_vp = sample_adjoint(&s, in->filter_mode, adj_density);
+      if (in->filter_mode == 3) {
+        /* the TF passes the colour through, and its adjoint the colour adjoint */
+        const v4 cur = rgba_adjoint_fetch(&rs, volume_pos(&r, t));
+        acc = blend_adjoint(in->blend_mode, acc, cur, r.step, &adj_acc, &adj_cur, &adj_step);
+        adj_vp = rgba_adjoint(&rs, adj_cur);
+      } else {
+        const real_t density = sample_adjoint_fetch(&s, in->filter_mode, volume_pos(&r, t));
+        const v4 cur = tf_eval(in, b, density);
+        acc = blend_adjoint(in->blend_mode, acc, cur, r.step, &adj_acc, &adj_cur, &adj_step);
+        const real_t adj_density = tf_adjoint(in, b, density, adj_cur, out);
+        adj_vp = sample_adjoint(&s, in->filter_mode, adj_density);
+      }
       /* chain through volumePos = (start + t*dir - boxMin) / voxelSize (:407-412) */
       const v3 adj_w = mk3(adj_vp.x / r.voxel.x, adj_vp.y / r.voxel.y, adj_vp.z / r.voxel.z);
       adj_start.x += adj_w.x; adj_start.y += adj_w.y; adj_start.z += adj_w.z;
@@ -567,7 +687,8 @@ int oracle_adjoint(const OracleInputs* in, const OracleTensor* color, const Orac
       const real_t adj_t = dot3(adj_w, r.dir);
       adj_step += adj_t * k;
     }
-    sampler_flush(&s, in->filter_mode);
+    if (in->filter_mode == 3) rgba_flush(&rs);
+    else sampler_flush(&s, in->filter_mode);
     if (out->has_stepsize) {
       real_t* p = at3(&out->adj_stepsize, b, y, x);
       if (out->stepsize_broadcast) atomic_add(p, adj_step);
@@ -719,7 +840,7 @@ static real_t trilerp_grad(const real_t* d, const real_t* f, v3* g) {
 
 int oracle_forward_gradients(const OracleInputs* in, const OracleForwardSettings* fs, OracleTensor* color,
                              OracleTensor* termination, OracleTensor* grads) {
-  if (check_modes(in)) return 2;
+  if (check_modes(in) || in->filter_mode == 3) return 2;
   const int D = fs->D;
   if (D <= 0) return 3;
   const int W = in->width, H = in->height, B = in->batch;
@@ -864,5 +985,53 @@ int oracle_forward_variables_to_gradients(const OracleTensor* fwd, const OracleT
         }
 #undef FWD4
   }
+  return 0;
+}
+
+/* ---- pre-shading (renderer/tf_utils_impl.cu:16-31, :120-140): a density
+ * volume 1 X Y Z becomes the colour volume 4 X Y Z through the TF of batch
+ * entry 0; the adjoint writes d loss / d density per voxel. ---- */
+static void preshade_inputs(const OracleTensor* tf, int tf_mode, OracleInputs* in) {
+  OracleInputs z = {0};
+  *in = z;
+  in->tf = *tf;
+  in->tf_mode = tf_mode;
+}
+
+int oracle_preshade_volume(const OracleTensor* density, const OracleTensor* tf, int tf_mode, OracleTensor* color) {
+  if (tf_mode < 0 || tf_mode > 3) return 2;
+  OracleInputs in;
+  preshade_inputs(tf, tf_mode, &in);
+  const int X = (int)density->sizes[1], Y = (int)density->sizes[2], Z = (int)density->sizes[3];
+#pragma omp parallel for schedule(static)
+  for (int x = 0; x < X; ++x)
+    for (int y = 0; y < Y; ++y)
+      for (int z = 0; z < Z; ++z) {
+        const v4 c = tf_eval(&in, 0, *at4(density, 0, x, y, z));
+        *at4(color, 0, x, y, z) = c.x;
+        *at4(color, 1, x, y, z) = c.y;
+        *at4(color, 2, x, y, z) = c.z;
+        *at4(color, 3, x, y, z) = c.w;
+      }
+  return 0;
+}
+
+int oracle_preshade_volume_adjoint(const OracleTensor* density, const OracleTensor* tf, int tf_mode,
+                                   const OracleTensor* adj_color, OracleTensor* adj_density) {
+  if (tf_mode < 0 || tf_mode > 3) return 2;
+  OracleInputs in;
+  preshade_inputs(tf, tf_mode, &in);
+  OracleAdjointOutputs none;
+  OracleAdjointOutputs z = {0};
+  none = z;  /* no TF gradient (:126-129) */
+  const int X = (int)density->sizes[1], Y = (int)density->sizes[2], Z = (int)density->sizes[3];
+#pragma omp parallel for schedule(static)
+  for (int x = 0; x < X; ++x)
+    for (int y = 0; y < Y; ++y)
+      for (int z = 0; z < Z; ++z) {
+        const v4 a = mk4(*at4(adj_color, 0, x, y, z), *at4(adj_color, 1, x, y, z), *at4(adj_color, 2, x, y, z),
+                         *at4(adj_color, 3, x, y, z));
+        *at4(adj_density, 0, x, y, z) = tf_adjoint(&in, 0, *at4(density, 0, x, y, z), a, &none);
+      }
   return 0;
 }

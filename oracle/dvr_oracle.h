@@ -38,12 +38,13 @@ typedef struct OracleTensor {
   int64_t strides[5];  /* in elements */
 } OracleTensor;
 
-/* Enum values are those of renderer/renderer_settings.cuh:81-146. */
+/* Enum values are those of renderer/renderer_settings.cuh:81-146; filter 3
+ * (pre-shaded) goes with TF 5 (pre-shaded) and a 4 X Y Z volume. */
 typedef struct OracleInputs {
   int32_t width, height;
-  int32_t filter_mode;   /* 0 nearest, 1 trilinear */
+  int32_t filter_mode;   /* 0 nearest, 1 trilinear, 3 pre-shaded */
   int32_t camera_mode;   /* 0 ray start/dir, 1 inverse view matrix, 2 reference frame */
-  int32_t tf_mode;       /* 0 identity, 1 texture, 2 linear, 3 gaussian */
+  int32_t tf_mode;       /* 0 identity, 1 texture, 2 linear, 3 gaussian, 5 pre-shaded */
   int32_t blend_mode;    /* 0 Beer-Lambert, 1 alpha */
   OracleTensor volume;        /* (B) X Y Z */
   OracleTensor box_min;       /* (B) 3 */
@@ -94,6 +95,15 @@ int oracle_forward_gradients(const OracleInputs* in, const OracleForwardSettings
  * enabled adjoint outputs (stepsize, camera, TF) — forwardVariablesToGradients. */
 int oracle_forward_variables_to_gradients(const OracleTensor* forward_variables, const OracleTensor* adj_color,
                                           const OracleForwardSettings* fs, OracleAdjointOutputs* out);
+/* Port only: pre-shading of a density volume (1 X Y Z) into a colour volume
+ * (4 X Y Z) with the TF of batch entry 0, and its adjoint (d loss / d
+ * density, written) — TFUtils::preshadeVolume. */
+int oracle_preshade_volume(const OracleTensor* density, const OracleTensor* tf, int tf_mode, OracleTensor* color);
+int oracle_preshade_volume_adjoint(const OracleTensor* density, const OracleTensor* tf, int tf_mode,
+                                   const OracleTensor* adj_color, OracleTensor* adj_density);
+/* Port only: the pre-shaded position adjoint follows the reference (0,
+ * default) or is the exact trilinear derivative (1). */
+void oracle_set_exact_preshaded(int exact);
 /* Size of real_t in this build (4 or 8). */
 int oracle_real_size(void);
 

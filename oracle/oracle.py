@@ -110,6 +110,17 @@ def load(kind: str = "port", precision: str = "f64") -> ctypes.CDLL:
         lib.oracle_forward.restype = ctypes.c_int
         lib.oracle_adjoint.restype = ctypes.c_int
         lib.oracle_real_size.restype = ctypes.c_int
+        if hasattr(lib, "oracle_preshade_volume"):
+            lib.oracle_preshade_volume.argtypes = [ctypes.POINTER(OracleTensor), ctypes.POINTER(OracleTensor),
+                                                   ctypes.c_int, ctypes.POINTER(OracleTensor)]
+            lib.oracle_preshade_volume.restype = ctypes.c_int
+            lib.oracle_preshade_volume_adjoint.argtypes = [ctypes.POINTER(OracleTensor), ctypes.POINTER(OracleTensor),
+                                                           ctypes.c_int, ctypes.POINTER(OracleTensor),
+                                                           ctypes.POINTER(OracleTensor)]
+            lib.oracle_preshade_volume_adjoint.restype = ctypes.c_int
+        if hasattr(lib, "oracle_set_exact_preshaded"):
+            lib.oracle_set_exact_preshaded.argtypes = [ctypes.c_int]
+            lib.oracle_set_exact_preshaded.restype = None
         if hasattr(lib, "oracle_forward_gradients"):  # the port only: the reference's needs cudAD
             lib.oracle_forward_gradients.argtypes = [
                 ctypes.POINTER(OracleInputs), ctypes.POINTER(OracleForwardSettings), ctypes.POINTER(OracleTensor),
@@ -160,7 +171,10 @@ class Scene:
     blending_early_out: float = 1.0 - 1e-5
 
     def batch(self) -> int:
-        arrs = [self.volume, self.tf, self.step_size, self.box_min, self.box_size]
+        # a pre-shaded volume (filter 3) holds its 4 channels in the first dimension
+        arrs = [self.tf, self.step_size, self.box_min, self.box_size]
+        if self.filter_mode != 3:
+            arrs.append(self.volume)
         if self.camera_mode == 0:
             arrs += [self.ray_start, self.ray_dir]
         else:
@@ -225,9 +239,14 @@ class AdjointRequest:
 
 
 def adjoint(scene: Scene, color: np.ndarray, term: np.ndarray, adj_color: np.ndarray,
-            req: AdjointRequest, kind: str = "port", precision: str = "f64") -> dict:
-    """Runs the adjoint march; returns a dict of gradient arrays (zero-initialised)."""
+            req: AdjointRequest, kind: str = "port", precision: str = "f64",
+            exact_preshaded: bool = False) -> dict:
+    """Runs the adjoint march; returns a dict of gradient arrays (zero-initialised).
+    exact_preshaded (port only): the exact position derivative of pre-shaded
+    volumes instead of the reference's."""
     lib = load(kind, precision)
+    if kind == "port":
+        lib.oracle_set_exact_preshaded(int(exact_preshaded))
     dt = _dtype(lib)
     keep: list = []
     inp = _inputs(scene, dt, keep)
@@ -350,3 +369,35 @@ def forward_variables_to_gradients(forward_variables: np.ndarray, adj_color: np.
     if rc != 0:
         raise RuntimeError(f"oracle_forward_variables_to_gradients failed with code {rc}")
     return res
+
+
+def preshade_volume(density: np.ndarray, tf: np.ndarray, tf_mode: int, precision: str = "f64") -> np.ndarray:
+    """Colour volume 4*X*Y*Z of a density volume 1*X*Y*Z (TF batch entry 0)."""
+    lib = load("port", precision)
+    dt = _dtype(lib)
+    keep: list = []
+    d = np.asarray(density, dtype=dt)
+    out = np.zeros((4,) + d.shape[1:], dtype=dt)
+    to = _tensor(out, keep)
+    rc = lib.oracle_preshade_volume(ctypes.byref(_tensor(d, keep)), ctypes.byref(_tensor(np.asarray(tf, dt), keep)),
+                                    int(tf_mode), ctypes.byref(to))
+    if rc != 0:
+        raise RuntimeError(f"oracle_preshade_volume failed with code {rc}")
+    return out
+
+
+def preshade_volume_adjoint(density: np.ndarray, tf: np.ndarray, tf_mode: int, adj_color: np.ndarray,
+                            precision: str = "f64") -> np.ndarray:
+    """d loss / d density (1*X*Y*Z) for the colour-volume adjoint adj_color (4*X*Y*Z)."""
+    lib = load("port", precision)
+    dt = _dtype(lib)
+    keep: list = []
+    d = np.asarray(density, dtype=dt)
+    out = np.zeros(d.shape, dtype=dt)
+    to = _tensor(out, keep)
+    rc = lib.oracle_preshade_volume_adjoint(ctypes.byref(_tensor(d, keep)),
+                                            ctypes.byref(_tensor(np.asarray(tf, dt), keep)), int(tf_mode),
+                                            ctypes.byref(_tensor(np.asarray(adj_color, dt), keep)), ctypes.byref(to))
+    if rc != 0:
+        raise RuntimeError(f"oracle_preshade_volume_adjoint failed with code {rc}")
+    return out

@@ -61,7 +61,8 @@ void adj(dim3 vs, const kernel::RendererInputs& i, const kernel::RendererOutputs
 #undef DVR_REF_ADJ
 }
 
-// Dispatch over the 2 x 3 x 4 x 2 mode combinations.
+// Dispatch over the 2 x 3 x 4 x 2 mode combinations, plus the pre-shaded
+// filter/TF pair with its 3 x 2 camera and blend modes.
 template <template <kernel::VolumeFilterMode, kernel::CameraMode, kernel::TFMode, kernel::BlendMode> class Fn,
           typename... Args>
 int dispatch(int f, int c, int t, int b, Args&&... args) {
@@ -87,6 +88,15 @@ int dispatch(int f, int c, int t, int b, Args&&... args) {
   }
   if (f == 0) { DVR_C(FilterNearest) }
   if (f == 1) { DVR_C(FilterTrilinear) }
+  if (f == 3 && t == 5) {
+    // pre-shaded volume: the TF mode is pre-shaded too (renderer/renderer.cpp:72-74)
+    switch (c) {
+      case 0: { DVR_B(FilterPreshaded, CameraRayStartDir, TFPreshaded) }
+      case 1: { DVR_B(FilterPreshaded, CameraInverseViewMatrix, TFPreshaded) }
+      case 2: { DVR_B(FilterPreshaded, CameraReferenceFrame, TFPreshaded) }
+      default: return 2;
+    }
+  }
   return 2;
 #undef DVR_B
 #undef DVR_T
