@@ -27,9 +27,19 @@ cudaError_t forward_go(const RenderParams& p, const LaunchInfo& li, cudaStream_t
 
 template <int BLEND, typename VT, bool EXACT>
 cudaError_t adjoint_go(const RenderParams& p, const AdjointParams& a, const LaunchInfo& li, cudaStream_t s) {
-  const int64_t rays = int64_t(p.B) * p.H * p.W;
+  const RayOrder order = RayOrder::make(p.W, p.H, p.B);
+  cudaError_t err = cudaSuccess;
+  int* ints = static_cast<int*>(acquire_scratch(li.device, s, work_order_ints(p) * sizeof(int), err));
+  if (err != cudaSuccess) return err;
+  err = order_rays_by_work(p, &a, ints, li, s);
+  if (err != cudaSuccess) return err;
+  int* counter = acquire_counter(li.device, s, err);
+  if (err != cudaSuccess) return err;
+  const int* list = ints + work_order_list_offset;
+  const int* count = ints + work_order_count_offset;
   auto run = [&](auto kernel) {
-    kernel<<<grid_for(kernel, 256, rays, li), 256, 0, s>>>(p, a);
+    kernel<<<grid_for(kernel, kFastThreads, order.total(), li), kFastThreads, 0, s>>>(p, a, order, counter, list,
+                                                                                     count);
     return cudaGetLastError();
   };
   return a.has_volume ? run(preshaded_adjoint_kernel<BLEND, VT, true, EXACT>)

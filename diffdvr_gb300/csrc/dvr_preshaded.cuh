@@ -165,111 +165,122 @@ __global__ void __launch_bounds__(256) preshaded_plain_forward_kernel(const Rend
 
 // Adjoint: one thread per ray, reverse march with blend inversion
 // (renderer/renderer_kernels.cuh:315-444); volume gradients accumulated per
-// cell and channel in registers, 32 atomics on cell exit.
+// cell and channel in registers, flushed on cell exit (z-adjacent corner
+// pairs as one vector atomic).  Persistent: the lanes of a warp take the
+// next 32 rays of the longest-first list of rays with samples together, so
+// a warp's rays have similar lengths and no block idles behind one long ray.
 template <int BLEND, typename VT, bool VOLGRAD, bool EXACT>
-__global__ void __launch_bounds__(256) preshaded_adjoint_kernel(const RenderParams p, const AdjointParams a) {
-  const int64_t total = int64_t(p.B) * p.H * p.W;
+__global__ void __launch_bounds__(kFastThreads) preshaded_adjoint_kernel(const RenderParams p, const AdjointParams a,
+                                                                         const RayOrder order, int* counter,
+                                                                         const int* ray_list, const int* ray_count) {
   const RgbaVolume<VT> vol = rgba_volume<VT>(p);
   float* adjv = VOLGRAD ? static_cast<float*>(a.adj_volume.p) : nullptr;
   const int64_t gc = a.adj_volume.s[0], gx = a.adj_volume.s[1], gy = a.adj_volume.s[2], gz = a.adj_volume.s[3];
-  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += int64_t(gridDim.x) * blockDim.x) {
-    const int b = int(i / (int64_t(p.W) * p.H));
-    const int y = int((i - int64_t(b) * p.W * p.H) / p.W);
-    const int x = int(i - int64_t(p.W) * (y + int64_t(p.H) * b));
-    Ray r;
-    setup_ray(p, x, y, b, r);
-    const float* fc = static_cast<const float*>(a.fwd_color.p) + b * a.fwd_color.s[0] + y * a.fwd_color.s[1] +
-                      x * a.fwd_color.s[2];
-    f4 acc = mk4(fc[0], fc[a.fwd_color.s[3]], fc[2 * a.fwd_color.s[3]], fc[3 * a.fwd_color.s[3]]);
-    int k = static_cast<const int*>(a.fwd_term.p)[b * a.fwd_term.s[0] + y * a.fwd_term.s[1] + x * a.fwd_term.s[2]];
-    k = min(k, max_samples(r.tmin, r.tmax, r.step));
-    const float* ac = static_cast<const float*>(a.adj_color.p) + b * a.adj_color.s[0] + y * a.adj_color.s[1] +
-                      x * a.adj_color.s[2];
-    f4 adj_acc = mk4(ac[0], ac[a.adj_color.s[3]], ac[2 * a.adj_color.s[3]], ac[3 * a.adj_color.s[3]]);
-    float adj_step = 0.f;
-    f3 adj_start = mk3(0, 0, 0), adj_dir = mk3(0, 0, 0);
-    int cx = -1, cy = -1, cz = -1;
-    float d[4][8], g[4][8];
+  const int total = *ray_count;
+  bool exhausted = false;
+  while (true) {
+    const int pos = fetch_rays(counter, total, true, exhausted);
+    if (__ballot_sync(kFullMask, pos >= 0) == 0u) break;
+    int b = 0, x = 0, y = 0;
+    // lanes without a ray skip the body; all lanes fetch together at the top
+    if (pos >= 0 && order.pixel(ray_list[pos], b, x, y)) {
+      Ray r;
+      setup_ray(p, x, y, b, r);
+      const float* fc = static_cast<const float*>(a.fwd_color.p) + b * a.fwd_color.s[0] + y * a.fwd_color.s[1] +
+                        x * a.fwd_color.s[2];
+      f4 acc = mk4(fc[0], fc[a.fwd_color.s[3]], fc[2 * a.fwd_color.s[3]], fc[3 * a.fwd_color.s[3]]);
+      int k = static_cast<const int*>(a.fwd_term.p)[b * a.fwd_term.s[0] + y * a.fwd_term.s[1] + x * a.fwd_term.s[2]];
+      k = min(k, max_samples(r.tmin, r.tmax, r.step));
+      const float* ac = static_cast<const float*>(a.adj_color.p) + b * a.adj_color.s[0] + y * a.adj_color.s[1] +
+                        x * a.adj_color.s[2];
+      f4 adj_acc = mk4(ac[0], ac[a.adj_color.s[3]], ac[2 * a.adj_color.s[3]], ac[3 * a.adj_color.s[3]]);
+      float adj_step = 0.f;
+      f3 adj_start = mk3(0, 0, 0), adj_dir = mk3(0, 0, 0);
+      int cx = -1, cy = -1, cz = -1;
+      float d[4][8], g[4][8];
 #pragma unroll
-    for (int c = 0; c < 4; ++c)
+      for (int c = 0; c < 4; ++c)
 #pragma unroll
-      for (int q = 0; q < 8; ++q) d[c][q] = g[c][q] = 0.f;
-    auto flush = [&]() {
-      if constexpr (VOLGRAD) {
-        if (cx < 0) return;
-        const int lx = clampi(cx, 0, p.X - 1), hx = clampi(cx + 1, 0, p.X - 1);
-        const int ly = clampi(cy, 0, p.Y - 1), hy = clampi(cy + 1, 0, p.Y - 1);
-        const int lz = clampi(cz, 0, p.Z - 1), hz = clampi(cz + 1, 0, p.Z - 1);
-        const int64_t o[8] = {lx * gx + ly * gy + lz * gz, lx * gx + ly * gy + hz * gz, lx * gx + hy * gy + lz * gz,
-                              lx * gx + hy * gy + hz * gz, hx * gx + ly * gy + lz * gz, hx * gx + ly * gy + hz * gz,
-                              hx * gx + hy * gy + lz * gz, hx * gx + hy * gy + hz * gz};
+        for (int q = 0; q < 8; ++q) d[c][q] = g[c][q] = 0.f;
+      auto flush = [&]() {
+        if constexpr (VOLGRAD) {
+          if (cx < 0) return;
+          const int lx = clampi(cx, 0, p.X - 1), hx = clampi(cx + 1, 0, p.X - 1);
+          const int ly = clampi(cy, 0, p.Y - 1), hy = clampi(cy + 1, 0, p.Y - 1);
+          const int lz = clampi(cz, 0, p.Z - 1), hz = clampi(cz + 1, 0, p.Z - 1);
+          // z-adjacent corner pairs go as one vector atomic where aligned
+          const bool pair = gz == 1 && hz == lz + 1;
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            float* base = adjv + c * gc;
+            VolGradCell<kTrilinear, true>::add_z(base + lx * gx + ly * gy, lz, hz, gz, pair, g[c][0], g[c][1]);
+            VolGradCell<kTrilinear, true>::add_z(base + lx * gx + hy * gy, lz, hz, gz, pair, g[c][2], g[c][3]);
+            VolGradCell<kTrilinear, true>::add_z(base + hx * gx + ly * gy, lz, hz, gz, pair, g[c][4], g[c][5]);
+            VolGradCell<kTrilinear, true>::add_z(base + hx * gx + hy * gy, lz, hz, gz, pair, g[c][6], g[c][7]);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) g[c][q] = 0.f;
+          }
+        }
+      };
+      for (--k; k >= 0; --k) {
+        const float t = r.tmin + k * r.step;
+        const f3 vp = volume_pos(r, t);
+        const int ix = int(vp.x), iy = int(vp.y), iz = int(vp.z);
+        if (ix != cx || iy != cy || iz != cz) {
+          flush();
+          cx = ix, cy = iy, cz = iz;
+          vol.corners(ix, iy, iz, d);
+        }
+        const float fx = vp.x - float(ix), fy = vp.y - float(iy), fz = vp.z - float(iz);
+        const f4 cur = mk4(trilerp(d[0], fx, fy, fz), trilerp(d[1], fx, fy, fz), trilerp(d[2], fx, fy, fz),
+                           trilerp(d[3], fx, fy, fz));
+        f4 adj_cur;
+        float step_contrib;
+        acc = blend_adjoint_invert<BLEND>(acc, cur, r.step, adj_acc, adj_cur, step_contrib);
+        if constexpr (EXACT) adj_step += step_contrib;
+        else adj_step = step_contrib;  // the reference assigns (renderer/renderer_blending.cuh:93, :158)
+        // adjoint of the four interpolants, corner order 000,100,010,110,001,101,011,111
+        const float cw[3] = {fx, fy, fz}, fw[3] = {1.f - fx, 1.f - fy, 1.f - fz};
+        float adj_c[3] = {0, 0, 0}, adj_f[3] = {0, 0, 0};
+        const float av[4] = {adj_cur.x, adj_cur.y, adj_cur.z, adj_cur.w};
+        constexpr int order[8] = {0, 4, 2, 6, 1, 5, 3, 7};
 #pragma unroll
         for (int c = 0; c < 4; ++c)
 #pragma unroll
           for (int q = 0; q < 8; ++q) {
-            atomicAdd(adjv + c * gc + o[q], g[c][q]);
-            g[c][q] = 0.f;
+            const int idx = order[q];
+            const int hx = (idx >> 2) & 1, hy = (idx >> 1) & 1, hz = idx & 1;
+            const float wx = hx ? cw[0] : fw[0], wy = hy ? cw[1] : fw[1], wz = hz ? cw[2] : fw[2];
+            if constexpr (VOLGRAD) g[c][idx] += av[c] * (wx * wy * wz);
+            const float ad = av[c] * d[c][idx];
+            if (hx) adj_c[0] += ad * wy * wz; else adj_f[0] += ad * wy * wz;
+            if (hy) adj_c[1] += ad * wx * wz; else adj_f[1] += ad * wx * wz;
+            if ((EXACT ? hz : hy) != 0) adj_c[2] += ad * wx * wy; else adj_f[2] += ad * wx * wy;
           }
+        const f3 adj_vp = mk3(adj_c[0] - adj_f[0], adj_c[1] - adj_f[1], adj_c[2] - adj_f[2]);
+        const f3 adj_w = mk3(adj_vp.x / r.voxel.x, adj_vp.y / r.voxel.y, adj_vp.z / r.voxel.z);
+        adj_start.x += adj_w.x; adj_start.y += adj_w.y; adj_start.z += adj_w.z;
+        adj_dir.x += adj_w.x * t; adj_dir.y += adj_w.y * t; adj_dir.z += adj_w.z * t;
+        adj_step += dot3(adj_w, r.dir) * k;
       }
-    };
-    for (--k; k >= 0; --k) {
-      const float t = r.tmin + k * r.step;
-      const f3 vp = volume_pos(r, t);
-      const int ix = int(vp.x), iy = int(vp.y), iz = int(vp.z);
-      if (ix != cx || iy != cy || iz != cz) {
-        flush();
-        cx = ix, cy = iy, cz = iz;
-        vol.corners(ix, iy, iz, d);
+      flush();
+      if (a.has_stepsize) {
+        float* ps = static_cast<float*>(a.adj_step.p) + b * a.adj_step.s[0] + y * a.adj_step.s[1] + x * a.adj_step.s[2];
+        if (a.stepsize_broadcast) atomicAdd(ps, adj_step);
+        else *ps = adj_step;
       }
-      const float fx = vp.x - float(ix), fy = vp.y - float(iy), fz = vp.z - float(iz);
-      const f4 cur = mk4(trilerp(d[0], fx, fy, fz), trilerp(d[1], fx, fy, fz), trilerp(d[2], fx, fy, fz),
-                         trilerp(d[3], fx, fy, fz));
-      f4 adj_cur;
-      float step_contrib;
-      acc = blend_adjoint_invert<BLEND>(acc, cur, r.step, adj_acc, adj_cur, step_contrib);
-      if constexpr (EXACT) adj_step += step_contrib;
-      else adj_step = step_contrib;  // the reference assigns (renderer/renderer_blending.cuh:93, :158)
-      // adjoint of the four interpolants, corner order 000,100,010,110,001,101,011,111
-      const float cw[3] = {fx, fy, fz}, fw[3] = {1.f - fx, 1.f - fy, 1.f - fz};
-      float adj_c[3] = {0, 0, 0}, adj_f[3] = {0, 0, 0};
-      const float av[4] = {adj_cur.x, adj_cur.y, adj_cur.z, adj_cur.w};
-      constexpr int order[8] = {0, 4, 2, 6, 1, 5, 3, 7};
+      if (a.has_camera) {
+        const float vs[3] = {adj_start.x, adj_start.y, adj_start.z};
+        const float vd[3] = {adj_dir.x, adj_dir.y, adj_dir.z};
 #pragma unroll
-      for (int c = 0; c < 4; ++c)
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const int idx = order[q];
-          const int hx = (idx >> 2) & 1, hy = (idx >> 1) & 1, hz = idx & 1;
-          const float wx = hx ? cw[0] : fw[0], wy = hy ? cw[1] : fw[1], wz = hz ? cw[2] : fw[2];
-          if constexpr (VOLGRAD) g[c][idx] += av[c] * (wx * wy * wz);
-          const float ad = av[c] * d[c][idx];
-          if (hx) adj_c[0] += ad * wy * wz; else adj_f[0] += ad * wy * wz;
-          if (hy) adj_c[1] += ad * wx * wz; else adj_f[1] += ad * wx * wz;
-          if ((EXACT ? hz : hy) != 0) adj_c[2] += ad * wx * wy; else adj_f[2] += ad * wx * wy;
-        }
-      const f3 adj_vp = mk3(adj_c[0] - adj_f[0], adj_c[1] - adj_f[1], adj_c[2] - adj_f[2]);
-      const f3 adj_w = mk3(adj_vp.x / r.voxel.x, adj_vp.y / r.voxel.y, adj_vp.z / r.voxel.z);
-      adj_start.x += adj_w.x; adj_start.y += adj_w.y; adj_start.z += adj_w.z;
-      adj_dir.x += adj_w.x * t; adj_dir.y += adj_w.y * t; adj_dir.z += adj_w.z * t;
-      adj_step += dot3(adj_w, r.dir) * k;
-    }
-    flush();
-    if (a.has_stepsize) {
-      float* ps = static_cast<float*>(a.adj_step.p) + b * a.adj_step.s[0] + y * a.adj_step.s[1] + x * a.adj_step.s[2];
-      if (a.stepsize_broadcast) atomicAdd(ps, adj_step);
-      else *ps = adj_step;
-    }
-    if (a.has_camera) {
-      const float vs[3] = {adj_start.x, adj_start.y, adj_start.z};
-      const float vd[3] = {adj_dir.x, adj_dir.y, adj_dir.z};
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        if (a.camera_broadcast) {
-          atomic_out(a.adj_start, b, y, x, c, vs[c]);
-          atomic_out(a.adj_dir, b, y, x, c, vd[c]);
-        } else {
-          write_out(a.adj_start, b, y, x, c, vs[c]);
-          write_out(a.adj_dir, b, y, x, c, vd[c]);
+        for (int c = 0; c < 3; ++c) {
+          if (a.camera_broadcast) {
+            atomic_out(a.adj_start, b, y, x, c, vs[c]);
+            atomic_out(a.adj_dir, b, y, x, c, vd[c]);
+          } else {
+            write_out(a.adj_start, b, y, x, c, vs[c]);
+            write_out(a.adj_dir, b, y, x, c, vd[c]);
+          }
         }
       }
     }
