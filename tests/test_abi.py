@@ -92,7 +92,10 @@ def _forward(lib, i, o):
     (lambda i, o: setattr(i, "volume", _fake((1, 4, 5, 6), _abi.DVR_FLOAT64)), "volume must be of type float32"),
     (lambda i, o: setattr(i, "tf", _fake((1, 8, 3))), "tf must have 4 entries at dimension 2"),
     (lambda i, o: setattr(i, "tf_mode", 6), "TFGaussianLog is not supported"),
-    (lambda i, o: setattr(i, "volume_filter_mode", 3), "pre-shaded volumes are not supported"),
+    (lambda i, o: setattr(i, "volume_filter_mode", 3),
+     "if pre-shading is selected, both the filter mode and TF mode must be set to preshaded"),
+    (lambda i, o: (setattr(i, "volume_filter_mode", 3), setattr(i, "tf_mode", 5)),
+     "the volume colors are encoded in the batch dimension of the volume. It must be 4, but is 1"),
     (lambda i, o: setattr(i, "camera_ray_start", _fake((1, 7, 9, 3))), "cameraRayStart must have 8 entries at dimension 2"),
     (lambda i, o: setattr(i, "camera_ray_dir", _fake((3, 7, 8, 3))), None),  # batch 3 vs 1 broadcasts; passes checks
     (lambda i, o: setattr(i, "camera_mode", 2), "'CameraReferenceFrame' specified in 'cameraMode'"),
