@@ -199,9 +199,9 @@ def profiled_traffic():
 
 # ------------------------------------------------------------------ GPU arm
 def algorithmic_bytes(w, s_v, V, P, S, ck_written, recorded, record_kernel, tf_numel):
-    """Compulsory HBM bytes per forward and adjoint launch (SURVEY §8(d) model,
-    with the sample record): volume once, per-ray outputs/inputs, checkpoints,
-    the record (8 B per sample), gradients read-modify-written once."""
+    """Compulsory HBM bytes per forward and adjoint launch: volume once,
+    per-ray outputs/inputs, checkpoints, the sample record (8 B per sample),
+    gradients read-modify-written once."""
     grads = set(w.grads)
     fwd = V * s_v + P * (16 + 4) + ck_written * 4
     if recorded:
