@@ -41,6 +41,11 @@ struct TexelPairAtomic {
   __device__ __forceinline__ void put(int t, f4 v) const {
     if (t < 0 || t >= R) return;
     float* e = dst + t * sr;
+    if (sc == 1 && (reinterpret_cast<uintptr_t>(e) & 15u) == 0u) {
+      if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f)
+        atomicAdd(reinterpret_cast<float4*>(e), make_float4(v.x, v.y, v.z, v.w));
+      return;
+    }
     if (v.x != 0.f) atomicAdd(e, v.x);
     if (v.y != 0.f) atomicAdd(e + sc, v.y);
     if (v.z != 0.f) atomicAdd(e + 2 * sc, v.z);
@@ -52,7 +57,13 @@ struct TexelPairAtomic {
     put(i + 1, a1);
     i = -1;
   }
+  // one texel's four channels: a single 16-byte vector reduction when the
+  // channels are contiguous and aligned (the per-warp slices are), else four
   __device__ __forceinline__ void red4(float* e, f4 v) const {
+    if (sc == 1 && (reinterpret_cast<uintptr_t>(e) & 15u) == 0u) {
+      atomicAdd(reinterpret_cast<float4*>(e), make_float4(v.x, v.y, v.z, v.w));
+      return;
+    }
     atomicAdd(e, v.x);
     atomicAdd(e + sc, v.y);
     atomicAdd(e + 2 * sc, v.z);
