@@ -213,6 +213,17 @@ __device__ __forceinline__ float trilerp(const float* d, float fx, float fy, flo
                lerp1(lerp1(d[1], d[5], fx), lerp1(d[3], d[7], fx), fy), fz);
 }
 
+// Trilinear density and its gradient with respect to the volume position.
+__device__ __forceinline__ float trilerp_grad(const float* d, float fx, float fy, float fz, f3& g) {
+  const float ay0 = lerp1(d[0], d[4], fx), ay1 = lerp1(d[2], d[6], fx);
+  const float by0 = lerp1(d[1], d[5], fx), by1 = lerp1(d[3], d[7], fx);
+  g.x = lerp1(lerp1(d[4] - d[0], d[6] - d[2], fy), lerp1(d[5] - d[1], d[7] - d[3], fy), fz);
+  g.y = lerp1(ay1 - ay0, by1 - by0, fz);
+  const float lo = lerp1(ay0, ay1, fy), hi = lerp1(by0, by1, fy);
+  g.z = hi - lo;
+  return lerp1(lo, hi, fz);
+}
+
 // Gradient of the trilinear interpolant w.r.t. the eight corners and the
 // position, in the reference's accumulation order 000,100,010,110,001,101,011,111
 // (renderer/renderer_interpolation.cuh:360-387).  acc may be nullptr.

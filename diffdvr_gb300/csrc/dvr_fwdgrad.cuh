@@ -43,17 +43,6 @@
 
 namespace dvr {
 
-// Trilinear density and its gradient with respect to the volume position.
-__device__ __forceinline__ float trilerp_grad(const float* d, float fx, float fy, float fz, f3& g) {
-  const float ay0 = lerp1(d[0], d[4], fx), ay1 = lerp1(d[2], d[6], fx);
-  const float by0 = lerp1(d[1], d[5], fx), by1 = lerp1(d[3], d[7], fx);
-  g.x = lerp1(lerp1(d[4] - d[0], d[6] - d[2], fy), lerp1(d[5] - d[1], d[7] - d[3], fy), fz);
-  g.y = lerp1(ay1 - ay0, by1 - by0, fz);
-  const float lo = lerp1(ay0, ay1, fy), hi = lerp1(by0, by1, fy);
-  g.z = hi - lo;
-  return lerp1(lo, hi, fz);
-}
-
 // d c / d density of the TF (renderer/renderer_tf.cuh:122-150, :256-290,
 // :437-486, :522-560 with a traced density).
 template <int TF, class A>

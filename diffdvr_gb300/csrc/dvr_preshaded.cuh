@@ -177,6 +177,7 @@ __global__ void __launch_bounds__(kFastThreads) preshaded_adjoint_kernel(const R
   float* adjv = VOLGRAD ? static_cast<float*>(a.adj_volume.p) : nullptr;
   const int64_t gc = a.adj_volume.s[0], gx = a.adj_volume.s[1], gy = a.adj_volume.s[2], gz = a.adj_volume.s[3];
   const int total = *ray_count;
+  const bool need_pos = a.has_camera || a.has_stepsize;
   bool exhausted = false;
   while (true) {
     const int pos = fetch_rays(counter, total, true, exhausted);
@@ -239,10 +240,34 @@ __global__ void __launch_bounds__(kFastThreads) preshaded_adjoint_kernel(const R
         acc = blend_adjoint_invert<BLEND>(acc, cur, r.step, adj_acc, adj_cur, step_contrib);
         if constexpr (EXACT) adj_step += step_contrib;
         else adj_step = step_contrib;  // the reference assigns (renderer/renderer_blending.cuh:93, :158)
-        // adjoint of the four interpolants, corner order 000,100,010,110,001,101,011,111
+        const float av[4] = {adj_cur.x, adj_cur.y, adj_cur.z, adj_cur.w};
+      f3 adj_vp = mk3(0, 0, 0);
+      if constexpr (EXACT) {
+        // the eight corner weights once for the four channels; the position
+        // gradient only where camera or step-size gradients are wanted
+        if constexpr (VOLGRAD) {
+          const float ux = 1.f - fx, uy = 1.f - fy, uz = 1.f - fz;
+          const float w8[8] = {ux * uy * uz, ux * uy * fz, ux * fy * uz, ux * fy * fz,
+                               fx * uy * uz, fx * uy * fz, fx * fy * uz, fx * fy * fz};
+#pragma unroll
+          for (int c = 0; c < 4; ++c)
+#pragma unroll
+            for (int q = 0; q < 8; ++q) g[c][q] = fmaf(av[c], w8[q], g[c][q]);
+        }
+        if (need_pos) {
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            f3 gc3;
+            trilerp_grad(d[c], fx, fy, fz, gc3);
+            adj_vp.x = fmaf(av[c], gc3.x, adj_vp.x);
+            adj_vp.y = fmaf(av[c], gc3.y, adj_vp.y);
+            adj_vp.z = fmaf(av[c], gc3.z, adj_vp.z);
+          }
+        }
+      } else {
+        // the reference's scatter, corner order 000,100,010,110,001,101,011,111
         const float cw[3] = {fx, fy, fz}, fw[3] = {1.f - fx, 1.f - fy, 1.f - fz};
         float adj_c[3] = {0, 0, 0}, adj_f[3] = {0, 0, 0};
-        const float av[4] = {adj_cur.x, adj_cur.y, adj_cur.z, adj_cur.w};
         constexpr int order[8] = {0, 4, 2, 6, 1, 5, 3, 7};
 #pragma unroll
         for (int c = 0; c < 4; ++c)
@@ -255,10 +280,11 @@ __global__ void __launch_bounds__(kFastThreads) preshaded_adjoint_kernel(const R
             const float ad = av[c] * d[c][idx];
             if (hx) adj_c[0] += ad * wy * wz; else adj_f[0] += ad * wy * wz;
             if (hy) adj_c[1] += ad * wx * wz; else adj_f[1] += ad * wx * wz;
-            if ((EXACT ? hz : hy) != 0) adj_c[2] += ad * wx * wy; else adj_f[2] += ad * wx * wy;
+            if (hy) adj_c[2] += ad * wx * wy; else adj_f[2] += ad * wx * wy;  // y selector, as the reference
           }
-        const f3 adj_vp = mk3(adj_c[0] - adj_f[0], adj_c[1] - adj_f[1], adj_c[2] - adj_f[2]);
-        const f3 adj_w = mk3(adj_vp.x / r.voxel.x, adj_vp.y / r.voxel.y, adj_vp.z / r.voxel.z);
+        adj_vp = mk3(adj_c[0] - adj_f[0], adj_c[1] - adj_f[1], adj_c[2] - adj_f[2]);
+      }
+      const f3 adj_w = mk3(adj_vp.x / r.voxel.x, adj_vp.y / r.voxel.y, adj_vp.z / r.voxel.z);
         adj_start.x += adj_w.x; adj_start.y += adj_w.y; adj_start.z += adj_w.z;
         adj_dir.x += adj_w.x * t; adj_dir.y += adj_w.y * t; adj_dir.z += adj_w.z * t;
         adj_step += dot3(adj_w, r.dir) * k;
