@@ -87,8 +87,10 @@ __global__ void __launch_bounds__(kFastThreads) fast_forward_warp_kernel(const R
     const size_t vb = p.volume.s[0] != 0 ? size_t(b) * p.X * p.Y * p.Z : 0;
     const CellVolume<VT> cv{cells ? cells + vb : nullptr, p.X - 1, p.Y - 1, p.Z - 1};
     const TfShared<C> tf{s_tf + (copies > 1 ? b : 0) * p.R * C, p.R};
-    float* ck = p.ckpt.p ? static_cast<float*>(p.ckpt.p) + b * p.ckpt.s[0] + y * p.ckpt.s[1] + x * p.ckpt.s[2]
-                         : nullptr;
+    // a recorded ray carries its opacities in the record: no checkpoints
+    float* ck = p.ckpt.p && !rec
+                    ? static_cast<float*>(p.ckpt.p) + b * p.ckpt.s[0] + y * p.ckpt.s[1] + x * p.ckpt.s[2]
+                    : nullptr;
 
     float alpha = 0.f;  // accumulated opacity before the chunk
     float cr = 0.f, cg = 0.f, cb = 0.f;  // this lane's samples' colour contributions

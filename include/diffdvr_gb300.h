@@ -134,7 +134,8 @@ typedef struct DvrRendererInputs {
  *    order, a multiple of 4 floats each) and writes the run's first float
  *    index / 4 to sample_offset, or -1 when the pool was full.  The adjoint
  *    then reads these instead of re-sampling the volume and re-marching from
- *    checkpoints; rays with offset -1 re-sample.  N = B*H*W*S with
+ *    checkpoints; rays with offset -1 re-sample.  Checkpoints are written
+ *    only for the rays without a record.  N = B*H*W*S with
  *    S = 4 * dvr_checkpoint_slots(length, step, 2) holds every ray.
  *    Written and read by the optimized single-instance entry points only. */
 typedef struct DvrRendererOutputs {

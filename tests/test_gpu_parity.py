@@ -593,8 +593,9 @@ def test_sample_density_record(fraction, cuda_device):
     """The forward's sample record: every ray with samples that got room holds
     n (density, incoming opacity) pairs in its own disjoint 4-aligned run of
     the pool: densities finite and inside the volume's range, opacities
-    starting at 0, non-decreasing, below 1 and equal to the checkpoints at
-    multiples of the interval; rays without samples or without room are -1;
+    starting at 0, non-decreasing, below 1 and equal to the checkpoints a
+    forward without record writes at multiples of the interval (recorded rays
+    get no checkpoints); rays without samples or without room are -1;
     the adjoint from the record equals the re-sampling adjoint (relative L2
     <= 1e-5: the recorded opacities are the forward's, the re-march's agree
     to rounding)."""
@@ -616,7 +617,11 @@ def test_sample_density_record(fraction, cuda_device):
     else:
         assert ((term > 0) & (off == -1)).any() and hit.any()
     lo, hi = float(case.volume.min()), float(case.volume.max())
-    ck = out.checkpoints.cpu().numpy()
+    ck_rec = out.checkpoints.cpu().numpy()
+    assert np.isnan(ck_rec[hit]).all()  # recorded rays: checkpoints left untouched
+    _, norec_out = gpu_forward(case, checkpoints=True)
+    assert np.array_equal(norec_out.terminationIndex.cpu().numpy(), term)
+    ck = norec_out.checkpoints.cpu().numpy()
     K = out.checkpoint_interval
     starts, ends = [], []
     for (bi, yi, xi), o, n in zip(np.argwhere(hit), off[hit], term[hit]):
@@ -635,7 +640,8 @@ def test_sample_density_record(fraction, cuda_device):
     rng = np.random.default_rng(3)
     adj = rng.standard_normal(out.color.shape).astype(np.float32)
     got = gpu_adjoint(case, inp, out, adj, volume=True, tf=True, camera=True, stepsize=True)
-    plain_out = type(out)(out.color, out.terminationIndex, out.checkpoints, out.checkpoint_interval)
+    # re-sampling adjoint: the same forward outputs with the record-less forward's checkpoints
+    plain_out = type(out)(out.color, out.terminationIndex, norec_out.checkpoints, out.checkpoint_interval)
     ref = gpu_adjoint(case, inp, plain_out, adj, volume=True, tf=True, camera=True, stepsize=True)
     for k in ref:
         assert rel_l2(got[k], ref[k]) <= 1e-5, (k, rel_l2(got[k], ref[k]))
