@@ -108,6 +108,23 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(values, world: int, device) -> list:
+    """Each timing's maximum over the ranks: the job's step takes as long as
+    its slowest replica.  device: where the collective's tensor lives (CUDA for
+    NCCL, CPU for gloo)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v) for v in values], device=device, dtype=torch.float64)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.cpu()]
+
+
+def job_rate(samples_per_rank: int, world: int, ms: float) -> float:
+    """Whole-job samples/s: every replica marches the same workload."""
+    return samples_per_rank * world / (ms / 1e3)
+
+
 # ------------------------------------------------------------------ clocks
 class ClockSampler:
     """nvidia-smi clock/throttle samples during the timed region."""
@@ -497,12 +514,9 @@ def run_gpu(args):
                  "kernels": "plain FP32 (one thread per ray, blend inversion)"}
 
     # ---- aggregate over ranks (max time)
-    t = torch.tensor([ms_graph, ms_e2e], device=dev, dtype=torch.float64)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_graph, ms_e2e = float(t[0]), float(t[1])
-    value = samples * world / (ms_graph / 1e3)
-    e2e_value = samples * world / (ms_e2e / 1e3)
+    ms_graph, ms_e2e = max_over_ranks([ms_graph, ms_e2e], world, dev)
+    value = job_rate(samples, world, ms_graph)
+    e2e_value = job_rate(samples, world, ms_e2e)
 
     # ---- roofline of the dominant kernel (compulsory HBM bytes per launch)
     peak, peak_kind = measured_peaks()
