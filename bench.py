@@ -299,7 +299,8 @@ def run_gpu(args):
     out = pr.RendererOutputs(color, term, ckpt, K)
     pool = 0
     record_mode = "none"
-    if args.record != "none" and args.method == "adjoint" and w.filter_mode != 3:
+    # pre-shaded: the record only on request (the adjoint uses it when the rays are few)
+    if args.record != "none" and args.method == "adjoint" and (w.filter_mode != 3 or args.record == "full"):
         full = pr.Renderer.sample_density_size(inp_s, B)
         pool = full
         if args.record == "auto":
@@ -532,6 +533,8 @@ def run_gpu(args):
     else:
         fwd_bytes, adj_bytes = algorithmic_bytes(w, s_v, V, P, samples, ck_written, pool > 0, record_kernel,
                                                  tf.numel())
+        if w.filter_mode == 3 and pool > 0:
+            adj_bytes += V * s_v  # the pre-shaded record holds opacities only: colours are gathered again
         names = ("adjoint", "forward")
     dominant = (names[0], adj_bytes, adj_ms) if adj_ms >= fwd_ms else (names[1], fwd_bytes, fwd_ms)
     achieved = dominant[1] / (dominant[2] / 1e3) / 1e9
@@ -549,7 +552,8 @@ def run_gpu(args):
     if forward_method:
         launches_per_step = 2  # forward-gradient march + contraction
     elif w.filter_mode == 3:
-        launches_per_step = 2  # pre-shaded forward + adjoint
+        # pre-shaded: forward; ray order (3) + the record kernel and the per-lane kernel over its leftovers
+        launches_per_step = 1 + 3 + (2 if pool > 0 else 1)
 
     result = {
         "metric": METRIC_FORWARD if forward_method else METRIC,

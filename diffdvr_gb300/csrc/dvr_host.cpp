@@ -409,9 +409,9 @@ void check_outputs(const DvrRendererOutputs& out, Checked& c, bool forward) {
   const bool has_off = out.sample_offset.ndim >= 0 && out.sample_offset.data != nullptr;
   if (has_dens != has_off) fail(DVR_E_INVALID_ARGUMENT, "sample_density and sample_offset go together");
   if (has_dens) {
-    if (c.filter == DVR_FILTER_PRESHADED)
-      fail(DVR_E_UNSUPPORTED, "sample_density records densities; pre-shaded volumes have none");
-    if (!p.ckpt.p) fail(DVR_E_INVALID_ARGUMENT, "sample_density needs a checkpoint buffer");
+    // the density path re-marches unrecorded rays from checkpoints; pre-shaded rays invert the blend
+    if (!p.ckpt.p && c.filter != DVR_FILTER_PRESHADED)
+      fail(DVR_E_INVALID_ARGUMENT, "sample_density needs a checkpoint buffer");
     const DvrTensor& d = out.sample_density;
     check_dim(d, "sample_density", 1);
     check_device(d, "sample_density", c.device);
@@ -610,7 +610,6 @@ cudaError_t dispatch_adjoint(const Checked& c, const AdjointParams& a, bool plai
 
 cudaError_t dispatch_adjoint_into(const Checked& c, const AdjointParams& a, const LaunchInfo& li,
                                   const CallerScratch& sc, cudaStream_t s) {
-  if (c.filter == DVR_FILTER_PRESHADED) return launch_preshaded_adjoint(c.p, a, c.blend, true, li, s);
   switch (c.tf_mode) {
     case DVR_TF_IDENTITY: return launch_fast_adjoint_into<0>(c.p, a, c.filter, c.blend, li, sc, s);
     case DVR_TF_TEXTURE: return launch_fast_adjoint_into<1>(c.p, a, c.filter, c.blend, li, sc, s);
@@ -665,6 +664,8 @@ int render_adjoint_into(const DvrRendererInputs* inputs, const DvrRendererOutput
     if (!inputs || !outputs_from_forward || !adj_color || !adj_outputs)
       fail(DVR_E_INVALID_ARGUMENT, "arguments must not be NULL");
     Checked c = check_inputs(*inputs);
+    if (c.filter == DVR_FILTER_PRESHADED)
+      fail(DVR_E_UNSUPPORTED, "pre-shaded volumes take dvr_render_adjoint, which orders the rays in library scratch");
     check_outputs(*outputs_from_forward, c, false);
     const AdjointParams a = check_adjoint(*adj_color, *adj_outputs, c);
     DeviceGuard guard(c.device);

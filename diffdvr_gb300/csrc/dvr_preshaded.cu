@@ -28,22 +28,58 @@ cudaError_t forward_go(const RenderParams& p, const LaunchInfo& li, cudaStream_t
 template <int BLEND, typename VT, bool EXACT>
 cudaError_t adjoint_go(const RenderParams& p, const AdjointParams& a, const LaunchInfo& li, cudaStream_t s) {
   const RayOrder order = RayOrder::make(p.W, p.H, p.B);
+  const int64_t total = order.total();
+  if (total > 0x7fffffff) return cudaErrorInvalidConfiguration;
+  // the warp-per-ray record kernel pays off when the rays are too few to fill
+  // the GPU one per lane (1 view of 256^2: 1.2 ms against 4.1 ms); with more
+  // rays the per-lane kernel, which gathers each sample once, is faster
+  // (8 views: 9.5 ms against 12.1 ms)
+  bool record = false;
+  if (EXACT && p.dens != nullptr) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, preshaded_adjoint_kernel<BLEND, VT, true, EXACT>,
+                                                      kFastThreads, 0) != cudaSuccess || per_sm < 1)
+      per_sm = 1;
+    record = int64_t(p.B) * p.H * p.W <= 2 * int64_t(per_sm) * li.num_sms * kFastThreads;
+  }
+  // scratch: the longest-first order, and the leftover list of the record kernel
+  const size_t order_bytes = (work_order_ints(p) * sizeof(int) + 255) & ~size_t(255);
+  const size_t left_bytes = record ? size_t(total) * sizeof(int) : 0;
   cudaError_t err = cudaSuccess;
-  int* ints = static_cast<int*>(acquire_scratch(li.device, s, work_order_ints(p) * sizeof(int), err));
-  if (err != cudaSuccess) return err;
+  char* scratch = static_cast<char*>(acquire_scratch(li.device, s, order_bytes + left_bytes, err));
+  if (!scratch) return err;
+  int* ints = reinterpret_cast<int*>(scratch);
   err = order_rays_by_work(p, &a, ints, li, s);
   if (err != cudaSuccess) return err;
   int* counter = acquire_counter(li.device, s, err);
   if (err != cudaSuccess) return err;
   const int* list = ints + work_order_list_offset;
   const int* count = ints + work_order_count_offset;
-  auto run = [&](auto kernel) {
-    kernel<<<grid_for(kernel, kFastThreads, order.total(), li), kFastThreads, 0, s>>>(p, a, order, counter, list,
-                                                                                     count);
+  auto run = [&](auto kernel, int* ctr, const int* l, const int* c) {
+    kernel<<<grid_for(kernel, kFastThreads, total, li), kFastThreads, 0, s>>>(p, a, order, ctr, l, c);
     return cudaGetLastError();
   };
-  return a.has_volume ? run(preshaded_adjoint_kernel<BLEND, VT, true, EXACT>)
-                      : run(preshaded_adjoint_kernel<BLEND, VT, false, EXACT>);
+  auto per_lane = [&](int* ctr, const int* l, const int* c) {
+    return a.has_volume ? run(preshaded_adjoint_kernel<BLEND, VT, true, EXACT>, ctr, l, c)
+                        : run(preshaded_adjoint_kernel<BLEND, VT, false, EXACT>, ctr, l, c);
+  };
+  if (!record) return per_lane(counter, list, count);
+  // one warp per recorded ray, then one lane per leftover ray
+  int* leftover = reinterpret_cast<int*>(scratch + order_bytes);
+  const bool pos = a.has_camera || a.has_stepsize;
+  auto rec = [&](auto kernel) {
+    kernel<<<grid_for(kernel, kFastThreads, total * 32, li), kFastThreads, 0, s>>>(p, a, order, counter, list, count,
+                                                                                  leftover);
+    return cudaGetLastError();
+  };
+  err = a.has_volume ? (pos ? rec(preshaded_record_adjoint_kernel<BLEND, VT, true, true>)
+                            : rec(preshaded_record_adjoint_kernel<BLEND, VT, true, false>))
+                     : (pos ? rec(preshaded_record_adjoint_kernel<BLEND, VT, false, true>)
+                            : rec(preshaded_record_adjoint_kernel<BLEND, VT, false, false>));
+  if (err != cudaSuccess) return err;
+  int* counter2 = acquire_counter(li.device, s, err);
+  if (err != cudaSuccess) return err;
+  return per_lane(counter2, leftover, counter + 1);
 }
 
 template <typename VT>

@@ -20,6 +20,7 @@
 #pragma once
 #include "dvr_kernels.h"
 #include "dvr_plain.cuh"
+#include "dvr_record.cuh"
 #include "dvr_warpray.cuh"
 
 namespace dvr {
@@ -60,12 +61,16 @@ __device__ __forceinline__ RgbaVolume<VT> rgba_volume(const RenderParams& p) {
 }
 
 // Forward: one warp per ray (dynamic fetch in scanline order), 32 samples
-// per step, opacity in front of each sample by an "over" scan.
+// per step, opacity in front of each sample by an "over" scan.  With a
+// sample record (p.dens), every ray with samples that finds room stores, for
+// sample k, (alpha_k, opacity in front of it) as floats 2k and 2k+1 of its
+// run in the pool, the format of the density path's record.
 template <int BLEND, typename VT>
 __global__ void __launch_bounds__(kFastThreads) preshaded_forward_kernel(const RenderParams p, int* counter) {
   const int lane = threadIdx.x & 31;
   const int rays = p.B * p.H * p.W;
   const RgbaVolume<VT> vol = rgba_volume<VT>(p);
+  unsigned long long* const bump = reinterpret_cast<unsigned long long*>(counter + 2);
   while (true) {
     int pos = 0;
     if (lane == 0) pos = atomicAdd(counter, 1);
@@ -77,6 +82,19 @@ __global__ void __launch_bounds__(kFastThreads) preshaded_forward_kernel(const R
     FastRay q;
     fast_setup(p, x, y, b, q);
     const int kmax = max_samples(q.tmin, q.tmax, q.step);
+    float* rec = nullptr;
+    if (p.dens) {
+      // room for kmax (alpha, opacity) pairs, in groups of 4 floats; -1 without samples or room
+      const unsigned long long claim = static_cast<unsigned long long>((kmax + 1) >> 1);
+      unsigned long long g = 0;
+      if (lane == 0 && kmax > 0) g = atomicAdd(bump, claim);
+      g = __shfl_sync(kFullMask, g, 0);
+      const bool fits = kmax > 0 && g + claim <= static_cast<unsigned long long>(p.dens_units);
+      if (lane == 0)
+        static_cast<int*>(p.dens_off.p)[b * p.dens_off.s[0] + y * p.dens_off.s[1] + x * p.dens_off.s[2]] =
+            fits ? int(g) : -1;
+      if (fits) rec = p.dens + 4 * g;
+    }
     float alpha = 0.f, cr = 0.f, cg = 0.f, cb = 0.f;
     int n = 0;
     for (int k0 = 0; k0 < kmax; k0 += 32) {
@@ -102,6 +120,7 @@ __global__ void __launch_bounds__(kFastThreads) preshaded_forward_kernel(const R
       const unsigned gm = __ballot_sync(kFullMask, go);
       const int f = gm == kFullMask ? 32 : __ffs(~gm) - 1;
       if (lane < f) {
+        if (rec) __stcs(reinterpret_cast<float2*>(rec) + k, make_float2(a, a_in));
         const float w = (1.f - a_in) * a;
         cr = fmaf(w, c.x, cr);
         cg = fmaf(w, c.y, cg);
@@ -312,5 +331,190 @@ __global__ void __launch_bounds__(kFastThreads) preshaded_adjoint_kernel(const R
     }
   }
 }
+
+// Adjoint from the sample record (exact derivatives): one warp per ray, lane
+// j on the j-th of 32 consecutive segments of L = ceil(n / 32) samples, the
+// scheme of the density path's record kernel.  The record gives every
+// sample's incoming opacity, so no blend is inverted; the colours are
+// gathered again.  Each lane composes its segment's affine maps of the
+// opacity adjoint (adj_in = (1 - a) adj_out - a (c . adj_rgb)), a warp suffix
+// scan gives the adjoint at every segment end, and each lane walks its
+// segment back to front: per-cell volume-gradient registers flushed on cell
+// exit, and (POS) the position chain for camera and step-size gradients,
+// summed over the warp per ray.  Rays without a record go to `leftover`.
+template <int BLEND, typename VT, bool VOLGRAD, bool POS>
+__global__ void __launch_bounds__(kFastThreads) preshaded_record_adjoint_kernel(
+    const RenderParams p, const AdjointParams a, const RayOrder order, int* counter, const int* ray_list,
+    const int* ray_count, int* leftover) {
+  const int lane = threadIdx.x & 31;
+  const int total = *ray_count;
+  const RgbaVolume<VT> vol = rgba_volume<VT>(p);
+  float* adjv = VOLGRAD ? static_cast<float*>(a.adj_volume.p) : nullptr;
+  const int64_t gc = a.adj_volume.s[0], gx = a.adj_volume.s[1], gy = a.adj_volume.s[2], gz = a.adj_volume.s[3];
+  while (true) {
+    int pos = 0;
+    if (lane == 0) pos = atomicAdd(counter, 1);
+    pos = __shfl_sync(kFullMask, pos, 0);
+    if (pos >= total) break;
+    const int id = ray_list[pos];
+    int b, x, y;
+    if (!order.pixel(id, b, x, y)) continue;
+    const int n = static_cast<const int*>(a.fwd_term.p)[b * a.fwd_term.s[0] + y * a.fwd_term.s[1] +
+                                                         x * a.fwd_term.s[2]];
+    if (n <= 0) continue;
+    const int g = static_cast<const int*>(p.dens_off.p)[b * p.dens_off.s[0] + y * p.dens_off.s[1] +
+                                                        x * p.dens_off.s[2]];
+    if (g < 0 || int64_t(g) + ((n + 1) >> 1) > p.dens_units) {
+      if (lane == 0) leftover[atomicAdd(counter + 1, 1)] = id;
+      continue;
+    }
+    const float2* rec = reinterpret_cast<const float2*>(p.dens + 4 * size_t(g));
+    FastRay q;
+    fast_setup(p, x, y, b, q);
+    const float* ac = static_cast<const float*>(a.adj_color.p) + b * a.adj_color.s[0] + y * a.adj_color.s[1] +
+                      x * a.adj_color.s[2];
+    const f4 adj_col = mk4(ac[0], ac[a.adj_color.s[3]], ac[2 * a.adj_color.s[3]], ac[3 * a.adj_color.s[3]]);
+    const int L = (n + 31) >> 5;
+    const int s0 = min(n, lane * L), s1 = min(n, s0 + L);
+
+    // cell cache of the four channels' corners
+    int cx = -1, cy = -1, cz = -1;
+    float d[4][8];
+    auto fetch = [&](int k, float& fx, float& fy, float& fz, int& ix, int& iy, int& iz) {
+      const float3 pq = fast_pos(q, q.tmin + k * q.step);
+      ix = int(pq.x), iy = int(pq.y), iz = int(pq.z);
+      fx = pq.x - float(ix), fy = pq.y - float(iy), fz = pq.z - float(iz);
+    };
+
+    // 1. affine map of the segment
+    float A = 1.f, B = 0.f;
+    for (int k = s0; k < s1; ++k) {
+      float fx, fy, fz;
+      int ix, iy, iz;
+      fetch(k, fx, fy, fz, ix, iy, iz);
+      if (ix != cx || iy != cy || iz != cz) {
+        vol.corners(ix, iy, iz, d);
+        cx = ix, cy = iy, cz = iz;
+      }
+      const f4 c = mk4(trilerp(d[0], fx, fy, fz), trilerp(d[1], fx, fy, fz), trilerp(d[2], fx, fy, fz),
+                       trilerp(d[3], fx, fy, fz));
+      const float ak = blend_alpha<BLEND>(c.w, q.step);
+      compose(A, B, 1.f - ak, -ak * (c.x * adj_col.x + c.y * adj_col.y + c.z * adj_col.z));
+    }
+    // 2. opacity adjoint behind each segment: suffix composition over the lanes
+    float SA = A, SB = B;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const float Ao = __shfl_down_sync(kFullMask, SA, o), Bo = __shfl_down_sync(kFullMask, SB, o);
+      if (lane + o < 32) compose(SA, SB, Ao, Bo);
+    }
+    const float NA = __shfl_down_sync(kFullMask, SA, 1), NB = __shfl_down_sync(kFullMask, SB, 1);
+    f4 adj_acc = adj_col;
+    if (lane < 31) adj_acc.w = fmaf(NA, adj_col.w, NB);
+
+    // 3. reverse walk over the segment
+    float gv[4][8];
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+      for (int i = 0; i < 8; ++i) gv[c][i] = 0.f;
+    int vx = -1, vy = -1, vz = -1;  // cell of the gradient registers
+    auto flush = [&]() {
+      if constexpr (VOLGRAD) {
+        if (vx < 0) return;
+        const int lx = clampi(vx, 0, p.X - 1), hx = clampi(vx + 1, 0, p.X - 1);
+        const int ly = clampi(vy, 0, p.Y - 1), hy = clampi(vy + 1, 0, p.Y - 1);
+        const int lz = clampi(vz, 0, p.Z - 1), hz = clampi(vz + 1, 0, p.Z - 1);
+        const bool pair = gz == 1 && hz == lz + 1;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          float* base = adjv + c * gc;
+          VolGradCell<kTrilinear, true>::add_z(base + lx * gx + ly * gy, lz, hz, gz, pair, gv[c][0], gv[c][1]);
+          VolGradCell<kTrilinear, true>::add_z(base + lx * gx + hy * gy, lz, hz, gz, pair, gv[c][2], gv[c][3]);
+          VolGradCell<kTrilinear, true>::add_z(base + hx * gx + ly * gy, lz, hz, gz, pair, gv[c][4], gv[c][5]);
+          VolGradCell<kTrilinear, true>::add_z(base + hx * gx + hy * gy, lz, hz, gz, pair, gv[c][6], gv[c][7]);
+#pragma unroll
+          for (int i = 0; i < 8; ++i) gv[c][i] = 0.f;
+        }
+      }
+    };
+    f3 adj_start = mk3(0, 0, 0), adj_dir = mk3(0, 0, 0);
+    float adj_step = 0.f;
+    for (int k = s1 - 1; k >= s0; --k) {
+      float fx, fy, fz;
+      int ix, iy, iz;
+      fetch(k, fx, fy, fz, ix, iy, iz);
+      if (ix != cx || iy != cy || iz != cz) {
+        vol.corners(ix, iy, iz, d);
+        cx = ix, cy = iy, cz = iz;
+      }
+      if (VOLGRAD && (ix != vx || iy != vy || iz != vz)) {
+        flush();
+        vx = ix, vy = iy, vz = iz;
+      }
+      const f4 c = mk4(trilerp(d[0], fx, fy, fz), trilerp(d[1], fx, fy, fz), trilerp(d[2], fx, fy, fz),
+                       trilerp(d[3], fx, fy, fz));
+      const float ak = blend_alpha<BLEND>(c.w, q.step);
+      const float a_in = __ldg(rec + k).y;
+      f4 adj_cur;
+      const float step_term = blend_adjoint_core<BLEND>(a_in, c, q.step, ak, adj_acc, adj_cur);
+      const float av[4] = {adj_cur.x, adj_cur.y, adj_cur.z, adj_cur.w};
+      if constexpr (VOLGRAD) {
+        const float ux = 1.f - fx, uy = 1.f - fy, uz = 1.f - fz;
+        const float w8[8] = {ux * uy * uz, ux * uy * fz, ux * fy * uz, ux * fy * fz,
+                             fx * uy * uz, fx * uy * fz, fx * fy * uz, fx * fy * fz};
+#pragma unroll
+        for (int ch = 0; ch < 4; ++ch)
+#pragma unroll
+          for (int i = 0; i < 8; ++i) gv[ch][i] = fmaf(av[ch], w8[i], gv[ch][i]);
+      }
+      if constexpr (POS) {
+        f3 adj_vp = mk3(0, 0, 0);
+#pragma unroll
+        for (int ch = 0; ch < 4; ++ch) {
+          f3 g3;
+          trilerp_grad(d[ch], fx, fy, fz, g3);
+          adj_vp.x = fmaf(av[ch], g3.x, adj_vp.x);
+          adj_vp.y = fmaf(av[ch], g3.y, adj_vp.y);
+          adj_vp.z = fmaf(av[ch], g3.z, adj_vp.z);
+        }
+        const float t = q.tmin + k * q.step;
+        const f3 adj_w = mk3(adj_vp.x / q.voxel.x, adj_vp.y / q.voxel.y, adj_vp.z / q.voxel.z);
+        adj_start.x += adj_w.x; adj_start.y += adj_w.y; adj_start.z += adj_w.z;
+        adj_dir.x += adj_w.x * t; adj_dir.y += adj_w.y * t; adj_dir.z += adj_w.z * t;
+        adj_step += step_term + dot3(adj_w, q.dir) * k;
+      }
+    }
+    flush();
+    if constexpr (POS) {
+      float v[7] = {adj_start.x, adj_start.y, adj_start.z, adj_dir.x, adj_dir.y, adj_dir.z, adj_step};
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int i = 0; i < 7; ++i) v[i] += __shfl_xor_sync(kFullMask, v[i], o);
+      if (lane == 0) {
+        if (a.has_stepsize) {
+          float* ps = static_cast<float*>(a.adj_step.p) + b * a.adj_step.s[0] + y * a.adj_step.s[1] +
+                      x * a.adj_step.s[2];
+          if (a.stepsize_broadcast) atomicAdd(ps, v[6]);
+          else *ps = v[6];
+        }
+        if (a.has_camera) {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            if (a.camera_broadcast) {
+              atomic_out(a.adj_start, b, y, x, c, v[c]);
+              atomic_out(a.adj_dir, b, y, x, c, v[3 + c]);
+            } else {
+              write_out(a.adj_start, b, y, x, c, v[c]);
+              write_out(a.adj_dir, b, y, x, c, v[3 + c]);
+            }
+          }
+        }
+      }
+    }
+  }
+}
+
 
 }  // namespace dvr

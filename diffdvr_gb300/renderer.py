@@ -120,13 +120,15 @@ class _RendererFunction(torch.autograd.Function):
         term = torch.empty(B, H, W, dtype=torch.int32, device=volume.device)
         needs_grad = any(ctx.needs_input_grad[:5])
         ckpt = None
-        # pre-shaded volumes take the adjoint that inverts the blend: no checkpoints, no record
+        # pre-shaded volumes need no checkpoints: rays without a record invert the blend
         preshaded = inputs.volume_filter_mode == pyrenderer.VolumeFilterMode.Preshaded
         if needs_grad and checkpoint_interval > 0 and not preshaded:
             slots = pyrenderer.Renderer.checkpoint_slots(inputs, checkpoint_interval)
             ckpt = torch.empty(B, H, W, slots, dtype=torch.float32, device=volume.device)
         outputs = pyrenderer.RendererOutputs(color, term, ckpt, checkpoint_interval)
-        pool = _record_floats(inputs, B, sample_record, volume.device) if ckpt is not None else 0
+        # pre-shaded rays use the record only when they are too few to fill the GPU one per lane
+        recordable = ckpt is not None or (preshaded and needs_grad and checkpoint_interval > 0 and B * H * W <= 1 << 17)
+        pool = _record_floats(inputs, B, sample_record, volume.device) if recordable else 0
         if pool > 0:
             outputs.sample_density = torch.empty(pool, dtype=torch.float32, device=volume.device)
             outputs.sample_offset = torch.empty(B, H, W, dtype=torch.int32, device=volume.device)

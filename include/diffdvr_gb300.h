@@ -126,7 +126,8 @@ typedef struct DvrRendererInputs {
  * absent):
  *  - checkpoints: B*H*W*C float32, the accumulated opacity every
  *    `checkpoint_interval` samples.  C >= ceil(max samples per ray / interval) - 1.
- *  - sample_density + sample_offset (both or neither; need checkpoints): a
+ *  - sample_density + sample_offset (both or neither; need checkpoints,
+ *    except with pre-shaded volumes): a
  *    1-D float32 pool of any size N (16-byte aligned, contiguous, N >= 4) and
  *    a B*H*W int32 tensor.  The forward stores, for every sample k of a ray,
  *    the density and the opacity accumulated in front of the sample as floats
@@ -135,7 +136,9 @@ typedef struct DvrRendererInputs {
  *    index / 4 to sample_offset, or -1 when the pool was full.  The adjoint
  *    then reads these instead of re-sampling the volume and re-marching from
  *    checkpoints; rays with offset -1 re-sample.  Checkpoints are written
- *    only for the rays without a record.  N = B*H*W*S with
+ *    only for the rays without a record.  With pre-shaded volumes the first
+ *    float of a pair is the sample's alpha (there is no density), and the
+ *    adjoint reads the record when the image has few rays.  N = B*H*W*S with
  *    S = 4 * dvr_checkpoint_slots(length, step, 2) holds every ray.
  *    Written and read by the optimized single-instance entry points only. */
 typedef struct DvrRendererOutputs {

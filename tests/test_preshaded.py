@@ -305,3 +305,49 @@ def test_preshaded_validation(cuda_device):
     a.adj_volume = torch.zeros(1, *case.volume.shape[1:], device="cuda")
     with pytest.raises(DvrError, match="adj_volume"):
         pr.Renderer.render_adjoint(inp, out, torch.zeros(1, 5, 6, 4, device="cuda"), a)
+    # the no-allocation adjoint does not order rays in library scratch: it refuses pre-shaded volumes
+    from test_zz_no_alloc import _adjoint_through_abi
+    from diffdvr_gb300 import _abi
+    with pytest.raises(DvrError, match="pre-shaded volumes take dvr_render_adjoint"):
+        _adjoint_through_abi(_abi.load().dvr_render_adjoint_noalloc, case, inp, out,
+                             torch.zeros(1, 5, 6, 4, device="cuda"))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("pool", ["full", 0.5])
+def test_preshaded_adjoint_from_record(pool, oracle_built, cuda_device):
+    """The optimized adjoint from the pre-shaded forward's sample record (one
+    warp per ray; rays without room in the pool go through the per-lane
+    kernel): volume and camera gradients against the oracle's exact variant,
+    and all gradients, step size included, against the per-lane kernel
+    without a record (relative L2 <= 1e-4: the record's opacities against
+    the inverted blend)."""
+    from dvr_cases import gpu_adjoint, gpu_forward
+    O = oracle_built
+    case = preshaded_case(97, 0, 0, W=40, H=36, B=2, shape=(20, 24, 28))
+    inp, out = gpu_forward(case, record="full")
+    if pool != "full":
+        t = out.terminationIndex.cpu().numpy()
+        inp, out = gpu_forward(case, record=int(pool * 4 * ((t + 1) // 2).sum()))
+    off = out.sample_offset.cpu().numpy()
+    term = out.terminationIndex.cpu().numpy()
+    assert (off[term == 0] == -1).all()
+    if pool == "full":
+        assert (off[term > 0] >= 0).all()
+    else:
+        assert ((term > 0) & (off == -1)).any() and ((term > 0) & (off >= 0)).any()
+    g = np.random.default_rng(12).standard_normal(out.color.shape).astype(np.float32) * 0.1
+    got = gpu_adjoint(case, inp, out, g, volume=True, camera=True, stepsize=True)
+    _, plain = gpu_forward(case)
+    lane = gpu_adjoint(case, inp, plain, g, volume=True, camera=True, stepsize=True)
+    for k in got:
+        assert rel_l2(got[k], lane[k]) <= 1e-4, (k, rel_l2(got[k], lane[k]))
+    sc = case.oracle_scene()
+    c64, t64 = O.forward(sc, "port", "f64")
+    c32, t32 = O.forward(sc, "port", "f32")
+    req = O.AdjointRequest(volume=True, camera=True)
+    r64 = O.adjoint(sc, c64, t64, g, req, "port", "f64", exact_preshaded=True)
+    r32 = O.adjoint(sc, c32, t32, g, req, "port", "f32", exact_preshaded=True)
+    for k in r64:
+        tol = max(1e-3, 3 * rel_l2(r32[k], r64[k]))
+        assert rel_l2(got[k], r64[k]) <= tol, (k, rel_l2(got[k], r64[k]), tol)
