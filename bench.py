@@ -523,7 +523,10 @@ def run_gpu(args):
     peak, peak_kind = measured_peaks()
     V = int(np.prod(w.volume.shape[1:])) * (4 if w.filter_mode == 3 else 1)  # pre-shaded: 4 channels
     P = B * H * W
-    ck_written = int(torch.clamp((term.to(torch.int64) - 1) // K, min=0).clamp_max(slots).sum().item())
+    ck_per_ray = torch.clamp((term.to(torch.int64) - 1) // K, min=0).clamp_max(slots)
+    if pool > 0:  # recorded rays write no checkpoints
+        ck_per_ray = torch.where(out.sample_offset >= 0, torch.zeros_like(ck_per_ray), ck_per_ray)
+    ck_written = int(ck_per_ray.sum().item())
     s_v = vol_s.element_size()
     if forward_method:
         # volume once, colour + termination, the forward variables written once and read once
