@@ -358,6 +358,9 @@ Checked check_inputs(const DvrRendererInputs& in) {
   c.blend = in.blend_mode;
   p.early_out = float(in.blending_early_out);
   p.B = B;
+  // ray and pixel indices are 32-bit in the kernels
+  if (int64_t(B) * p.H * p.W > 0x7fffffff)
+    fail(DVR_E_INVALID_ARGUMENT, "batch x height x width must be below 2^31 rays");
   return c;
 }
 
