@@ -492,11 +492,20 @@ __global__ void __launch_bounds__(kFwdVarsThreads) forward_variables_to_gradient
   const int b = blockIdx.y;
   const int E = v.has_tf ? v.R * v.C : 0;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const bool tf_smem = E > 0 && E * nw <= kFwdVarsSmemFloats;
+  // shared memory: the warps' TF sums, then each entry's derivative index
+  const bool tf_smem = E > 0 && E * (nw + 1) <= kFwdVarsSmemFloats;
   float* acc = fv_smem + warp * E;
-  if (tf_smem)
-    for (int e = lane; e < E; e += 32) acc[e] = 0.f;
+  int* s_idx = reinterpret_cast<int*>(fv_smem + nw * E);
   const int* dtf = E > 0 ? v.d_tf + b * v.dtf_s[0] : nullptr;
+  if (tf_smem) {
+    for (int e = lane; e < E; e += 32) acc[e] = 0.f;
+    for (int e = threadIdx.x; e < E; e += blockDim.x) {
+      const int r = e / v.C, c = e - r * v.C;
+      const int idx = __ldg(dtf + r * v.dtf_s[1] + c * v.dtf_s[2]);
+      s_idx[e] = idx >= 0 && idx < v.D ? idx : -1;
+    }
+    __syncthreads();
+  }
   float* tf_out = E > 0 ? v.adj_tf + b * v.tf_s[0] : nullptr;
   const bool vec = v.fwd_s[4] == 1 && v.fwd_s[3] == 4 && (reinterpret_cast<uintptr_t>(v.fwd) & 15u) == 0 &&
                    (v.fwd_s[2] & 3) == 0 && (v.fwd_s[1] & 3) == 0 && (v.fwd_s[0] & 3) == 0;
@@ -541,13 +550,20 @@ __global__ void __launch_bounds__(kFwdVarsThreads) forward_variables_to_gradient
       if (my_acc) atomicAdd(o, val);
       else *o = val;
     }
-    for (int e = lane; e < E; e += 32) {
-      const int r = e / v.C, c = e - r * v.C;
-      const int idx = __ldg(dtf + r * v.dtf_s[1] + c * v.dtf_s[2]);
-      if (idx < 0 || idx >= v.D) continue;
-      const float val = dotd(idx);
-      if (tf_smem) acc[e] += val;
-      else atomicAdd(tf_out + r * v.tf_s[1] + c * v.tf_s[2], val);
+    if (tf_smem) {
+      // indices from shared memory: the row reads of a pixel are independent
+#pragma unroll 4
+      for (int e = lane; e < E; e += 32) {
+        const int idx = s_idx[e];
+        if (idx >= 0) acc[e] += dotd(idx);
+      }
+    } else {
+      for (int e = lane; e < E; e += 32) {
+        const int r = e / v.C, c = e - r * v.C;
+        const int idx = __ldg(dtf + r * v.dtf_s[1] + c * v.dtf_s[2]);
+        if (idx < 0 || idx >= v.D) continue;
+        atomicAdd(tf_out + r * v.tf_s[1] + c * v.tf_s[2], dotd(idx));
+      }
     }
   }
   if (tf_smem) {

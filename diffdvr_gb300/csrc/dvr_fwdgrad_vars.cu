@@ -12,7 +12,7 @@ cudaError_t launch_forward_variables_to_gradients(const FwdVarsParams& v, const 
   if (pixels == 0 || v.B == 0) return cudaSuccess;
   constexpr int nw = kFwdVarsThreads / 32;
   const int E = v.has_tf ? v.R * v.C : 0;
-  const size_t smem = E > 0 && E * nw <= kFwdVarsSmemFloats ? size_t(E) * nw * sizeof(float) : 0;
+  const size_t smem = E > 0 && E * (nw + 1) <= kFwdVarsSmemFloats ? size_t(E) * (nw + 1) * sizeof(float) : 0;
   // about four blocks per SM in total, fewer when the image is small
   const int per_b = std::max(1, std::min((pixels + nw - 1) / nw, (4 * li.num_sms + v.B - 1) / v.B));
   const dim3 grid(per_b, v.B);

@@ -86,7 +86,7 @@ struct FwdGradParams {
 // forwardVariablesToGradients: forward variables and output adjoint in,
 // enabled gradients out.  Indices are -1 or in [0, D).
 constexpr int kFwdVarsThreads = 256;        // 8 warps, one pixel each at a time
-constexpr int kFwdVarsSmemFloats = 12288;   // per-warp TF sums in shared memory (48 KB), else global atomics
+constexpr int kFwdVarsSmemFloats = 12288;   // per-warp TF sums + entry indices in shared memory (48 KB), else global atomics
 struct FwdVarsParams {
   int32_t B, H, W, D;
   int32_t R, C;
