@@ -49,12 +49,6 @@ int64_t instance_items(const RenderParams& p) {
   return int64_t(p.B) * ((p.W + kTileW - 1) / kTileW) * ((p.H + kTileH - 1) / kTileH);
 }
 
-size_t max_tf_entries(const RenderParams* ps, int n) {
-  size_t m = 0;
-  for (int i = 0; i < n; ++i) m = std::max(m, size_t(ps[i].R) * ps[i].C);
-  return m;
-}
-
 template <int TF>
 cudaError_t fwd_tf(const BatchForwardTable& t, int n_items, size_t smem, int vst, int filter, int blend,
                    cudaStream_t s) {

@@ -3,7 +3,6 @@ round trips, the header layout, x-fastest file order, the reference's own
 C60Large.cvol where the reference sources are present, and known values of
 the Marschner-Lobb function."""
 import os
-import struct
 
 import numpy as np
 import pytest
