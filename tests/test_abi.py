@@ -218,3 +218,149 @@ def test_forward_mode_interface():
     Renderer(optimize_camera=True, gradient_method="forward", forward_delayed_gradients=True)
     with pytest.raises(AssertionError):
         Renderer(optimize_volume=True, gradient_method="forward")
+
+
+# ---------------------------------------------------------------- forward mode and pre-shading
+def _settings(D=3, step=0, start=(-1, -1, -1), dirs=(-1, -1, -1), d_tf=None, has_tf=None):
+    s = _abi.DvrForwardDifferencesSettings()
+    s.D, s.d_stepsize = D, step
+    for k in range(3):
+        s.d_ray_start[k], s.d_ray_dir[k] = start[k], dirs[k]
+    if d_tf is None:
+        s.d_tf = _fake(())
+        s.d_tf.ndim = -1
+    else:
+        s.d_tf = d_tf
+    s.has_tf_derivatives = int(d_tf is not None if has_tf is None else has_tf)
+    return s
+
+
+def _no_gpu():
+    """Descriptors that pass every check reach the launch; their pointers are
+    fake, so such cases run only where there is no GPU to launch on."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("fake device pointers: validation pass-through is checked without a GPU only")
+
+
+def _preshaded_inputs():
+    i = _inputs()
+    i.volume_filter_mode, i.tf_mode = 3, 5
+    i.volume = _fake((4, 4, 5, 6))
+    i.tf = _fake((1, 1, 1))
+    return i
+
+
+# renderer/renderer.cpp:419-498
+@pytest.mark.parametrize("make,expect", [
+    (lambda: (_inputs(), _settings(D=0), _fake((1, 7, 8, 1, 4))), "number of derivatives must be positive"),
+    (lambda: (_inputs(), _settings(step=-1), _fake((1, 7, 8, 3, 4))), "at least one derivative must be activated"),
+    (lambda: (_inputs(), _settings(step=5), _fake((1, 7, 8, 3, 4))), "d_stepsize = 5 is not a derivative index"),
+    (lambda: (_inputs(), _settings(start=(0, 1, 7)), _fake((1, 7, 8, 3, 4))), "d_rayStart = 7"),
+    (lambda: (_inputs(), _settings(has_tf=True), _fake((1, 7, 8, 3, 4))), "d_tf not defined"),
+    (lambda: (_inputs(), _settings(d_tf=_fake((1, 8, 4))), _fake((1, 7, 8, 3, 4))), "d_tf must be of type int32"),
+    (lambda: (_inputs(), _settings(d_tf=_fake((1, 2, 4), _abi.DVR_INT32)), _fake((1, 7, 8, 3, 4))),
+     "d_tf must have 8 entries at dimension 1"),
+    (lambda: (_inputs(), _settings(), _fake((1, 7, 8, 2, 4))), "gradientsOut must have 3 entries at dimension 3"),
+    (lambda: (_inputs(), _settings(), _fake((1, 7, 8, 3, 4), _abi.DVR_FLOAT64)), "gradientsOut must be of type float32"),
+    (lambda: (_preshaded_inputs(), _settings(), _fake((1, 7, 8, 3, 4))),
+     "forward derivatives are not available for pre-shaded volumes"),
+    (lambda: (_inputs(), _settings(d_tf=_fake((1, 8, 4), _abi.DVR_INT32)), _fake((1, 7, 8, 3, 4))), None),
+])
+def test_forward_gradients_validation(dvr_lib, make, expect):
+    if expect is None:
+        _no_gpu()
+    i, s, g = make()
+    o = _outputs()
+    code = dvr_lib.dvr_render_forward_gradients(ctypes.byref(i), ctypes.byref(s), ctypes.byref(o), ctypes.byref(g),
+                                                None)
+    msg = dvr_lib.dvr_last_error().decode()
+    if expect is None:
+        assert code == _abi.DVR_E_CUDA, msg  # every check passed; no GPU here
+    else:
+        assert code in (_abi.DVR_E_INVALID_ARGUMENT, _abi.DVR_E_UNSUPPORTED)
+        assert expect in msg, msg
+
+
+def _adj_outputs(**kw):
+    a = _abi.DvrAdjointOutputs()
+    for name in ("adj_volume", "adj_stepsize", "adj_camera_ray_start", "adj_camera_ray_dir", "adj_tf", "adj_viewport"):
+        t = _fake(())
+        t.ndim = -1
+        setattr(a, name, t)
+    for k, v in kw.items():
+        setattr(a, k, v)
+    return a
+
+
+# renderer/renderer.cpp:500-558
+@pytest.mark.parametrize("make,expect", [
+    (lambda: (_fake((1, 7, 8, 3, 4), cuda=False), _fake((1, 7, 8, 4)), _settings(), _adj_outputs()), "is a CPU tensor"),
+    (lambda: (_fake((1, 7, 8, 3, 4)), _fake((1, 6, 8, 4)), _settings(), _adj_outputs()),
+     "gradientOutputColor must have 7 entries at dimension 1"),
+    (lambda: (_fake((1, 7, 8, 3, 4)), _fake((1, 7, 8, 4)), _settings(),
+              _adj_outputs(has_volume_derivatives=1, adj_volume=_fake((1, 4, 5, 6)))),
+     "volume derivatives are not supported with forward variables"),
+    (lambda: (_fake((1, 7, 8, 3, 4)), _fake((1, 7, 8, 4)), _settings(dirs=(9, -1, -1)), _adj_outputs()),
+     "d_rayDir = 9 is not a derivative index"),
+    (lambda: (_fake((1, 7, 8, 3, 4)), _fake((1, 7, 8, 4)), _settings(),
+              _adj_outputs(has_tf_derivatives=1, adj_tf=_fake((1, 8, 4)))),
+     "TF derivatives need the TF derivative indices"),
+    (lambda: (_fake((1, 7, 8, 3, 4)), _fake((1, 7, 8, 4)), _settings(d_tf=_fake((1, 8, 4), _abi.DVR_INT32)),
+              _adj_outputs(has_tf_derivatives=1, adj_tf=_fake((1, 8, 5)))), "adj_tf must have 4 entries at dimension 2"),
+    (lambda: (_fake((1, 7, 8, 3, 4)), _fake((1, 7, 8, 4)), _settings(),
+              _adj_outputs(has_stepsize_derivatives=1, adj_stepsize=_fake((1, 7, 8)))), None),
+])
+def test_forward_variables_to_gradients_validation(dvr_lib, make, expect):
+    if expect is None:
+        _no_gpu()
+    fv, ac, s, a = make()
+    code = dvr_lib.dvr_forward_variables_to_gradients(ctypes.byref(fv), ctypes.byref(ac), ctypes.byref(s),
+                                                      ctypes.byref(a), None)
+    msg = dvr_lib.dvr_last_error().decode()
+    if expect is None:
+        assert code == _abi.DVR_E_CUDA, msg
+    else:
+        assert code == _abi.DVR_E_INVALID_ARGUMENT and expect in msg, msg
+
+
+# renderer/tf_utils.cpp:173-249
+@pytest.mark.parametrize("make,expect", [
+    (lambda: (_fake((2, 4, 5, 6)), _fake((1, 8, 4)), 1, _fake((4, 4, 5, 6))),
+     "densityVolume must have 1 entries at dimension 0"),
+    (lambda: (_fake((1, 4, 5, 6)), _fake((2, 8, 4)), 1, _fake((4, 4, 5, 6))), "tf must have 1 entries at dimension 0"),
+    (lambda: (_fake((1, 4, 5, 6)), _fake((1, 8, 5)), 1, _fake((4, 4, 5, 6))), "tf must have 4 entries at dimension 2"),
+    (lambda: (_fake((1, 4, 5, 6)), _fake((1, 8, 6)), 6, _fake((4, 4, 5, 6))), "TFGaussianLog is not supported"),
+    (lambda: (_fake((1, 4, 5, 6)), _fake((1, 8, 4)), 1, _fake((3, 4, 5, 6))), "color must have 4 entries at dimension 0"),
+    (lambda: (_fake((1, 4, 5, 6)), _fake((1, 8, 4)), 1, _fake((4, 4, 5, 7))), "color must have 6 entries at dimension 3"),
+    (lambda: (_fake((1, 4, 5, 6)), _fake((1, 8, 4)), 1, _fake((4, 4, 5, 6))), None),
+])
+def test_preshade_volume_validation(dvr_lib, make, expect):
+    if expect is None:
+        _no_gpu()
+    d, tf, mode, out = make()
+    code = dvr_lib.dvr_preshade_volume(ctypes.byref(d), ctypes.byref(tf), mode, ctypes.byref(out), None)
+    msg = dvr_lib.dvr_last_error().decode()
+    if expect is None:
+        assert code == _abi.DVR_E_CUDA, msg
+    else:
+        assert code in (_abi.DVR_E_INVALID_ARGUMENT, _abi.DVR_E_UNSUPPORTED) and expect in msg, msg
+
+
+def test_preshade_volume_adjoint_validation(dvr_lib):
+    d, tf = _fake((1, 4, 5, 6)), _fake((1, 8, 4))
+    code = dvr_lib.dvr_preshade_volume_adjoint(ctypes.byref(d), ctypes.byref(tf), 1, ctypes.byref(_fake((4, 4, 5, 6))),
+                                               ctypes.byref(_fake((2, 4, 5, 6))), None)
+    msg = dvr_lib.dvr_last_error().decode()
+    assert code == _abi.DVR_E_INVALID_ARGUMENT and "adj_density must have 1 entries at dimension 0" in msg
+
+
+def test_preshaded_inputs_validation(dvr_lib):
+    _no_gpu()
+    i, o = _preshaded_inputs(), _outputs()
+    code, msg = _forward(dvr_lib, i, o)
+    assert code == _abi.DVR_E_CUDA, msg  # valid pre-shaded inputs: every check passes
+    o.sample_density = _fake((64,))
+    o.sample_offset = _fake((1, 7, 8), _abi.DVR_INT32)
+    code, msg = _forward(dvr_lib, i, o)
+    assert code == _abi.DVR_E_CUDA, msg  # a record without checkpoints is fine for pre-shaded volumes
