@@ -364,3 +364,22 @@ def test_preshaded_inputs_validation(dvr_lib):
     o.sample_offset = _fake((1, 7, 8), _abi.DVR_INT32)
     code, msg = _forward(dvr_lib, i, o)
     assert code == _abi.DVR_E_CUDA, msg  # a record without checkpoints is fine for pre-shaded volumes
+
+
+def test_forward_method_derivative_layout():
+    """The forward method's derivative indices: the six ray components first,
+    then the TF entries row-major, one index per entry and batch entry
+    (pytests/diffdvr/renderer.py:63-80)."""
+    import torch
+    from diffdvr_gb300.renderer import _forward_settings
+    tf = torch.zeros(2, 3, 4)
+    s = _forward_settings(True, True, tf)
+    assert s.D == 6 + 12
+    assert tuple(s.d_rayStart) == (0, 1, 2) and tuple(s.d_rayDir) == (3, 4, 5)
+    assert s.has_tf_derivatives and s.d_tf.dtype == torch.int32 and tuple(s.d_tf.shape) == (2, 3, 4)
+    assert torch.equal(s.d_tf[0], torch.arange(6, 18, dtype=torch.int32).reshape(3, 4))
+    assert torch.equal(s.d_tf[1], s.d_tf[0])
+    s = _forward_settings(False, True, tf)
+    assert s.D == 12 and tuple(s.d_rayStart) == (-1, -1, -1) and int(s.d_tf.min()) == 0
+    s = _forward_settings(True, False, tf)
+    assert s.D == 6 and not s.has_tf_derivatives and s.d_tf is None
