@@ -295,11 +295,22 @@ __global__ void __launch_bounds__(kFwdThreads) forward_gradients_kernel(const Re
     const int rem = pos - b * p.H * p.W;
     const int y = rem / p.W, x = rem - y * p.W;
 
-    for (int i = lane; i < g.dn; i += 32) J[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    __syncwarp();
     FastRay q;
     fast_setup(p, x, y, b, q);
     const int kmax = max_samples(q.tmin, q.tmax, q.step);
+    if (kmax == 0) {
+      // no samples: zero colour and derivatives, written straight to the outputs
+      float* out = g.grad + b * g.grad_s[0] + y * g.grad_s[1] + x * g.grad_s[2] + g.d0 * g.grad_s[3];
+      for (int e = lane; e < 4 * g.dn; e += 32) out[(e >> 2) * g.grad_s[3] + (e & 3) * g.grad_s[4]] = 0.f;
+      if (lane == 0) {
+        float* col = static_cast<float*>(p.color.p) + b * p.color.s[0] + y * p.color.s[1] + x * p.color.s[2];
+        col[0] = col[p.color.s[3]] = col[2 * p.color.s[3]] = col[3 * p.color.s[3]] = 0.f;
+        static_cast<int*>(p.term.p)[b * p.term.s[0] + y * p.term.s[1] + x * p.term.s[2]] = 0;
+      }
+      continue;
+    }
+    for (int i = lane; i < g.dn; i += 32) J[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncwarp();
     const VolumeFast<VT> vol{static_cast<const VT*>(p.volume.p) + b * p.volume.s[0], int(p.volume.s[1]),
                              int(p.volume.s[2]), int(p.volume.s[3]), p.X - 1, p.Y - 1, p.Z - 1};
     const TfShared<C> tf{s_tf + (copies > 1 ? b : 0) * p.R * C, p.R};
