@@ -383,3 +383,43 @@ def test_forward_method_derivative_layout():
     assert s.D == 12 and tuple(s.d_rayStart) == (-1, -1, -1) and int(s.d_tf.min()) == 0
     s = _forward_settings(True, False, tf)
     assert s.D == 6 and not s.has_tf_derivatives and s.d_tf is None
+
+
+def test_header_is_plain_c_and_links(dvr_lib, tmp_path):
+    """The boundary is plain C: a C99 program includes the header, links the
+    library and calls it (version, checkpoint sizing, a validation failure
+    with its message) without a GPU."""
+    import shutil
+    import subprocess
+    from diffdvr_gb300 import _abi as abi
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not available")
+    src = tmp_path / "probe.c"
+    src.write_text(r"""
+#include <stdio.h>
+#include <string.h>
+#include "diffdvr_gb300.h"
+int main(void) {
+  if (dvr_abi_version() != DVR_ABI_VERSION) return 1;
+  if (dvr_checkpoint_slots(1.7320508, 0.001, 16) <= 0) return 2;
+  if (dvr_checkpoint_slots(1.0, -1.0, 16) >= 0) return 3;
+  DvrRendererInputs in;
+  DvrRendererOutputs out;
+  memset(&in, 0, sizeof in);
+  memset(&out, 0, sizeof out);
+  in.volume.ndim = 3;  /* must be 4 */
+  int code = dvr_render_forward(&in, &out, NULL);
+  if (code != DVR_E_INVALID_ARGUMENT) return 4;
+  if (strstr(dvr_last_error(), "volume must be a tensor with 4 dimensions") == NULL) return 5;
+  printf("ok %d\n", dvr_abi_version());
+  return 0;
+}
+""")
+    lib_dir = os.path.dirname(abi.library_path())
+    exe = tmp_path / "probe"
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+                        str(src), "-L", lib_dir, "-ldvr_gb300", f"-Wl,-rpath,{lib_dir}", "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0 and r.stdout.strip() == "ok 4", (r.returncode, r.stdout, r.stderr)
