@@ -79,7 +79,7 @@ def build(reference: bool = True, quiet: bool = True) -> None:
     out = subprocess.DEVNULL if quiet else None
     subprocess.run(["make", "-C", HERE, "-j2", "all"], check=True, stdout=out)
     if reference and os.path.isdir(REFERENCE_SOURCES):
-        subprocess.run(["make", "-C", HERE, "-j2", "ref", f"REF_DIR={REFERENCE_SOURCES}"],
+        subprocess.run(["make", "-C", HERE, "-j3", "ref", f"REF_DIR={REFERENCE_SOURCES}"],
                        check=True, stdout=out)
 
 
@@ -250,7 +250,20 @@ def adjoint(scene: Scene, color: np.ndarray, term: np.ndarray, adj_color: np.nda
     dt = _dtype(lib)
     keep: list = []
     inp = _inputs(scene, dt, keep)
-    B, H, W = inp.batch, scene.height, scene.width
+    out, res = _adjoint_outputs(scene, req, inp.batch, dt, keep)
+    tc =_tensor(np.asarray(color, dtype=dt), keep)
+    tt = _tensor(np.asarray(term, dtype=np.int32), keep)
+    ta = _tensor(np.asarray(adj_color, dtype=dt), keep)
+    rc = lib.oracle_adjoint(ctypes.byref(inp), ctypes.byref(tc), ctypes.byref(tt), ctypes.byref(ta),
+                            ctypes.byref(out))
+    if rc != 0:
+        raise RuntimeError(f"oracle_adjoint failed with code {rc}")
+    return res
+
+
+def _adjoint_outputs(scene: Scene, req: AdjointRequest, B: int, dt, keep: list):
+    """Zeroed gradient arrays for the request and the OracleAdjointOutputs over them."""
+    H, W = scene.height, scene.width
     out = OracleAdjointOutputs()
     res = {}
     if req.volume:
@@ -277,14 +290,22 @@ def adjoint(scene: Scene, color: np.ndarray, term: np.ndarray, adj_color: np.nda
         out.has_stepsize = 1
         out.stepsize_broadcast = int(tuple(shp) != (B, H, W))
         out.adj_stepsize = _tensor(res["adj_stepsize"], keep)
-    tc =_tensor(np.asarray(color, dtype=dt), keep)
-    tt = _tensor(np.asarray(term, dtype=np.int32), keep)
-    ta = _tensor(np.asarray(adj_color, dtype=dt), keep)
-    rc = lib.oracle_adjoint(ctypes.byref(inp), ctypes.byref(tc), ctypes.byref(tt), ctypes.byref(ta),
-                            ctypes.byref(out))
-    if rc != 0:
-        raise RuntimeError(f"oracle_adjoint failed with code {rc}")
-    return res
+    return out, res
+
+
+def reference_image_check(scene: Scene, req: AdjointRequest, precision: str = "f32") -> int:
+    """0 when the parameter-block images of oracle/ref_image.h (which the GPU
+    harness oracle/ref_device.cu builds) equal what the reference's own
+    accessor constructors make of the same inputs and gradient outputs, else
+    the number of the failing check (oracle_ref_image_check)."""
+    lib = load("reference", precision)
+    lib.oracle_ref_image_check.argtypes = [ctypes.POINTER(OracleInputs), ctypes.POINTER(OracleAdjointOutputs)]
+    lib.oracle_ref_image_check.restype = ctypes.c_int
+    dt = _dtype(lib)
+    keep: list = []
+    inp = _inputs(scene, dt, keep)
+    out, _ = _adjoint_outputs(scene, req, inp.batch, dt, keep)
+    return int(lib.oracle_ref_image_check(ctypes.byref(inp), ctypes.byref(out)))
 
 
 @dataclass

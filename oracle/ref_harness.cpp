@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 #include "renderer_kernels.cuh"
 #include "dvr_oracle.h"
+#include "ref_image.h"
 
 namespace {
 
@@ -37,6 +38,20 @@ kernel::RendererInputs build_inputs(const OracleInputs* in) {
   r.tf = make_acc<kernel::Tensor3Read>(in->tf);
   r.blendingEarlyOut = real_t(in->blending_early_out);
   return r;
+}
+
+kernel::AdjointOutputs build_adjoint(const OracleAdjointOutputs* out) {
+  kernel::AdjointOutputs o;
+  if (out->has_volume) o.adj_volume = make_acc<kernel::BTensor4RW>(out->adj_volume);
+  o.stepSizeHasBroadcasting = out->stepsize_broadcast != 0;
+  if (out->has_stepsize) o.adj_stepSize = make_acc<kernel::BTensor3RW>(out->adj_stepsize);
+  o.cameraHasBroadcasting = out->camera_broadcast != 0;
+  if (out->has_camera) {
+    o.adj_cameraRayStart = make_acc<kernel::BTensor4RW>(out->adj_ray_start);
+    o.adj_cameraRayDir = make_acc<kernel::BTensor4RW>(out->adj_ray_dir);
+  }
+  if (out->has_tf) o.adj_tf = make_acc<kernel::BTensor3RW>(out->adj_tf);
+  return o;
 }
 
 template <kernel::VolumeFilterMode F, kernel::CameraMode C, kernel::TFMode T, kernel::BlendMode B>
@@ -132,19 +147,30 @@ extern "C" int oracle_adjoint(const OracleInputs* in, const OracleTensor* color,
   kernel::RendererOutputsAsInput fwd{make_acc<kernel::Tensor4Read>(*color),
                                      make_acc<kernel::ITensor3Read>(*termination)};
   kernel::AdjointColor_t ac = make_acc<kernel::AdjointColor_t>(*adj_color);
-  kernel::AdjointOutputs o;
-  if (out->has_volume) o.adj_volume = make_acc<kernel::BTensor4RW>(out->adj_volume);
-  o.stepSizeHasBroadcasting = out->stepsize_broadcast != 0;
-  if (out->has_stepsize) o.adj_stepSize = make_acc<kernel::BTensor3RW>(out->adj_stepsize);
-  o.cameraHasBroadcasting = out->camera_broadcast != 0;
-  if (out->has_camera) {
-    o.adj_cameraRayStart = make_acc<kernel::BTensor4RW>(out->adj_ray_start);
-    o.adj_cameraRayDir = make_acc<kernel::BTensor4RW>(out->adj_ray_dir);
-  }
-  if (out->has_tf) o.adj_tf = make_acc<kernel::BTensor3RW>(out->adj_tf);
+  kernel::AdjointOutputs o = build_adjoint(out);
   const int flags = (out->has_stepsize ? 1 : 0) | (out->has_camera ? 2 : 0) | (out->has_tf ? 4 : 0) |
                     (out->has_volume ? 8 : 0);
   if (flags == 0) return 3;
   dim3 vs(unsigned(in->width), unsigned(in->height), unsigned(in->batch));
   return dispatch<AdjFn>(in->filter_mode, in->camera_mode, in->tf_mode, in->blend_mode, vs, inputs, fwd, ac, o, flags);
+}
+
+// The parameter-block images of ref_image.h against the reference's own
+// constructors: 0 when the constructors produce exactly what the images
+// encode (so the GPU harness, which has no constructors, passes the
+// reference's kernels the blocks its host code would), else the failing check.
+extern "C" int oracle_ref_image_check(const OracleInputs* in, const OracleAdjointOutputs* out) {
+  const kernel::RendererInputs by_ctor = build_inputs(in);
+  if (!dvr_ref::inputs_match(by_ctor, *in)) return 1;
+  alignas(kernel::RendererInputs) unsigned char ibuf[sizeof(kernel::RendererInputs)];
+  auto* img = reinterpret_cast<kernel::RendererInputs*>(ibuf);
+  dvr_ref::inputs_image(*in, img);
+  if (!dvr_ref::inputs_match(*img, *in)) return 2;
+  const kernel::AdjointOutputs o = build_adjoint(out);
+  if (!dvr_ref::adjoint_match(o, *out)) return 3;
+  alignas(kernel::AdjointOutputs) unsigned char obuf[sizeof(kernel::AdjointOutputs)];
+  auto* oimg = reinterpret_cast<kernel::AdjointOutputs*>(obuf);
+  dvr_ref::adjoint_image(*out, oimg);
+  if (!dvr_ref::adjoint_match(*oimg, *out)) return 4;
+  return 0;
 }

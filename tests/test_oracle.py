@@ -155,3 +155,64 @@ def test_port_matches_reference_all_modes(oracle_built):
         g2 = O.adjoint(sc, c2, t2, adj, req, "reference", "f64")
         for k in g1:
             assert rel_l2(g1[k], g2[k]) <= 1e-12 or symmetric_error(g1[k], g2[k]) <= 1e-12, k
+
+
+@pytest.mark.parametrize("camera_mode", [0, 1, 2])
+def test_reference_parameter_block_images(oracle_built, camera_mode):
+    """The GPU harness of the reference's CUDA kernels (oracle/ref_device.cu)
+    has no accessor constructors: it writes each parameter block as a byte
+    image (oracle/ref_image.h).  Here, on the CPU, the reference's own
+    constructors build the same blocks from the same inputs, and every field
+    of both, read through the accessors' getters, must agree: sizes, element
+    strides, stride 0 for broadcast dimensions, pointers, scalars."""
+    O = oracle_built
+    if not O.reference_available():
+        pytest.skip("reference sources not present")
+    case = make_case(40 + camera_mode, tf_mode=1, camera_mode=camera_mode, B=2)
+    sc = case.oracle_scene()
+    for precision in ("f32", "f64"):
+        req = O.AdjointRequest(volume=True, tf=True, camera=camera_mode == 0, stepsize=True)
+        assert O.reference_image_check(sc, req, precision) == 0, precision
+    # broadcast inputs and gradients: size-1 batch (and pixel) dimensions
+    g = golden("broadcast.npz")
+    bsc = golden_case(g, "b_").oracle_scene()
+    req = O.AdjointRequest(volume=True, tf=True, camera=True, stepsize=True, stepsize_shape=(1, 1, 1),
+                           camera_batch=1, volume_batch=1)
+    assert O.reference_image_check(bsc, req, "f32") == 0
+    assert O.reference_image_check(bsc, O.AdjointRequest(tf=True), "f32") == 0
+
+
+def test_reference_cuda_kernel_names(oracle_built, tmp_path):
+    """Every kernel oracle/ref_cuda.py launches is defined by
+    oracle/ref_device.cu (read from its preprocessed source, not the cubin),
+    and each adjoint kernel instantiates the reference's template with the
+    derivative switches its name states."""
+    import re
+    import shutil
+    import subprocess
+    O = oracle_built
+    if not O.reference_available():
+        pytest.skip("reference sources not present")
+    from oracle import ref_cuda as R
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    out = tmp_path / "ref_device.ii"
+    subprocess.run([nvcc, "-E", "-std=c++17", "-DUSE_DOUBLE_PRECISION=0", "-DNDEBUG", "-w", "-I", O.HERE,
+                    "-I", f"{O.HERE}/ref_shim", "-I", O.REFERENCE_SOURCES, f"{O.HERE}/ref_device.cu", "-o", str(out)],
+                   check=True)
+    src = out.read_text()
+    defined = set(re.findall(r"void (ref_\w+)\s*\(", src))
+    want = {"ref_build_params"}
+    for tfm, filt, blend, cam in all_mode_combos():
+        sc = O.Scene(width=1, height=1, volume=None, tf=None, step_size=None, box_min=None, box_size=None,
+                     filter_mode=filt, camera_mode=cam, tf_mode=tfm, blend_mode=blend)
+        want.add(R.forward_kernel_name(sc))
+        want.add(R.adjoint_kernel_name(sc, True, cam == 0, True, False, True))
+    sc = O.Scene(width=1, height=1, volume=None, tf=None, step_size=None, box_min=None, box_size=None)
+    for delayed in (False, True):
+        want.add(R.adjoint_kernel_name(sc, False, False, True, delayed, False))
+    assert want == defined, (sorted(want - defined), sorted(defined - want))
+    adj = list(re.finditer(r"void (ref_adj_\w+)\s*\(.*?DvrKernelAdjointImpl<[^>]*?,\s*(\d),\s*(\d),\s*(\d),"
+                           r"\s*(\d),\s*(\d)\s*>", src, re.S))
+    assert len(adj) == sum(n.startswith("ref_adj_") for n in want)
+    for m in adj:
+        assert m.group(1).endswith("_" + "".join(m.group(i) for i in range(2, 7))), m.group(1)
