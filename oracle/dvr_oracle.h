@@ -13,7 +13,10 @@
  *                               compiled from its headers (ref_harness.cpp),
  *                               only where the reference sources are present.
  * Both take identical arguments so the Python wrapper (oracle.py) can call
- * either one and the tests can pin the restatement to the reference.
+ * either one and the tests can pin the restatement to the reference.  The
+ * reference's CUDA kernels, compiled from the same headers into
+ * _ref/ref_kernels_sm103a.cubin (ref_device.cu), take the same structs on
+ * the GPU (ref_cuda.py).
  *
  * All real-valued buffers hold `real_t` = float (f32 build) or double (f64
  * build).  Tensors follow the reference memory layout
