@@ -216,3 +216,53 @@ def test_reference_cuda_kernel_names(oracle_built, tmp_path):
     assert len(adj) == sum(n.startswith("ref_adj_") for n in want)
     for m in adj:
         assert m.group(1).endswith("_" + "".join(m.group(i) for i in range(2, 7))), m.group(1)
+
+
+def _edge_cases():
+    """Degenerate inputs the marcher must handle: (name, case)."""
+    cases = []
+    c = make_case(61, shape=(1, 2, 3), W=1, H=1, B=1)
+    cases.append(("1x1 image, one-voxel x axis", c))
+    c = make_case(62, shape=(2, 1, 1), W=3, H=2, B=2)
+    cases.append(("one-voxel y and z axes", c))
+    c = make_case(63, W=5, H=4, B=2)
+    c.ray_dir = -c.ray_dir  # every ray points away from the box
+    cases.append(("all rays miss the box", c))
+    c = make_case(64, W=5, H=4, B=1)
+    c.step = 4.0  # longer than the box diagonal: at most one sample per ray
+    cases.append(("one sample per ray", c))
+    c = make_case(65, W=5, H=4, B=1)
+    c.early_out = 0.0  # stop after the first sample with any opacity
+    cases.append(("early out at zero opacity", c))
+    c = make_case(66, W=6, H=5, B=1)
+    c.width, c.height = 0, 0
+    c.ray_start, c.ray_dir = c.ray_start[:, :0, :0], c.ray_dir[:, :0, :0]
+    cases.append(("empty image", c))
+    return cases
+
+
+@pytest.mark.parametrize("filter_mode", [0, 1])
+def test_port_matches_reference_edge_cases(oracle_built, filter_mode):
+    """Degenerate inputs: the restatement against the reference's own CPU
+    templates, FP64, forward and every gradient."""
+    O = oracle_built
+    if not O.reference_available():
+        pytest.skip("reference sources not present")
+    for name, case in _edge_cases():
+        case.filter_mode = filter_mode
+        sc = case.oracle_scene()
+        c1, t1 = O.forward(sc, "port", "f64")
+        c2, t2 = O.forward(sc, "reference", "f64")
+        assert np.array_equal(t1, t2), name
+        assert c1.size == 0 or symmetric_error(c1, c2) <= 1e-12, name
+        if name == "all rays miss the box":
+            assert not t1.any() and not c1.any(), name
+        if name == "one sample per ray":
+            assert t1.max() <= 1, name
+        adj = np.random.default_rng(3).normal(size=c1.shape)
+        req = O.AdjointRequest(volume=True, tf=True, camera=True, stepsize=True)
+        g1 = O.adjoint(sc, c2, t2, adj, req, "port", "f64")
+        g2 = O.adjoint(sc, c2, t2, adj, req, "reference", "f64")
+        for k in g1:
+            assert g1[k].size == 0 or rel_l2(g1[k], g2[k]) <= 1e-12 or symmetric_error(g1[k], g2[k]) <= 1e-12, (
+                name, k)
