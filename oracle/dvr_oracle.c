@@ -14,11 +14,10 @@
  *
  * Citations are to files of the reference project (shamanDevel/DiffDVR).
  */
-#include "dvr_oracle.h"
-
 #include <math.h>
 #include <stddef.h>
 #include <stdlib.h>
+#include <string.h>
 
 #if DVR_ORACLE_DOUBLE
 typedef double real_t;
@@ -37,6 +36,10 @@ typedef float real_t;
 #define R_FMIN fminf
 #define R_FMAX fmaxf
 #endif
+
+/* real_t is this build's; the header declares the per-step components with it */
+#define DVR_ORACLE_HAS_REAL_T 1
+#include "dvr_oracle.h"
 
 typedef struct { real_t x, y, z; } v3;
 typedef struct { real_t x, y, z, w; } v4;
@@ -483,6 +486,17 @@ static inline v3 volume_pos(const RaySetup* r, real_t t) {
   return mk3((w.x - r->bmin.x) / r->voxel.x, (w.y - r->bmin.y) / r->voxel.y, (w.z - r->bmin.z) / r->voxel.z);
 }
 
+/* adjoint of volumePos = (start + t*dir - boxMin) / voxelSize at t = tmin + k*step,
+ * tmin held fixed (:407-412): accumulates into the ray start, direction and step */
+static inline void ray_step_adjoint(const RaySetup* r, real_t t, int k, v3 adj_vp, v3* adj_start, v3* adj_dir,
+                                    real_t* adj_step) {
+  const v3 adj_w = mk3(adj_vp.x / r->voxel.x, adj_vp.y / r->voxel.y, adj_vp.z / r->voxel.z);
+  adj_start->x += adj_w.x; adj_start->y += adj_w.y; adj_start->z += adj_w.z;
+  adj_dir->x += adj_w.x * t; adj_dir->y += adj_w.y * t; adj_dir->z += adj_w.z * t;
+  const real_t adj_t = dot3(adj_w, r->dir);
+  *adj_step += adj_t * k;
+}
+
 static int check_modes(const OracleInputs* in) {
   /* pre-shaded: filter 3 together with TF 5 (renderer/renderer.cpp:72-80) */
   const int preshaded = in->filter_mode == 3;
@@ -680,12 +694,7 @@ int oracle_adjoint(const OracleInputs* in, const OracleTensor* color, const Orac
         const real_t adj_density = tf_adjoint(in, b, density, adj_cur, out);
         adj_vp = sample_adjoint(&s, in->filter_mode, adj_density);
       }
-      /* chain through volumePos = (start + t*dir - boxMin) / voxelSize (:407-412) */
-      const v3 adj_w = mk3(adj_vp.x / r.voxel.x, adj_vp.y / r.voxel.y, adj_vp.z / r.voxel.z);
-      adj_start.x += adj_w.x; adj_start.y += adj_w.y; adj_start.z += adj_w.z;
-      adj_dir.x += adj_w.x * t; adj_dir.y += adj_w.y * t; adj_dir.z += adj_w.z * t;
-      const real_t adj_t = dot3(adj_w, r.dir);
-      adj_step += adj_t * k;
+      ray_step_adjoint(&r, t, k, adj_vp, &adj_start, &adj_dir, &adj_step);
     }
     if (in->filter_mode == 3) rgba_flush(&rs);
     else sampler_flush(&s, in->filter_mode);
@@ -1033,5 +1042,112 @@ int oracle_preshade_volume_adjoint(const OracleTensor* density, const OracleTens
                          *at4(adj_color, 3, x, y, z));
         *at4(adj_density, 0, x, y, z) = tf_adjoint(&in, 0, *at4(density, 0, x, y, z), a, &none);
       }
+  return 0;
+}
+
+/* ---- per-step components, exported for the per-component adjoint tests
+ * (the reference's unittests/testAdjoint{Blending,TF,Interpolation,Camera}.cpp):
+ * each runs the function the march above uses, on one step. */
+
+int oracle_blend_step(int mode, const real_t* acc, const real_t* cur, real_t step, real_t* out) {
+  const v4 r = blend(mode, mk4(acc[0], acc[1], acc[2], acc[3]), mk4(cur[0], cur[1], cur[2], cur[3]), step);
+  out[0] = r.x; out[1] = r.y; out[2] = r.z; out[3] = r.w;
+  return 0;
+}
+
+int oracle_blend_step_adjoint(int mode, const real_t* acc_out, const real_t* cur, real_t step, const real_t* adj_out,
+                              real_t* acc_in, real_t* adj_acc_in, real_t* adj_cur, real_t* adj_step) {
+  v4 aa = mk4(adj_out[0], adj_out[1], adj_out[2], adj_out[3]), ac;
+  const v4 prev = blend_adjoint(mode, mk4(acc_out[0], acc_out[1], acc_out[2], acc_out[3]),
+                                mk4(cur[0], cur[1], cur[2], cur[3]), step, &aa, &ac, adj_step);
+  acc_in[0] = prev.x; acc_in[1] = prev.y; acc_in[2] = prev.z; acc_in[3] = prev.w;
+  adj_acc_in[0] = aa.x; adj_acc_in[1] = aa.y; adj_acc_in[2] = aa.z; adj_acc_in[3] = aa.w;
+  adj_cur[0] = ac.x; adj_cur[1] = ac.y; adj_cur[2] = ac.z; adj_cur[3] = ac.w;
+  return 0;
+}
+
+int oracle_tf_step(const OracleTensor* tf, int tf_mode, real_t density, real_t* out) {
+  if (tf_mode < 0 || tf_mode > 3) return 2;
+  OracleInputs in;
+  preshade_inputs(tf, tf_mode, &in);
+  const v4 c = tf_eval(&in, 0, density);
+  out[0] = c.x; out[1] = c.y; out[2] = c.z; out[3] = c.w;
+  return 0;
+}
+
+int oracle_tf_step_adjoint(const OracleTensor* tf, int tf_mode, real_t density, const real_t* adj, OracleTensor* adj_tf,
+                           real_t* adj_density) {
+  if (tf_mode < 0 || tf_mode > 3) return 2;
+  OracleInputs in;
+  preshade_inputs(tf, tf_mode, &in);
+  OracleAdjointOutputs out;
+  memset(&out, 0, sizeof out);
+  if (adj_tf && adj_tf->data) {
+    out.has_tf = 1;
+    out.adj_tf = *adj_tf;
+  }
+  *adj_density = tf_adjoint(&in, 0, density, mk4(adj[0], adj[1], adj[2], adj[3]), &out);
+  return 0;
+}
+
+static void component_sampler(const OracleTensor* volume, OracleTensor* adj_volume, Sampler* s) {
+  memset(s, 0, sizeof *s);
+  s->X = (int)volume->sizes[1]; s->Y = (int)volume->sizes[2]; s->Z = (int)volume->sizes[3];
+  s->vol = volume;
+  s->adj = adj_volume;
+  s->has_adj = adj_volume && adj_volume->data;
+  s->li[0] = s->li[1] = s->li[2] = -1;
+}
+
+/* pos: volume (voxel) coordinates of batch entry 0 */
+int oracle_sample_step(const OracleTensor* volume, int filter, const real_t* pos, real_t* density) {
+  if (filter != 0 && filter != 1) return 2;
+  Sampler s;
+  component_sampler(volume, NULL, &s);
+  *density = sample_forward(&s, filter, mk3(pos[0], pos[1], pos[2]));
+  return 0;
+}
+
+int oracle_sample_step_adjoint(const OracleTensor* volume, int filter, const real_t* pos, real_t adj_density,
+                               real_t* adj_pos, OracleTensor* adj_volume) {
+  if (filter != 0 && filter != 1) return 2;
+  Sampler s;
+  component_sampler(volume, adj_volume, &s);
+  (void)sample_adjoint_fetch(&s, filter, mk3(pos[0], pos[1], pos[2]));
+  const v3 g = sample_adjoint(&s, filter, adj_density);
+  sampler_flush(&s, filter);
+  adj_pos[0] = g.x; adj_pos[1] = g.y; adj_pos[2] = g.z;
+  return 0;
+}
+
+/* n positions volumePos(t_k), t_k = tmin + k*step, of one ray, and their adjoint */
+int oracle_ray_steps(const real_t* start, const real_t* dir, const real_t* box_min, const real_t* voxel, real_t tmin,
+                     real_t step, int n, real_t* pos) {
+  RaySetup r;
+  r.start = mk3(start[0], start[1], start[2]); r.dir = mk3(dir[0], dir[1], dir[2]);
+  r.bmin = mk3(box_min[0], box_min[1], box_min[2]); r.voxel = mk3(voxel[0], voxel[1], voxel[2]);
+  r.step = step; r.tmin = tmin; r.tmax = tmin + n * step;
+  for (int k = 0; k < n; ++k) {
+    const v3 p = volume_pos(&r, r.tmin + k * r.step);
+    pos[3 * k] = p.x; pos[3 * k + 1] = p.y; pos[3 * k + 2] = p.z;
+  }
+  return 0;
+}
+
+int oracle_ray_steps_adjoint(const real_t* start, const real_t* dir, const real_t* box_min, const real_t* voxel,
+                             real_t tmin, real_t step, int n, const real_t* adj_pos, real_t* adj_start, real_t* adj_dir,
+                             real_t* adj_step) {
+  RaySetup r;
+  r.start = mk3(start[0], start[1], start[2]); r.dir = mk3(dir[0], dir[1], dir[2]);
+  r.bmin = mk3(box_min[0], box_min[1], box_min[2]); r.voxel = mk3(voxel[0], voxel[1], voxel[2]);
+  r.step = step; r.tmin = tmin; r.tmax = tmin + n * step;
+  v3 as = mk3(0, 0, 0), ad = mk3(0, 0, 0);
+  real_t at = 0;
+  for (int k = n - 1; k >= 0; --k)
+    ray_step_adjoint(&r, r.tmin + k * r.step, k, mk3(adj_pos[3 * k], adj_pos[3 * k + 1], adj_pos[3 * k + 2]), &as, &ad,
+                     &at);
+  adj_start[0] = as.x; adj_start[1] = as.y; adj_start[2] = as.z;
+  adj_dir[0] = ad.x; adj_dir[1] = ad.y; adj_dir[2] = ad.z;
+  *adj_step = at;
   return 0;
 }

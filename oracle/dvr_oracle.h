@@ -110,6 +110,38 @@ void oracle_set_exact_preshaded(int exact);
 /* Size of real_t in this build (4 or 8). */
 int oracle_real_size(void);
 
+#ifdef DVR_ORACLE_HAS_REAL_T
+/* Port only: one step of each part of the march, as the march computes it,
+ * for per-component adjoint tests.  Vectors are real_t[4] (r, g, b, opacity
+ * or absorption) or real_t[3]; TFs and volumes are batch entry 0.
+ * blend: the accumulator after compositing `cur` over `acc`.  Its adjoint
+ * inverts the blend (acc_in, from acc_out) and maps the accumulator's adjoint
+ * to those of acc_in, cur and the step size (the latter ASSIGNED, as the
+ * reference's blend adjoint does). */
+int oracle_blend_step(int mode, const real_t* acc, const real_t* cur, real_t step, real_t* out);
+int oracle_blend_step_adjoint(int mode, const real_t* acc_out, const real_t* cur, real_t step, const real_t* adj_out,
+                              real_t* acc_in, real_t* adj_acc_in, real_t* adj_cur, real_t* adj_step);
+/* TF evaluation at one density, and its adjoint: d/d density returned in
+ * *adj_density, TF gradient accumulated into adj_tf (skipped when null). */
+int oracle_tf_step(const OracleTensor* tf, int tf_mode, real_t density, real_t* out);
+int oracle_tf_step_adjoint(const OracleTensor* tf, int tf_mode, real_t density, const real_t* adj, OracleTensor* adj_tf,
+                           real_t* adj_density);
+/* One volume sample at a position in voxel coordinates (filter 0 nearest,
+ * 1 trilinear), and its adjoint: d/d position written to adj_pos, volume
+ * gradient accumulated into adj_volume (skipped when null). */
+int oracle_sample_step(const OracleTensor* volume, int filter, const real_t* pos, real_t* density);
+int oracle_sample_step_adjoint(const OracleTensor* volume, int filter, const real_t* pos, real_t adj_density,
+                               real_t* adj_pos, OracleTensor* adj_volume);
+/* The n sample positions (start + t*dir - box_min) / voxel, t = tmin + k*step,
+ * of one ray (pos: n x 3), and their adjoint for the ray start, direction and
+ * step size (tmin held fixed, as in the march). */
+int oracle_ray_steps(const real_t* start, const real_t* dir, const real_t* box_min, const real_t* voxel, real_t tmin,
+                     real_t step, int n, real_t* pos);
+int oracle_ray_steps_adjoint(const real_t* start, const real_t* dir, const real_t* box_min, const real_t* voxel,
+                             real_t tmin, real_t step, int n, const real_t* adj_pos, real_t* adj_start, real_t* adj_dir,
+                             real_t* adj_step);
+#endif
+
 #ifdef __cplusplus
 }
 #endif

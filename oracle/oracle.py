@@ -422,3 +422,122 @@ def preshade_volume_adjoint(density: np.ndarray, tf: np.ndarray, tf_mode: int, a
     if rc != 0:
         raise RuntimeError(f"oracle_preshade_volume_adjoint failed with code {rc}")
     return out
+
+
+# ---------------------------------------------------------------- per-step components
+def _component_lib(precision: str):
+    """The port library with the per-step component entry points typed for its real_t."""
+    lib = load("port", precision)
+    if not getattr(lib, "_components_typed", False):
+        R = ctypes.c_double if lib.oracle_real_size() == 8 else ctypes.c_float
+        P = ctypes.POINTER(R)
+        T = ctypes.POINTER(OracleTensor)
+        i = ctypes.c_int
+        lib.oracle_blend_step.argtypes = [i, P, P, R, P]
+        lib.oracle_blend_step_adjoint.argtypes = [i, P, P, R, P, P, P, P, P]
+        lib.oracle_tf_step.argtypes = [T, i, R, P]
+        lib.oracle_tf_step_adjoint.argtypes = [T, i, R, P, T, P]
+        lib.oracle_sample_step.argtypes = [T, i, P, P]
+        lib.oracle_sample_step_adjoint.argtypes = [T, i, P, R, P, T]
+        lib.oracle_ray_steps.argtypes = [P, P, P, P, R, R, i, P]
+        lib.oracle_ray_steps_adjoint.argtypes = [P, P, P, P, R, R, i, P, P, P, P]
+        lib._components_typed = True
+        lib._real = R
+    return lib
+
+
+def _vec(v, lib, keep: list, n: Optional[int] = None):
+    a = np.ascontiguousarray(v if n is None else np.zeros(n), dtype=np.float64 if lib._real is ctypes.c_double
+                             else np.float32)
+    keep.append(a)
+    return a, a.ctypes.data_as(ctypes.POINTER(lib._real))
+
+
+def _ok(rc: int, what: str) -> None:
+    if rc != 0:
+        raise RuntimeError(f"{what} failed with code {rc}")
+
+
+def blend_step(mode: int, acc, cur, step: float, precision: str = "f64") -> np.ndarray:
+    """The accumulator after compositing cur (r, g, b, absorption) over acc."""
+    lib, keep = _component_lib(precision), []
+    out, po = _vec(None, lib, keep, 4)
+    _ok(lib.oracle_blend_step(mode, _vec(acc, lib, keep)[1], _vec(cur, lib, keep)[1], step, po), "blend_step")
+    return out
+
+
+def blend_step_adjoint(mode: int, acc_out, cur, step: float, adj_out, precision: str = "f64"):
+    """(acc_in recovered by inverting the blend, adj_acc_in, adj_cur, adj_step)."""
+    lib, keep = _component_lib(precision), []
+    acc_in, p1 = _vec(None, lib, keep, 4)
+    adj_acc, p2 = _vec(None, lib, keep, 4)
+    adj_cur, p3 = _vec(None, lib, keep, 4)
+    adj_step, p4 = _vec(None, lib, keep, 1)
+    _ok(lib.oracle_blend_step_adjoint(mode, _vec(acc_out, lib, keep)[1], _vec(cur, lib, keep)[1], step,
+                                      _vec(adj_out, lib, keep)[1], p1, p2, p3, p4), "blend_step_adjoint")
+    return acc_in, adj_acc, adj_cur, float(adj_step[0])
+
+
+def tf_step(tf: np.ndarray, tf_mode: int, density: float, precision: str = "f64") -> np.ndarray:
+    """TF (1 R C) evaluated at one density: (r, g, b, absorption)."""
+    lib, keep = _component_lib(precision), []
+    t = _tensor(_vec(tf, lib, keep)[0], keep)
+    out, po = _vec(None, lib, keep, 4)
+    _ok(lib.oracle_tf_step(ctypes.byref(t), tf_mode, density, po), "tf_step")
+    return out
+
+
+def tf_step_adjoint(tf: np.ndarray, tf_mode: int, density: float, adj, precision: str = "f64"):
+    """(d/d density, TF gradient 1 R C) of adj . tf(density)."""
+    lib, keep = _component_lib(precision), []
+    t = _tensor(_vec(tf, lib, keep)[0], keep)
+    g, _ = _vec(np.zeros_like(tf), lib, keep)
+    tg = _tensor(g, keep)
+    ad, pd = _vec(None, lib, keep, 1)
+    _ok(lib.oracle_tf_step_adjoint(ctypes.byref(t), tf_mode, density, _vec(adj, lib, keep)[1], ctypes.byref(tg), pd),
+        "tf_step_adjoint")
+    return float(ad[0]), g
+
+
+def sample_step(volume: np.ndarray, filter_mode: int, pos, precision: str = "f64") -> float:
+    """Volume (1 X Y Z) sampled at a position in voxel coordinates."""
+    lib, keep = _component_lib(precision), []
+    v = _tensor(_vec(volume, lib, keep)[0], keep)
+    d, pd = _vec(None, lib, keep, 1)
+    _ok(lib.oracle_sample_step(ctypes.byref(v), filter_mode, _vec(pos, lib, keep)[1], pd), "sample_step")
+    return float(d[0])
+
+
+def sample_step_adjoint(volume: np.ndarray, filter_mode: int, pos, adj_density: float, precision: str = "f64"):
+    """(d/d position, volume gradient 1 X Y Z) of adj_density * sample(pos)."""
+    lib, keep = _component_lib(precision), []
+    v = _tensor(_vec(volume, lib, keep)[0], keep)
+    g, _ = _vec(np.zeros_like(volume), lib, keep)
+    tg = _tensor(g, keep)
+    ap, pp = _vec(None, lib, keep, 3)
+    _ok(lib.oracle_sample_step_adjoint(ctypes.byref(v), filter_mode, _vec(pos, lib, keep)[1], adj_density, pp,
+                                       ctypes.byref(tg)), "sample_step_adjoint")
+    return ap, g
+
+
+def ray_steps(start, direction, box_min, voxel, tmin: float, step: float, n: int, precision: str = "f64"):
+    """The n sample positions of one ray in voxel coordinates (n x 3)."""
+    lib, keep = _component_lib(precision), []
+    pos, pp = _vec(None, lib, keep, 3 * n)
+    _ok(lib.oracle_ray_steps(_vec(start, lib, keep)[1], _vec(direction, lib, keep)[1], _vec(box_min, lib, keep)[1],
+                             _vec(voxel, lib, keep)[1], tmin, step, n, pp), "ray_steps")
+    return pos.reshape(n, 3)
+
+
+def ray_steps_adjoint(start, direction, box_min, voxel, tmin: float, step: float, adj_pos, precision: str = "f64"):
+    """(adj_start, adj_dir, adj_step) of sum(adj_pos * positions)."""
+    lib, keep = _component_lib(precision), []
+    n = int(np.asarray(adj_pos).shape[0])
+    a1, p1 = _vec(None, lib, keep, 3)
+    a2, p2 = _vec(None, lib, keep, 3)
+    a3, p3 = _vec(None, lib, keep, 1)
+    _ok(lib.oracle_ray_steps_adjoint(_vec(start, lib, keep)[1], _vec(direction, lib, keep)[1],
+                                     _vec(box_min, lib, keep)[1], _vec(voxel, lib, keep)[1], tmin, step, n,
+                                     _vec(np.asarray(adj_pos).reshape(-1), lib, keep)[1], p1, p2, p3),
+        "ray_steps_adjoint")
+    return a1, a2, float(a3[0])
