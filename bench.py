@@ -22,8 +22,10 @@ Arms:
 
 Other configurations of the metric (`--workload`, not the default line):
 absorption_recon_128 (volume gradient, 64 views into 128^3), large_mixed_512
-(512^3 BF16, 16 views at 1024^2, ray + volume + TF gradients) and
-plain_cpu_64 (the CPU-sized case).
+(512^3 BF16, 16 views at 1024^2, ray + volume + TF gradients),
+batched_uneven_32 (32 instances of different volume and image sizes through
+the batched entry points, one CUDA graph per step) and plain_cpu_64 (the
+CPU-sized case).
 
 --method forward times the forward method of the same workload instead
 (render_forward_gradients tracing one derivative per TF entry, and camera
@@ -70,6 +72,12 @@ WORKLOADS = {
     "plain_cpu_64": {
         "desc": "plain_cpu_64: 64^3 blobs, linear TF R=8, one 128x128 view, step 0.5 voxel, TF + volume grads",
         "camera": "frame", "interval": 16, "estimate": "target", "res": 64, "views": 1, "image": 128},
+    "batched_uneven_32": {
+        "desc": "batched_uneven_32: 32 instances in one batched call per pass, volume edges from "
+                "{32,64,96,128,192,256}, images from {64,128,256,512}^2, 16 blobs, sum of 4 Gaussians TF, "
+                "step 0.5 voxel, TF + volume grads",
+        "camera": "rays", "interval": 16, "estimate": "target", "res": 256, "views": 1, "image": 512,
+        "instances": 32},
 }
 
 
@@ -185,6 +193,8 @@ class ClockSampler:
 # ------------------------------------------------------------------ workload
 def make_workload(args):
     from diffdvr_gb300 import scenes
+    if args.workload == "batched_uneven_32":
+        return scenes.batched_uneven(seed=3, n=WORKLOADS[args.workload]["instances"])
     if args.workload == "absorption_recon_128":
         return scenes.absorption_recon_128(seed=2, views=args.views, image=args.image)
     if args.workload == "large_mixed_512":
@@ -603,6 +613,246 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+def run_gpu_batched(args):
+    """The batched-uneven workload: every instance's forward in one
+    render_forward_batched call and every adjoint in one
+    render_adjoint_batched call (one launch per 24 instances each), the
+    per-instance L2-loss gradients between them, the step captured in one
+    CUDA graph.  value = samples of all instances / step time."""
+    import torch
+    import torch.distributed as dist
+    from diffdvr_gb300 import _abi, pyrenderer as pr
+
+    if args.method != "adjoint":
+        raise SystemExit("the batched entry points have no forward method")
+    rank, world, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    _abi.load()
+    spec = WORKLOADS[args.workload]
+    ws = make_workload(args)
+    sdt = {"bf16": torch.bfloat16, "f16": torch.float16, "f32": torch.float32}[args.storage]
+    K = args.interval or spec["interval"]
+    pr.set_kernel_family("optimized")
+
+    def inputs(w, volume, tf_t, rs, rd):
+        inp = pr.RendererInputs()
+        inp.screen_size = pr.int2(w.width, w.height)
+        inp.volume = volume
+        inp.volume_filter_mode = pr.VolumeFilterMode(w.filter_mode)
+        inp.box_min = pr.real3(*w.box_min)
+        inp.box_size = pr.real3(*w.box_size)
+        inp.camera_mode = pr.CameraMode.RayStartDir
+        inp.camera = pr.CameraPerPixelRays(rs, rd)
+        inp.step_size = float(w.step_size)
+        inp.tf_mode = pr.TFMode(w.tf_mode)
+        inp.tf = tf_t
+        inp.blend_mode = pr.BlendMode(w.blend_mode)
+        return inp
+
+    I = []  # per instance: device tensors, inputs, outputs, gradients
+    g = torch.Generator(device="cpu").manual_seed(3)
+    for w in ws:
+        d = {"w": w}
+        d["vol_s"] = torch.from_numpy(w.volume).to(dev).to(sdt)
+        d["tf"] = torch.from_numpy(w.tf).to(dev)
+        d["rs"], d["rd"] = torch.from_numpy(w.ray_start).to(dev), torch.from_numpy(w.ray_dir).to(dev)
+        d["inp"] = inputs(w, d["vol_s"], d["tf"], d["rs"], d["rd"])
+        slots = pr.Renderer.checkpoint_slots(d["inp"], K)
+        d["color"] = torch.empty(1, w.height, w.width, 4, device=dev)
+        d["term"] = torch.empty(1, w.height, w.width, dtype=torch.int32, device=dev)
+        d["out"] = pr.RendererOutputs(d["color"], d["term"],
+                                      torch.empty(1, w.height, w.width, slots, device=dev), K)
+        d["slots"] = slots
+        a = pr.AdjointOutputs()
+        a.has_tf_derivatives = True
+        a.tf_delayed_accumulation = True
+        a.adj_tf = torch.zeros(d["tf"].shape, device=dev)
+        a.has_volume_derivatives = True
+        a.adj_volume = torch.zeros(d["vol_s"].shape, device=dev)
+        d["adj"] = a
+        d["adj_color"] = torch.empty_like(d["color"])
+        # target image: the instance's TF perturbed by N(0, 0.05)
+        tf_t = (d["tf"].cpu() + 0.05 * torch.randn(d["tf"].shape, generator=g)).clamp_min(0).to(dev)
+        tf_t[..., 5] = d["tf"][..., 5]  # keep the Gaussians' widths positive as drawn
+        d["target"] = torch.empty_like(d["color"])
+        pr.Renderer.render_forward(inputs(w, d["vol_s"], tf_t, d["rs"], d["rd"]),
+                                   pr.RendererOutputs(d["target"], torch.empty_like(d["term"])))
+        d["inv_n"] = 1.0 / d["color"].numel()
+        I.append(d)
+    torch.cuda.synchronize()
+    ins, outs = [d["inp"] for d in I], [d["out"] for d in I]
+    adjs, aos = [d["adj_color"] for d in I], [d["adj"] for d in I]
+
+    stream = torch.cuda.Stream(device=dev)
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    fwd_ev, adj_ev = [], []
+
+    def loss_grads(targets=None):
+        for j, d in enumerate(I):
+            torch.sub(d["color"], d["target"] if targets is None else targets[j], out=d["adj_color"])
+            d["adj_color"].mul_(2 * d["inv_n"])
+            d["adj"].adj_tf.zero_()
+            d["adj"].adj_volume.zero_()
+
+    def step(record=False):
+        if record:
+            e = (ev(), ev(), ev(), ev())
+            e[0].record()
+        pr.Renderer.render_forward_batched(ins, outs)
+        if record:
+            e[1].record()
+        loss_grads()
+        if record:
+            e[2].record()
+        pr.Renderer.render_adjoint_batched(ins, outs, adjs, aos)
+        if record:
+            e[3].record()
+            fwd_ev.append((e[0], e[1]))
+            adj_ev.append((e[2], e[3]))
+
+    with torch.cuda.stream(stream):
+        step()
+    torch.cuda.synchronize()
+    samples = sum(int(d["term"].to(torch.int64).sum().item()) for d in I)
+
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(stream):
+        step()
+        torch.cuda.synchronize()
+        with torch.cuda.graph(graph, stream=stream):
+            step()
+    torch.cuda.synchronize()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        starts = [ev() for _ in range(steps)]
+        stops = [ev() for _ in range(steps)]
+        cur = torch.cuda.current_stream()
+        for i in range(steps):
+            flush.zero_()
+            starts[i].record(cur)
+            fn()
+            stops[i].record(cur)
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        return sum(a.elapsed_time(b) for a, b in zip(starts, stops)) / steps
+
+    with torch.cuda.stream(stream):
+        with ClockSampler(local) as clocks:
+            ms_graph = timed(lambda: graph.replay(), args.steps, args.warmup)
+    clock_summary = clocks.summary()
+
+    with torch.cuda.stream(stream):
+        for _ in range(max(3, args.steps // 2)):
+            flush.zero_()
+            step(record=True)
+        torch.cuda.synchronize()
+    fwd_ms = float(np.mean([a.elapsed_time(b) for a, b in fwd_ev]))
+    adj_ms = float(np.mean([a.elapsed_time(b) for a, b in adj_ev]))
+
+    # ---- e2e: the batched public API with every input copied from pinned host memory
+    host = [{k: d[k].cpu().pin_memory() for k in ("vol_s", "tf", "rs", "rd", "target")} for d in I]
+    devc = [{k: torch.empty_like(d[k]) for k in ("vol_s", "tf", "rs", "rd", "target")} for d in I]
+    ins_e2e = [inputs(d["w"], c["vol_s"], c["tf"], c["rs"], c["rd"]) for d, c in zip(I, devc)]
+    loss_d = torch.empty(len(I), device=dev)
+    loss_host = torch.empty(len(I), pin_memory=True)
+    grad_host = [torch.empty(d["tf"].shape, pin_memory=True) for d in I]
+
+    def e2e_step():
+        for h, c in zip(host, devc):
+            for k in h:
+                c[k].copy_(h[k], non_blocking=True)
+        pr.Renderer.render_forward_batched(ins_e2e, outs)
+        loss_grads([c["target"] for c in devc])
+        for j, d in enumerate(I):
+            loss_d[j] = (d["adj_color"] * d["adj_color"]).sum() / (4 * d["inv_n"] * d["inv_n"])
+        pr.Renderer.render_adjoint_batched(ins_e2e, outs, adjs, aos)
+        loss_host.copy_(loss_d, non_blocking=True)
+        for gh, d in zip(grad_host, I):
+            gh.copy_(d["adj"].adj_tf, non_blocking=True)
+
+    with torch.cuda.stream(stream):
+        ms_e2e = timed(e2e_step, args.steps, args.warmup)
+    h2d = sum(sum(t.numel() * t.element_size() for t in h.values()) for h in host)
+    d2h = loss_host.numel() * 4 + sum(gh.numel() * 4 for gh in grad_host)
+
+    ms_graph, ms_e2e = max_over_ranks([ms_graph, ms_e2e], world, dev)
+    value = job_rate(samples, world, ms_graph)
+    e2e_value = job_rate(samples, world, ms_e2e)
+
+    # ---- roofline: compulsory bytes summed over the instances of one batched launch pair
+    peak, peak_kind = measured_peaks()
+    fwd_bytes = adj_bytes = 0
+    for d in I:
+        w = d["w"]
+        V = int(np.prod(w.volume.shape[1:]))
+        P = w.width * w.height
+        ck = int(torch.clamp((d["term"].to(torch.int64) - 1) // K, min=0).clamp_max(d["slots"]).sum().item())
+        S = int(d["term"].to(torch.int64).sum().item())
+        f, a = algorithmic_bytes(w, d["vol_s"].element_size(), V, P, S, ck, False, False, d["tf"].numel())
+        fwd_bytes += f
+        adj_bytes += a
+    dominant = ("adjoint", adj_bytes, adj_ms) if adj_ms >= fwd_ms else ("forward", fwd_bytes, fwd_ms)
+    achieved = dominant[1] / (dominant[2] / 1e3) / 1e9
+    s_v = I[0]["vol_s"].element_size()
+    launches = -(-len(I) // 24)  # one persistent launch per 24 instances and pass
+
+    result = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "samples/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_graph,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": f"{args.storage}-storage/f32-compute",
+        "data": "synthetic (seeded, shapes and distributions of the workload)",
+        "config": {"workload": spec["desc"], "volume_storage": args.storage, "instances": len(I),
+                   "volume_edges": [int(d["w"].volume.shape[1]) for d in I],
+                   "image_edges": [int(d["w"].width) for d in I], "gradients": ["tf", "volume"],
+                   "samples_per_step": samples, "checkpoint_interval": K,
+                   "l2": "flushed (256 MB write) before every timed step",
+                   "graph": "batched forward + loss gradients + batched adjoint captured in one CUDA graph",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": e2e_value, "unit": "samples/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": ms_e2e,
+                "path": "pyrenderer.Renderer.render_forward_batched/render_adjoint_batched, pinned host inputs"},
+        "gpu_launches": 2 * launches * args.steps,
+        "kernel_ms": {"forward": fwd_ms, "adjoint": adj_ms},
+        "roofline": {"bound": "hbm", "kernel": dominant[0], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_launch": int(dominant[1]),
+                     "gather_model_GBps": samples * 8 * s_v * 2 / ((fwd_ms + adj_ms) / 1e3) / 1e9},
+        "clocks": clock_summary,
+    }
+    if rank == 0:
+        if args.no_cpu:
+            result["cpu_baseline"] = None
+        else:
+            from oracle import oracle as O
+            O.build(reference=True)
+            kind = "reference" if O.reference_available() else "port"
+            v, sample = time_cpu_instances(ws, args.cpu_seconds, kind)
+            result["cpu_baseline"] = {"value": v, "unit": "samples/s", "cores": os.cpu_count(), "kind": kind,
+                                      "sample": sample}
+        print(json.dumps(result))
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
 # ------------------------------------------------------------------ CPU (reference) arm
 def cpu_sample_scene(w, volume, n_rays: int, seed: int = 0):
     """A bounded sample of the workload: n_rays rays of its views, chosen
@@ -678,6 +928,13 @@ def cpu_baseline(w, args, volume, method: str = "adjoint"):
     return {"value": value, "unit": "samples/s", "cores": os.cpu_count(), "kind": kind, "sample": sample}
 
 
+def time_cpu_instances(ws, budget_s: float, kind: str):
+    """time_cpu over the instances of a batched workload, an equal share of
+    the budget each (at least 0.3 s); returns (mean samples/s, description)."""
+    rates = [time_cpu(w, w.volume, max(0.3, budget_s / len(ws)), kind)[0] for w in ws]
+    return float(np.mean(rates)), f"rays of each of the {len(ws)} instances (hitting the volume), fwd+adj passes"
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -686,14 +943,20 @@ def run_reference(args):
     O.build(reference=True)
     kind = "reference" if O.reference_available() and args.method == "adjoint" else "port"
     w = make_workload(args)
-    est = WORKLOADS[args.workload]["estimate"]
-    volume = np.full_like(w.volume, 0.1) if est == "const0.1" else (w.volume * 0.5 if est == "half" else w.volume)
+    if isinstance(w, list):  # batched instances
+        if args.method != "adjoint":
+            raise SystemExit("the batched entry points have no forward method")
+        timer = lambda budget: time_cpu_instances(w, budget, kind)
+    else:
+        est = WORKLOADS[args.workload]["estimate"]
+        volume = np.full_like(w.volume, 0.1) if est == "const0.1" else (w.volume * 0.5 if est == "half" else w.volume)
+        timer = lambda budget: time_cpu(w, volume, budget, kind, args.method)
     for _ in range(args.warmup):
-        time_cpu(w, volume, 1.0, kind, args.method)
+        timer(1.0)
     vals = []
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        v, sample = time_cpu(w, volume, max(1.0, args.cpu_seconds / max(args.steps, 1)), kind, args.method)
+        v, sample = timer(max(1.0, args.cpu_seconds / max(args.steps, 1)))
         vals.append(v)
     wall = time.perf_counter() - t0
     value = float(np.median(vals))
@@ -711,5 +974,7 @@ if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
         run_reference(a)
+    elif "instances" in WORKLOADS[a.workload]:
+        run_gpu_batched(a)
     else:
         run_gpu(a)

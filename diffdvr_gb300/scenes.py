@@ -199,6 +199,31 @@ def preshaded_256(seed: int = 1, res: int = 256, views: int = 8, image: int = 25
                     w.step_size, image, image, viewport=w.viewport, fov_y=w.fov_y, grads=("volume",))
 
 
+def batched_uneven(seed: int = 3, n: int = 32, n_blobs: int = 16) -> list:
+    """n independent instances for one batched call: volume edge drawn from
+    {32, 64, 96, 128, 192, 256}, image edge from {64, 128, 256, 512}, a
+    volume of n_blobs seeded blobs, a sum of 4 Gaussians TF (means U(0,1),
+    sigma U(0.02,0.2), RGBA U(0,1)), trilinear, Beer-Lambert, step 0.5 voxel,
+    one orbit view at radius 3 (FOV 45 degrees) as per-pixel rays, gradients
+    with respect to the TF and the volume."""
+    rng = np.random.default_rng(seed)
+    edges = rng.choice([32, 64, 96, 128, 192, 256], size=n)
+    images = rng.choice([64, 128, 256, 512], size=n)
+    fov = np.radians(45.0)
+    out = []
+    for i in range(n):
+        res, img = int(edges[i]), int(images[i])
+        vol = blob_volume(res, n_blobs, rng)
+        tf = tf_gaussian(4, rng, absorption_scale=1.0)
+        lat = rng.uniform(-np.pi / 2 * 0.9, np.pi / 2 * 0.9)
+        lon = rng.uniform(0, 2 * np.pi)
+        vp = viewport_from_sphere(lat, lon, 3.0)
+        rs, rd = generate_rays(vp, fov, img, img)
+        out.append(Workload(f"batched_uneven_{i}", vol, tf, 3, 0, 1, rs, rd, 0.5 / (res - 1), img, img,
+                            viewport=vp, fov_y=fov, grads=("tf", "volume")))
+    return out
+
+
 def plain_cpu_64(seed: int = 0) -> Workload:
     """64^3 volume of 8 blobs, trilinear, 8-point linear TF (absorption x10),
     Beer-Lambert, step 0.5 voxel, one 128^2 orbit view at radius 3."""

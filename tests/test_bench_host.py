@@ -1,9 +1,11 @@
-"""bench.py's host-side arithmetic on the CPU: the algorithmic bytes behind
-`roofline.achieved`, the clock record's parsing and the peak fallback."""
+"""bench.py's host-side logic on the CPU: the algorithmic bytes behind
+`roofline.achieved`, the clock record's parsing, the peak fallback, the
+batched workload's instances and its CPU arm, and the workload options."""
 import os
 import sys
 from types import SimpleNamespace
 
+import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -67,3 +69,45 @@ def test_peak_falls_back_without_measured_peaks(monkeypatch, tmp_path):
     assert bench.measured_peaks() == (6800.0, "fallback")
     (tmp_path / "MEASURED_PEAKS.json").write_text('{"hbm_gbs": 6786.2}')
     assert bench.measured_peaks() == (6786.2, "measured")
+
+
+def test_batched_uneven_instances():
+    """The batched workload's instances: volume edges and image sizes from
+    their sets, a 4-Gaussian TF with widths in [0.02, 0.2], step 0.5 voxel,
+    per-pixel rays of one view, TF and volume gradients."""
+    from diffdvr_gb300 import scenes
+    ws = scenes.batched_uneven(seed=3, n=6, n_blobs=2)
+    assert len(ws) == 6
+    for w in ws:
+        res = w.volume.shape[1]
+        assert w.volume.shape == (1, res, res, res) and res in (32, 64, 96, 128, 192, 256)
+        assert w.width == w.height and w.width in (64, 128, 256, 512)
+        assert w.ray_start.shape == w.ray_dir.shape == (1, w.height, w.width, 3)
+        assert w.tf.shape == (1, 4, 6) and np.all((w.tf[0, :, 5] >= 0.02) & (w.tf[0, :, 5] <= 0.2))
+        assert w.step_size == pytest.approx(0.5 / (res - 1))
+        assert (w.tf_mode, w.filter_mode, w.blend_mode) == (3, 1, 0) and set(w.grads) == {"tf", "volume"}
+
+
+def test_batched_reference_arm_times_every_instance(monkeypatch):
+    """The CPU arm of the batched workload times each instance with an equal
+    share of the budget and reports the mean rate."""
+    from diffdvr_gb300 import scenes
+    ws = scenes.batched_uneven(seed=3, n=2, n_blobs=2)
+    seen = []
+
+    def fake_time_cpu(w, volume, budget, kind):
+        seen.append((w, budget))
+        return 10.0 * len(seen), ""
+
+    monkeypatch.setattr(bench, "time_cpu", fake_time_cpu)
+    rate, desc = bench.time_cpu_instances(ws, 1.0, "port")
+    assert [w for w, _ in seen] == ws and all(b == pytest.approx(0.5) for _, b in seen)
+    assert rate == pytest.approx(15.0) and "2 instances" in desc
+
+
+def test_workload_options_parse(monkeypatch):
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--workload", "batched_uneven_32"])
+    a = bench.parse()
+    assert (a.res, a.views, a.image) == (256, 1, 512) and bench.WORKLOADS[a.workload]["instances"] == 32
+    monkeypatch.setattr(sys, "argv", ["bench.py"])
+    assert bench.parse().workload == "tf_reconstruction_256"
