@@ -285,6 +285,27 @@ def large_mixed_512(seed: int = 4, res: int = 512, views: int = 16, image: int =
                     viewport=vp, fov_y=fov, grads=("camera", "volume", "tf"))
 
 
+def crop(w: Workload, origin, size: int, views=None) -> Workload:
+    """The sub-volume of `size`^3 voxels starting at voxel `origin` of a
+    workload whose volume fills its box, with the box shrunk to that
+    sub-volume (same voxel size, same world positions, same step size) and
+    the rays of the chosen views (all by default), which keep their pixels;
+    rays that miss the sub-box take no samples."""
+    o = np.asarray(origin, dtype=np.int64)
+    X = np.array(w.volume.shape[1:], dtype=np.int64)
+    if np.any(o < 0) or np.any(o + size > X) or size < 2:
+        raise ValueError("the crop must lie inside the volume and hold at least 2 voxels per axis")
+    voxel = np.asarray(w.box_size, np.float64) / (X - 1)
+    bmin = np.asarray(w.box_min, np.float64) + o * voxel
+    vol = np.ascontiguousarray(w.volume[:, o[0]:o[0] + size, o[1]:o[1] + size, o[2]:o[2] + size])
+    sel = slice(None) if views is None else list(views)
+    return Workload(f"{w.name}_crop{size}", vol, w.tf, w.tf_mode, w.blend_mode, w.filter_mode,
+                    np.ascontiguousarray(w.ray_start[sel]), np.ascontiguousarray(w.ray_dir[sel]), w.step_size,
+                    w.width, w.height, viewport=None if w.viewport is None else w.viewport[sel], fov_y=w.fov_y,
+                    box_min=tuple(float(v) for v in bmin), box_size=tuple(float(v) for v in voxel * (size - 1)),
+                    grads=w.grads)
+
+
 def small_scene(seed: int, shape=(9, 10, 11), W: int = 12, H: int = 10, B: int = 2,
                 tf_mode: int = 1, R: Optional[int] = None, opacity: float = 1.0, pad_faces: bool = False,
                 dtype=np.float32) -> Workload:

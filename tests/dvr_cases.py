@@ -122,6 +122,29 @@ def make_case(seed: int, tf_mode: int = 1, filter_mode: int = 1, blend_mode: int
     return case
 
 
+def edge_cases():
+    """Degenerate inputs the marcher must handle: (name, case)."""
+    cases = []
+    c = make_case(61, shape=(1, 2, 3), W=1, H=1, B=1)
+    cases.append(("1x1 image, one-voxel x axis", c))
+    c = make_case(62, shape=(2, 1, 1), W=3, H=2, B=2)
+    cases.append(("one-voxel y and z axes", c))
+    c = make_case(63, W=5, H=4, B=2)
+    c.ray_dir = -c.ray_dir  # every ray points away from the box
+    cases.append(("all rays miss the box", c))
+    c = make_case(64, W=5, H=4, B=1)
+    c.step = 4.0  # longer than the box diagonal: at most one sample per ray
+    cases.append(("one sample per ray", c))
+    c = make_case(65, W=5, H=4, B=1)
+    c.early_out = 0.0  # stop after the first sample with any opacity
+    cases.append(("early out at zero opacity", c))
+    c = make_case(66, W=6, H=5, B=1)
+    c.width, c.height = 0, 0
+    c.ray_start, c.ray_dir = c.ray_start[:, :0, :0], c.ray_dir[:, :0, :0]
+    cases.append(("empty image", c))
+    return cases
+
+
 def all_mode_combos():
     return list(itertools.product(TF_MODES, FILTERS, BLENDS, CAMERAS))
 

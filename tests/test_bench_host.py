@@ -111,3 +111,27 @@ def test_workload_options_parse(monkeypatch):
     assert (a.res, a.views, a.image) == (256, 1, 512) and bench.WORKLOADS[a.workload]["instances"] == 32
     monkeypatch.setattr(sys, "argv", ["bench.py"])
     assert bench.parse().workload == "tf_reconstruction_256"
+
+
+def test_crop_keeps_the_sampling_grid(oracle_built):
+    """A crop's box is the sub-volume's extent on the same voxel grid: a
+    world point samples the same density in the crop as in the full volume
+    (the oracle's trilinear sample), and the chosen views' rays are kept."""
+    from diffdvr_gb300 import scenes
+    O = oracle_built
+    w = scenes.plain_cpu_64(seed=0)
+    w.ray_start = np.concatenate([w.ray_start, w.ray_start])  # a second view looking the other way
+    w.ray_dir = np.concatenate([w.ray_dir, -w.ray_dir])
+    w.viewport = np.concatenate([w.viewport, w.viewport])
+    c = scenes.crop(w, (10, 20, 30), 16, views=[1])
+    assert c.volume.shape == (1, 16, 16, 16) and c.ray_dir.shape == (1, 128, 128, 3)
+    assert np.array_equal(c.ray_dir[0], w.ray_dir[1])
+    voxel = np.asarray(w.box_size) / 63
+    assert np.allclose(np.asarray(c.box_size) / 15, voxel)
+    assert np.allclose(c.box_min, np.asarray(w.box_min) + np.array([10, 20, 30]) * voxel)
+    rng = np.random.default_rng(0)
+    for _ in range(20):
+        p = np.array([10, 20, 30]) + rng.uniform(0.0, 15.0, 3)  # voxel coordinates of the full volume
+        assert O.sample_step(c.volume, 1, p - [10, 20, 30]) == pytest.approx(O.sample_step(w.volume, 1, p), abs=1e-6)
+    with pytest.raises(ValueError):
+        scenes.crop(w, (60, 0, 0), 16)

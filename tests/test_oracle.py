@@ -4,7 +4,7 @@ the reference sources exist) a direct comparison over all mode combinations."""
 import numpy as np
 import pytest
 
-from dvr_cases import (all_mode_combos, golden, golden_case, golden_prefixes, make_case, rel_l2,
+from dvr_cases import (all_mode_combos, edge_cases, golden, golden_case, golden_prefixes, make_case, rel_l2,
                        symmetric_error)
 
 
@@ -218,29 +218,6 @@ def test_reference_cuda_kernel_names(oracle_built, tmp_path):
         assert m.group(1).endswith("_" + "".join(m.group(i) for i in range(2, 7))), m.group(1)
 
 
-def _edge_cases():
-    """Degenerate inputs the marcher must handle: (name, case)."""
-    cases = []
-    c = make_case(61, shape=(1, 2, 3), W=1, H=1, B=1)
-    cases.append(("1x1 image, one-voxel x axis", c))
-    c = make_case(62, shape=(2, 1, 1), W=3, H=2, B=2)
-    cases.append(("one-voxel y and z axes", c))
-    c = make_case(63, W=5, H=4, B=2)
-    c.ray_dir = -c.ray_dir  # every ray points away from the box
-    cases.append(("all rays miss the box", c))
-    c = make_case(64, W=5, H=4, B=1)
-    c.step = 4.0  # longer than the box diagonal: at most one sample per ray
-    cases.append(("one sample per ray", c))
-    c = make_case(65, W=5, H=4, B=1)
-    c.early_out = 0.0  # stop after the first sample with any opacity
-    cases.append(("early out at zero opacity", c))
-    c = make_case(66, W=6, H=5, B=1)
-    c.width, c.height = 0, 0
-    c.ray_start, c.ray_dir = c.ray_start[:, :0, :0], c.ray_dir[:, :0, :0]
-    cases.append(("empty image", c))
-    return cases
-
-
 @pytest.mark.parametrize("filter_mode", [0, 1])
 def test_port_matches_reference_edge_cases(oracle_built, filter_mode):
     """Degenerate inputs: the restatement against the reference's own CPU
@@ -248,7 +225,7 @@ def test_port_matches_reference_edge_cases(oracle_built, filter_mode):
     O = oracle_built
     if not O.reference_available():
         pytest.skip("reference sources not present")
-    for name, case in _edge_cases():
+    for name, case in edge_cases():
         case.filter_mode = filter_mode
         sc = case.oracle_scene()
         c1, t1 = O.forward(sc, "port", "f64")
