@@ -423,3 +423,17 @@ int main(void) {
     assert r.returncode == 0, r.stderr
     r = subprocess.run([str(exe)], capture_output=True, text=True)
     assert r.returncode == 0 and r.stdout.strip() == "ok 4", (r.returncode, r.stdout, r.stderr)
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    """Without libdvr_gb300.so every entry point raises: there is no CPU
+    fallback, in the direct binding or the autograd module."""
+    from diffdvr_gb300 import _abi as abi, pyrenderer as pr
+    monkeypatch.setattr(abi, "_LIB", None)
+    monkeypatch.setattr(abi, "library_path", lambda: str(tmp_path / "libdvr_gb300.so"))
+    with pytest.raises(RuntimeError, match="CUDA library not found"):
+        pr.Renderer.render_forward(pr.RendererInputs(), pr.RendererOutputs(None, None))
+    with pytest.raises(RuntimeError, match="CUDA library not found"):
+        pr.set_kernel_family("plain")
+    with pytest.raises(RuntimeError, match="CUDA library not found"):
+        abi.load()
