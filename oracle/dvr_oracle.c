@@ -1120,6 +1120,20 @@ int oracle_sample_step_adjoint(const OracleTensor* volume, int filter, const rea
   return 0;
 }
 
+/* the ray (start, direction) of every pixel as the march computes it, B H W 3 each */
+int oracle_camera_rays(const OracleInputs* in, OracleTensor* start, OracleTensor* dir) {
+  if (in->camera_mode < 0 || in->camera_mode > 2) return 2;
+  for (int b = 0; b < in->batch; ++b)
+    for (int y = 0; y < in->height; ++y)
+      for (int x = 0; x < in->width; ++x) {
+        v3 s, d;
+        compute_ray(in, x, y, b, &s, &d);
+        *at4(start, b, y, x, 0) = s.x; *at4(start, b, y, x, 1) = s.y; *at4(start, b, y, x, 2) = s.z;
+        *at4(dir, b, y, x, 0) = d.x; *at4(dir, b, y, x, 1) = d.y; *at4(dir, b, y, x, 2) = d.z;
+      }
+  return 0;
+}
+
 /* n positions volumePos(t_k), t_k = tmin + k*step, of one ray, and their adjoint */
 int oracle_ray_steps(const real_t* start, const real_t* dir, const real_t* box_min, const real_t* voxel, real_t tmin,
                      real_t step, int n, real_t* pos) {

@@ -132,6 +132,9 @@ int oracle_tf_step_adjoint(const OracleTensor* tf, int tf_mode, real_t density, 
 int oracle_sample_step(const OracleTensor* volume, int filter, const real_t* pos, real_t* density);
 int oracle_sample_step_adjoint(const OracleTensor* volume, int filter, const real_t* pos, real_t adj_density,
                                real_t* adj_pos, OracleTensor* adj_volume);
+/* The ray (start, direction; B H W 3 each) of every pixel, as the march
+ * computes it for the inputs' camera mode. */
+int oracle_camera_rays(const OracleInputs* in, OracleTensor* start, OracleTensor* dir);
 /* The n sample positions (start + t*dir - box_min) / voxel, t = tmin + k*step,
  * of one ray (pos: n x 3), and their adjoint for the ray start, direction and
  * step size (tmin held fixed, as in the march). */

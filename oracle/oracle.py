@@ -441,6 +441,7 @@ def _component_lib(precision: str):
         lib.oracle_sample_step_adjoint.argtypes = [T, i, P, R, P, T]
         lib.oracle_ray_steps.argtypes = [P, P, P, P, R, R, i, P]
         lib.oracle_ray_steps_adjoint.argtypes = [P, P, P, P, R, R, i, P, P, P, P]
+        lib.oracle_camera_rays.argtypes = [ctypes.POINTER(OracleInputs), T, T]
         lib._components_typed = True
         lib._real = R
     return lib
@@ -541,3 +542,17 @@ def ray_steps_adjoint(start, direction, box_min, voxel, tmin: float, step: float
                                      _vec(np.asarray(adj_pos).reshape(-1), lib, keep)[1], p1, p2, p3),
         "ray_steps_adjoint")
     return a1, a2, float(a3[0])
+
+
+def camera_rays(scene: Scene, precision: str = "f64"):
+    """(ray start, ray direction), each B*H*W*3, as the march computes them
+    for the scene's camera mode."""
+    lib, keep = _component_lib(precision), []
+    dt = np.float64 if lib._real is ctypes.c_double else np.float32
+    inp = _inputs(scene, dt, keep)
+    B = inp.batch
+    start = np.zeros((B, scene.height, scene.width, 3), dtype=dt)
+    direction = np.zeros_like(start)
+    ts, td = _tensor(start, keep), _tensor(direction, keep)
+    _ok(lib.oracle_camera_rays(ctypes.byref(inp), ctypes.byref(ts), ctypes.byref(td)), "camera_rays")
+    return start, direction
