@@ -437,3 +437,84 @@ def test_missing_library_fails_loudly(monkeypatch, tmp_path):
         pr.set_kernel_family("plain")
     with pytest.raises(RuntimeError, match="CUDA library not found"):
         abi.load()
+
+
+def _batched_forward(lib, ins, outs, n=None):
+    ci = (_abi.DvrRendererInputs * max(len(ins), 1))(*ins)
+    co = (_abi.DvrRendererOutputs * max(len(outs), 1))(*outs)
+    code = lib.dvr_render_forward_batched(ci, co, len(ins) if n is None else n, None)
+    return code, lib.dvr_last_error().decode()
+
+
+def _with(obj, **kw):
+    for k, v in kw.items():
+        setattr(obj, k, v)
+    return obj
+
+
+# batched calls: each instance is checked as a single call, and all must share
+# their modes, storage types and device (diffdvr_gb300/csrc/dvr_host.cpp)
+@pytest.mark.parametrize("make,expect", [
+    (lambda: ([_inputs()], [_outputs()], -1), "invalid instance list"),
+    (lambda: ([_inputs(), _inputs(tf_mode=3)], [_outputs(), _outputs()], None),
+     "must share filter, TF and blend modes, storage types and device"),
+    (lambda: ([_inputs(), _with(_inputs(), blend_mode=1)], [_outputs(), _outputs()], None),
+     "must share filter, TF and blend modes"),
+    (lambda: ([_inputs(), _with(_inputs(), volume=_fake((1, 4, 5, 6), _abi.DVR_BFLOAT16))],
+              [_outputs(), _outputs()], None), "storage types"),
+    (lambda: ([_preshaded_inputs()], [_outputs()], None), "pre-shaded volumes are rendered by the single-instance"),
+    (lambda: ([_inputs(), _inputs(W=9)], [_outputs(), _outputs()], None), "must have 9 entries at dimension 2"),
+    (lambda: ([_inputs(X=9, Y=3, Z=17), _inputs(W=16, H=4)], [_outputs(), _outputs(W=16, H=4)], None), None),
+])
+def test_batched_forward_validation(dvr_lib, make, expect):
+    if expect is None:
+        _no_gpu()
+    ins, outs, n = make()
+    code, msg = _batched_forward(dvr_lib, ins, outs, n)
+    if expect is None:
+        assert code == _abi.DVR_E_CUDA, msg  # instances of different sizes pass every check; no GPU here
+    else:
+        assert code in (_abi.DVR_E_INVALID_ARGUMENT, _abi.DVR_E_UNSUPPORTED)
+        assert expect in msg, msg
+
+
+def test_batched_calls_without_instances_do_nothing(dvr_lib):
+    assert dvr_lib.dvr_render_forward_batched(None, None, 0, None) == _abi.DVR_OK
+    assert dvr_lib.dvr_render_adjoint_batched(None, None, None, None, 0, None) == _abi.DVR_OK
+
+
+def _batched_adjoint(lib, ins, outs, adjs, grads):
+    n = len(ins)
+    code = lib.dvr_render_adjoint_batched((_abi.DvrRendererInputs * n)(*ins), (_abi.DvrRendererOutputs * n)(*outs),
+                                          (_abi.DvrTensor * n)(*adjs), (_abi.DvrAdjointOutputs * n)(*grads), n, None)
+    return code, lib.dvr_last_error().decode()
+
+
+def _tf_grad(B=1, R=8):
+    return _adj_outputs(has_tf_derivatives=1, adj_tf=_fake((B, R, 4)))
+
+
+@pytest.mark.parametrize("make,expect", [
+    (lambda: ([_inputs(), _inputs()], [_outputs(), _outputs()],
+              [_tf_grad(), _adj_outputs(has_volume_derivatives=1, adj_volume=_fake((1, 4, 5, 6)))]),
+     "must share modes, storage types, device and gradient selection"),
+    (lambda: ([_inputs(), _inputs()], [_outputs(), _outputs()],
+              [_tf_grad(), _with(_tf_grad(), has_volume_derivatives=1, adj_volume=_fake((1, 4, 5, 6)))]),
+     "gradient selection"),
+    (lambda: ([_with(_inputs(), camera_mode=2, camera_kind=_abi.DVR_CAMERA_REFERENCE_FRAME_KIND,
+                     camera_matrix=_fake((1, 3, 3)), camera_fov_y_radians=0.7)], [_outputs()],
+              [_adj_outputs(has_viewport_derivatives=1, adj_viewport=_fake((1, 3, 3)))]),
+     "do not compute viewport derivatives"),
+    (lambda: ([_inputs(), _inputs(W=16, H=4)], [_outputs(), _outputs(W=16, H=4)], [_tf_grad(), _tf_grad()]), None),
+])
+def test_batched_adjoint_validation(dvr_lib, make, expect):
+    if expect is None:
+        _no_gpu()
+    ins, outs, grads = make()
+    adjs = [_fake((1, o.color.sizes[1], o.color.sizes[2], 4)) for o in outs]
+    code, msg = _batched_adjoint(dvr_lib, ins, outs, adjs, grads)
+    if expect is None:
+        assert code == _abi.DVR_E_CUDA, msg
+    else:
+        assert code in (_abi.DVR_E_INVALID_ARGUMENT, _abi.DVR_E_UNSUPPORTED)
+        assert expect in msg, msg
