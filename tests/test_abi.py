@@ -518,3 +518,26 @@ def test_batched_adjoint_validation(dvr_lib, make, expect):
     else:
         assert code in (_abi.DVR_E_INVALID_ARGUMENT, _abi.DVR_E_UNSUPPORTED)
         assert expect in msg, msg
+
+
+@pytest.mark.parametrize("make,expect", [
+    (lambda: (_preshaded_inputs(), _tf_grad(1, 1)), "pre-shaded volumes take dvr_render_adjoint"),
+    (lambda: (_inputs(), _adj_outputs()), None),  # no gradient requested
+    (lambda: (_inputs(), _tf_grad()), "pass"),
+])
+def test_noalloc_adjoint_validation(dvr_lib, make, expect):
+    """dvr_render_adjoint_noalloc checks its arguments as dvr_render_adjoint
+    does, and rejects pre-shaded volumes, before any CUDA call."""
+    if expect == "pass":
+        _no_gpu()
+    i, g = make()
+    o = _outputs()
+    code = dvr_lib.dvr_render_adjoint_noalloc(ctypes.byref(i), ctypes.byref(o), ctypes.byref(_fake((1, 7, 8, 4))),
+                                              ctypes.byref(g), None)
+    msg = dvr_lib.dvr_last_error().decode()
+    if expect == "pass":
+        assert code == _abi.DVR_E_CUDA, msg  # every check passed; no GPU here
+    elif expect is None:
+        assert code == _abi.DVR_E_NO_GRADIENT, msg
+    else:
+        assert code == _abi.DVR_E_UNSUPPORTED and expect in msg, msg
