@@ -541,3 +541,57 @@ def test_noalloc_adjoint_validation(dvr_lib, make, expect):
         assert code == _abi.DVR_E_NO_GRADIENT, msg
     else:
         assert code == _abi.DVR_E_UNSUPPORTED and expect in msg, msg
+
+
+def test_python_mirror_descriptors():
+    """pyrenderer turns the reference's settings variants into the C ABI's
+    tagged descriptors (renderer/renderer.h:20-71): value or tensor boxes and
+    step sizes, the four camera types, element strides as the tensors have
+    them (non-contiguous views included), dtype codes, no pointer for an
+    empty tensor."""
+    import torch
+    inp = pr.RendererInputs()
+    inp.screen_size = pr.int2(6, 5)
+    inp.volume = torch.zeros(1, 4, 5, 6, dtype=torch.bfloat16)
+    inp.box_min = pr.real3(-0.5, -0.25, -0.125)
+    rays = torch.zeros(2, 6, 5, 3).transpose(1, 2)  # B H W 3 with non-contiguous strides
+    inp.camera = pr.CameraPerPixelRays(rays, rays)
+    inp.step_size = 0.01
+    inp.tf = torch.zeros(1, 8, 4)
+    c = pr._inputs(inp)
+    assert (c.screen_width, c.screen_height) == (6, 5)
+    assert c.volume.dtype == _abi.DVR_BFLOAT16 and tuple(c.volume.sizes[:4]) == (1, 4, 5, 6)
+    assert c.box_min_kind == _abi.DVR_KIND_VALUE and tuple(c.box_min_value) == (-0.5, -0.25, -0.125)
+    assert c.box_min.ndim == -1 and c.box_size_kind == _abi.DVR_KIND_VALUE
+    assert c.camera_kind == _abi.DVR_CAMERA_PER_PIXEL_RAYS and c.camera_matrix.ndim == -1
+    assert tuple(c.camera_ray_start.sizes[:4]) == (2, 5, 6, 3)
+    assert tuple(c.camera_ray_start.strides[:4]) == tuple(rays.stride())
+    assert c.camera_ray_start.device_type == _abi.DVR_DEVICE_CPU and c.camera_ray_start.device_index == -1
+    assert c.step_size_kind == _abi.DVR_KIND_VALUE and c.step_size_value == pytest.approx(0.01)
+
+    inp.box_min = torch.zeros(1, 3)
+    inp.box_size = torch.ones(2, 3)
+    inp.step_size = torch.full((1, 5, 6), 0.02)
+    inp.camera = pr.CameraReferenceFrame(torch.zeros(2, 3, 3), 0.7)
+    c = pr._inputs(inp)
+    assert c.box_min_kind == c.box_size_kind == c.step_size_kind == _abi.DVR_KIND_TENSOR
+    assert tuple(c.box_size.sizes[:2]) == (2, 3) and tuple(c.step_size.sizes[:3]) == (1, 5, 6)
+    assert c.camera_kind == _abi.DVR_CAMERA_REFERENCE_FRAME_KIND and c.camera_fov_y_radians == pytest.approx(0.7)
+    assert tuple(c.camera_matrix.sizes[:3]) == (2, 3, 3) and c.camera_ray_start.ndim == -1
+
+    m = np.arange(16, dtype=np.float32).reshape(4, 4)
+    inp.camera = pr.mat4(m)
+    c = pr._inputs(inp)
+    assert c.camera_kind == _abi.DVR_CAMERA_INVERSE_VIEW_VALUE and list(c.camera_matrix_value) == list(range(16))
+    inp.camera = torch.zeros(1, 4, 4)
+    c = pr._inputs(inp)
+    assert c.camera_kind == _abi.DVR_CAMERA_INVERSE_VIEW_TENSOR and tuple(c.camera_matrix.sizes[:3]) == (1, 4, 4)
+    inp.camera = "eye"
+    with pytest.raises(RuntimeError, match="unknown camera type"):
+        pr._inputs(inp)
+
+    out = pr.RendererOutputs(torch.zeros(2, 0, 6, 4), torch.zeros(2, 0, 6, dtype=torch.int32))
+    o = pr._outputs(out)
+    assert o.color.data is None and o.color.ndim == 4  # an empty tensor passes no pointer
+    assert o.termination_index.dtype == _abi.DVR_INT32 and o.checkpoints.ndim == -1 and o.sample_density.ndim == -1
+    assert pr._tensor(torch.zeros(3, dtype=torch.int64)).dtype not in (_abi.DVR_FLOAT32, _abi.DVR_INT32)
