@@ -595,3 +595,25 @@ def test_python_mirror_descriptors():
     assert o.color.data is None and o.color.ndim == 4  # an empty tensor passes no pointer
     assert o.termination_index.dtype == _abi.DVR_INT32 and o.checkpoints.ndim == -1 and o.sample_density.ndim == -1
     assert pr._tensor(torch.zeros(3, dtype=torch.int64)).dtype not in (_abi.DVR_FLOAT32, _abi.DVR_INT32)
+
+
+def test_autograd_module_argument_checks():
+    """diffdvr_gb300.Renderer checks its arguments as the reference's module
+    does (pytests/diffdvr/renderer.py:264-335): assertion errors for an
+    unknown gradient method, a volume optimised by the forward method, or a
+    missing input of an optimised quantity; a ValueError for training
+    without parameters."""
+    import torch
+    from diffdvr_gb300 import Renderer
+    with pytest.raises(AssertionError):
+        Renderer(gradient_method="backward")
+    with pytest.raises(AssertionError, match="gradient method must be 'adjoint'"):
+        Renderer(optimize_volume=True, gradient_method="forward")
+    r = Renderer(optimize_tf=True)
+    with pytest.raises(AssertionError):
+        r(tf=None, volume=torch.zeros(1, 2, 2, 2))
+    with pytest.raises(ValueError, match="no parameters were specified"):
+        Renderer().train()
+    with pytest.raises(AssertionError):
+        r.settings = None
+    assert Renderer(optimize_camera=True).train() is not None
