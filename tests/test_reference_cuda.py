@@ -69,6 +69,7 @@ def test_reference_cuda_forward_all_modes(ref_cuda, oracle_built):
         if e_ref.size and e_ref.max() > 1e-3:
             bad.append(f"reference CUDA: colour error {e_ref.max():.2e} against FP64")
         share = 0.97 if filt == 0 else 0.99
+        stats = [f"mode {(tfm, filt, blend, cam)}: reference CUDA vs FP64 max {e_ref.max() if e_ref.size else 0:.2e}"]
         for family in ("plain", "optimized"):
             _, out = gpu_forward(case, family)
             color, term = out.color.cpu().numpy(), out.terminationIndex.cpu().numpy()
@@ -76,8 +77,11 @@ def test_reference_cuda_forward_all_modes(ref_cuda, oracle_built):
             if np.mean(term != rt) > 0.05:
                 bad.append(f"{family}: sample counts differ on {np.mean(term != rt):.3f}")
             pe = _pixel_errors(color[same], rc[same])
+            if pe.size:
+                stats.append(f"{family} vs reference CUDA max {pe.max():.2e}, within 1e-5 {np.mean(pe <= 1e-5):.3f}")
             if pe.size and (np.mean(pe <= 1e-5) < share or pe.max() > 1e-4):
                 bad.append(f"{family}: {np.mean(pe <= 1e-5):.3f} of pixels within 1e-5, max {pe.max():.2e}")
+        print("; ".join(stats))  # shown in full with the failure report
         if bad:
             failures[(tfm, filt, blend, cam)] = bad
     assert not failures, failures
@@ -114,13 +118,16 @@ def test_reference_cuda_adjoint_all_modes(family, ref_cuda, oracle_built):
         got, ref, ref64 = _three_adjoints(ref_cuda, O, case, inp, out, family, req, adj,
                                           dict(volume=True, tf=True, camera=cam == 0, stepsize=True))
         bad = {}
+        stats = []
         for k in got:
             if k == "adj_stepsize" and family == "optimized":
                 continue
             r = rel_l2(got[k], ref[k])
             tol = max(1e-3, 3 * rel_l2(ref[k], ref64[k]), 3 * rel_l2(got[k], ref64[k]))
+            stats.append(f"{k} {r:.2e} (reference CUDA vs FP64 {rel_l2(ref[k], ref64[k]):.2e})")
             if r > tol:
                 bad[k] = (r, tol)
+        print(f"mode {(tfm, filt, blend, cam)} {family}: " + ", ".join(stats))
         if bad:
             failures[(tfm, filt, blend, cam)] = bad
     assert not failures, failures
