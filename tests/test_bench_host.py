@@ -135,3 +135,49 @@ def test_crop_keeps_the_sampling_grid(oracle_built):
         assert O.sample_step(c.volume, 1, p - [10, 20, 30]) == pytest.approx(O.sample_step(w.volume, 1, p), abs=1e-6)
     with pytest.raises(ValueError):
         scenes.crop(w, (60, 0, 0), 16)
+
+
+def _orbit_checks(w, views, image, fov_deg=45.0, radius=3.0):
+    assert w.ray_start.shape == w.ray_dir.shape == (views, image, image, 3)
+    eyes = w.ray_start[:, 0, 0]
+    assert np.allclose(np.linalg.norm(eyes, axis=1), radius, rtol=1e-5)  # orbit camera around the origin
+    assert np.allclose(np.linalg.norm(w.ray_dir, axis=-1), 1.0, atol=1e-5)
+    assert w.fov_y == pytest.approx(np.radians(fov_deg))
+    assert tuple(w.box_min) == (-0.5, -0.5, -0.5) and tuple(w.box_size) == (1.0, 1.0, 1.0)
+
+
+def test_workloads_follow_their_configurations():
+    """The seeded synthetic workloads have the shapes and distributions of
+    the configurations they stand for (at reduced sizes where the generator
+    takes them): blob or ellipsoid volumes in [0, 1], the TF type and size,
+    orbit views at radius 3 and 45 degrees, the step in voxels, the
+    gradients."""
+    from diffdvr_gb300 import scenes
+    w = scenes.tf_reconstruction_256(seed=1, res=32, views=8, image=16)
+    _orbit_checks(w, 8, 16)
+    assert w.volume.shape == (1, 32, 32, 32) and 0 <= w.volume.min() and w.volume.max() <= 1
+    assert w.tf.shape == (1, 64, 4) and (w.tf_mode, w.filter_mode, w.blend_mode) == (1, 1, 0)
+    assert w.step_size == pytest.approx(0.25 / 31) and w.grads == ("tf",)
+    lat, _ = scenes.fibonacci_sphere(8)
+    assert len(np.unique(np.round(lat, 6))) == 8  # distinct Fibonacci views
+
+    w = scenes.absorption_recon_128(seed=2, views=4, image=8)
+    _orbit_checks(w, 4, 8)
+    assert w.volume.shape == (1, 128, 128, 128) and w.volume.min() == 0.0
+    inside = w.volume[w.volume > 0]
+    assert inside.min() >= 0.2 and inside.max() <= 1.0  # ellipsoid densities U(0.2, 1) on a zero background
+    assert np.array_equal(w.tf, [[[20.0, 1.0]]]) and w.tf_mode == 0 and w.grads == ("volume",)
+    assert w.step_size == pytest.approx(0.5 / 127)
+
+    w = scenes.large_mixed_512(seed=4, res=32, views=2, image=8)
+    _orbit_checks(w, 2, 8)
+    assert w.tf.shape == (1, 16, 5) and w.tf_mode == 2 and w.tf[0, 0, 4] == 0 and w.tf[0, -1, 4] == 1
+    assert np.all(np.diff(w.tf[0, :, 4]) >= 0) and w.tf[0, :, 3].max() > 1  # sorted positions, absorption x10
+    assert set(w.grads) == {"camera", "volume", "tf"} and w.step_size == pytest.approx(0.5 / 31)
+
+    w = scenes.plain_cpu_64(seed=0)
+    _orbit_checks(w, 1, 128)
+    assert w.volume.shape == (1, 64, 64, 64) and w.tf.shape == (1, 8, 5) and set(w.grads) == {"tf", "volume"}
+
+    p = scenes.preshaded_256(seed=1, res=16, views=2, image=8)
+    assert p.volume.shape == (4, 16, 16, 16) and (p.tf_mode, p.filter_mode) == (5, 3)
