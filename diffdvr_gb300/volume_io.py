@@ -14,8 +14,9 @@ followed by the X*Y*Z values with x fastest (slice by slice in z).  Integer
 data are scaled to [0, 1] (value / 255 or / 65535).  The renderer's volume
 layout is [b][x][y][z]; ``load_cvol`` returns a view with exactly the file's
 memory order (strides 1, X, X*Y in elements along x, y, z), which the
-renderer accepts as it is.  LZ4-compressed files need the LZ4 library, which
-this package does not bundle; loading one raises NotImplementedError.
+renderer accepts as it is.  LZ4-compressed files are written in chunks
+whose framing the reference's LZ4 wrapper defines (renderer/volume.cpp:127-137);
+loading one raises NotImplementedError.
 
 Marschner-Lobb (renderer/volume_implicit.cpp:28-42, sampled as
 renderer/volume.cpp:369-387): on [-1, 1]^3 sampled at ``resolution`` points
@@ -64,7 +65,8 @@ def load_cvol(path: str) -> Tuple[np.ndarray, Tuple[float, float, float]]:
     array of shape 1*X*Y*Z in the file's x-fastest memory order."""
     hdr = read_cvol_header(path)
     if hdr["compressed"]:
-        raise NotImplementedError(f"{path}: LZ4-compressed .cvol files are not supported (no LZ4 library)")
+        raise NotImplementedError(f"{path}: LZ4-compressed .cvol files are not supported "
+                                  "(their chunk framing is that of the reference's LZ4 wrapper)")
     X, Y, Z = hdr["size"]
     n = X * Y * Z
     if n > np.iinfo(np.int32).max:
