@@ -17,6 +17,11 @@
 // Because every call on a device shares this one array, calls that may
 // overlap on the same device (other streams, other host threads) race; the
 // caller serialises them.
+//
+// The array's device address is resolved once per device, on the first call
+// there, and kept for the life of the process.  cudaDeviceReset destroys the
+// context that address belongs to: a process that resets a device must not
+// call this entry point on that device afterwards.
 #include <cuda_runtime.h>
 
 #include <mutex>

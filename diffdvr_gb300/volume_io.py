@@ -40,7 +40,9 @@ import numpy as np
 MAGIC = b"cvol"
 HEADER_BYTES = 64
 _TYPES = {0: np.uint8, 1: np.uint16, 2: np.float32}
-_SCALE = {0: 1.0 / 255.0, 1: 1.0 / 65535.0, 2: None}
+# integer data are divided by the type's maximum in float32, as the
+# reference's loader does (renderer/volume.cpp:244, :251)
+_DIVISOR = {0: np.float32(255.0), 1: np.float32(65535.0), 2: None}
 
 
 def read_cvol_header(path: str) -> dict:
@@ -75,8 +77,8 @@ def load_cvol(path: str) -> Tuple[np.ndarray, Tuple[float, float, float]]:
     raw = np.fromfile(path, dtype=np.dtype(t).newbyteorder("<"), count=n, offset=HEADER_BYTES)
     if raw.size != n:
         raise ValueError(f"{path}: truncated data ({raw.size} of {n} values)")
-    scale = _SCALE[hdr["dtype"]]
-    data = raw.astype(np.float32) * np.float32(scale) if scale is not None else raw.astype(np.float32)
+    div = _DIVISOR[hdr["dtype"]]
+    data = raw.astype(np.float32) / div if div is not None else raw.astype(np.float32)
     # file order: x fastest -> [z][y][x] in C order -> view as [x][y][z]
     vol = data.reshape(Z, Y, X).transpose(2, 1, 0)[None]
     return vol, hdr["world_size"]

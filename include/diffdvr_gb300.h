@@ -178,7 +178,15 @@ typedef struct DvrAdjointOutputs {
 
 /* Forward rendering without gradients.
  * Replaces renderer::Renderer::renderForward (renderer/renderer.h:159-161,
- * renderer/renderer.cpp:393-417). */
+ * renderer/renderer.cpp:393-417).
+ * Library scratch: the optimized family takes work counters and, per
+ * stream, a ray-order buffer (and the cell-corner volume for trilinear
+ * filtering) from pools that it grows with cudaMalloc when a call needs more
+ * than they hold; dvr_render_adjoint does the same for its ray order and
+ * TF-gradient slices.  cudaMalloc is not allowed while a stream is being
+ * captured into a CUDA graph, so make one call of the same sizes on the same
+ * stream before capturing it; later calls reuse the pools and allocate
+ * nothing. */
 int dvr_render_forward(const DvrRendererInputs* inputs, const DvrRendererOutputs* outputs, void* cuda_stream);
 
 /* Adjoint (backward) rendering: traces adj_color (B*H*W*4) back through the
@@ -201,10 +209,12 @@ int dvr_render_adjoint(const DvrRendererInputs* inputs, const DvrRendererOutputs
  * 4 MiB - 256 bytes (R = TF control points, C = channels), i.e. R x C <= 6898
  * on a 152-SM GPU; larger TFs are rejected with DVR_E_INVALID_ARGUMENT.
  * Volume and image sizes are not limited.  The kernel-family switch does not
- * apply.  The first call on a device resolves the array's address; make it
- * before capturing the stream into a CUDA graph.  All calls on one device
- * share the array: calls that may overlap (other streams or host threads)
- * race, so the caller serialises them.
+ * apply.  The first call on a device resolves the array's address and keeps
+ * it for the life of the process; make it before capturing the stream into a
+ * CUDA graph, and do not call this entry point on a device after
+ * cudaDeviceReset there (the reset destroys the context the address belongs
+ * to).  All calls on one device share the array: calls that may overlap
+ * (other streams or host threads) race, so the caller serialises them.
  * No counterpart in the reference. */
 int dvr_render_adjoint_noalloc(const DvrRendererInputs* inputs, const DvrRendererOutputs* outputs_from_forward,
                                const DvrTensor* adj_color, const DvrAdjointOutputs* adj_outputs,

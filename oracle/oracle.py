@@ -30,7 +30,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 REF_DIR = os.path.join(HERE, "_ref")
-REFERENCE_SOURCES = "/root/reference/renderer"
+# the reference checkout: DIFFDVR_REFERENCE, else its path in the build container
+REFERENCE_ROOT = os.environ.get("DIFFDVR_REFERENCE", "/root/reference")
+REFERENCE_SOURCES = os.path.join(REFERENCE_ROOT, "renderer")
 
 
 class OracleTensor(ctypes.Structure):

@@ -115,4 +115,5 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    from oracle.oracle import REFERENCE_ROOT
+    main(sys.argv[1] if len(sys.argv) > 1 else REFERENCE_ROOT)

@@ -8,8 +8,9 @@ import numpy as np
 import pytest
 
 from diffdvr_gb300 import volume_io as vio
+from oracle.oracle import REFERENCE_ROOT
 
-REF_CVOL = "/root/reference/pytests/volumes/C60Large.cvol"
+REF_CVOL = os.path.join(REFERENCE_ROOT, "pytests", "volumes", "C60Large.cvol")
 
 
 @pytest.mark.parametrize("dtype,tol", [("float32", 0.0), ("uint8", 0.5 / 255), ("uint16", 0.5 / 65535)])
@@ -60,7 +61,21 @@ def test_reference_c60_volume():
     with open(REF_CVOL, "rb") as f:
         f.seek(64 + 128 * 128 * 64)  # slice z = 64
         raw = np.frombuffer(f.read(128 * 128), np.uint8).reshape(128, 128)  # [y][x]
-    np.testing.assert_allclose(vol[0, :, :, 64], raw.T.astype(np.float32) / 255.0, rtol=0, atol=1e-7)
+    # bit-identical to the reference loader's src[i] / 255.0f (renderer/volume.cpp:244)
+    assert np.array_equal(vol[0, :, :, 64], raw.T.astype(np.float32) / np.float32(255.0))
+
+
+@pytest.mark.parametrize("dtype,mx", [("uint8", 255), ("uint16", 65535)])
+def test_cvol_integer_values_divide_like_the_reference(tmp_path, dtype, mx):
+    """Every integer value v loads as float32(v) / float32(max), bit for bit,
+    as the reference's loader computes it (renderer/volume.cpp:244, :251);
+    multiplying by the reciprocal differs in the last bit for some values."""
+    n = mx + 1
+    path = str(tmp_path / "all.cvol")
+    vio.save_cvol(path, (np.arange(n, dtype=np.float64) / mx).reshape(n, 1, 1), dtype=dtype)
+    got, _ = vio.load_cvol(path)
+    want = np.arange(n, dtype=np.float32) / np.float32(mx)
+    assert np.array_equal(got[0, :, 0, 0], want)
 
 
 def test_marschner_lobb_values():
