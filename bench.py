@@ -94,7 +94,8 @@ def parse():
     ap.add_argument("--storage", choices=["bf16", "f16", "f32"], default="bf16", help="volume storage type")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP32 comparison arm")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline budget")
-    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
+    ap.add_argument("--no-cpu", action="store_true",
+                    help="skip the CPU baseline, the reference CUDA timing and the accuracy check (profiling runs)")
     ap.add_argument("--interval", type=int, default=0, help="transmittance checkpoint interval (workload default)")
     ap.add_argument("--method", choices=["adjoint", "forward"], default="adjoint",
                     help="gradient method: adjoint (the headline) or forward-mode derivatives")
@@ -246,6 +247,149 @@ def algorithmic_bytes(w, s_v, V, P, S, ck_written, recorded, record_kernel, tf_n
         if "camera" in grads:
             adj += P * 24 * 2
     return fwd, adj
+
+
+def compulsory_bytes(w, s_v, V, P, ck_written, tf_numel, D=0):
+    """Compulsory HBM bytes per forward and adjoint launch of the measurement
+    plan: the volume read once per launch, colour (16 B) and termination index
+    (4 B) written by the forward and read again by the adjoint with the output
+    adjoint (16 B), gradients read-modify-written once (volume 4 B per voxel,
+    rays 24 B per ray), the TF gradient, and the checkpoints (4 B each here)
+    written by the forward and read by the adjoint.  The forward method adds
+    its forward variables (16 B per derivative and ray), written once and read
+    once."""
+    grads = set(w.grads)
+    fwd = V * s_v + P * (16 + 4) + ck_written * 4 + P * D * 16
+    if D:  # the contraction: forward variables and the output adjoint in, gradients out
+        adj = P * D * 16 + P * 16
+    else:
+        adj = V * s_v + P * (16 + 4 + 16) + ck_written * 4
+    if "tf" in grads:
+        adj += tf_numel * 4 * 2
+    if "volume" in grads:
+        adj += V * 4 * 2
+    if "camera" in grads:
+        adj += P * 24 * 2
+    return fwd, adj
+
+
+# warp-instruction issue rate of the GPU: 4 schedulers per SM, one warp
+# instruction each per cycle
+ISSUE_PER_SM_CLOCK = 4
+
+
+def issue_bound(workload: str, kernel: str, samples: int, ms: float):
+    """The issue-slot ceiling of the dominant kernel: warp instructions per
+    sample from the committed ncu summary of the same workload
+    (profiles/issue_rate.txt), the rate they were issued at in this run, and
+    the GPU's peak issue rate at its maximum clock."""
+    p = os.path.join(ROOT, "profiles", "issue_rate.txt")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    per = d.get("warp_instructions_per_sample", {}).get(workload, {}).get(kernel)
+    if per is None:
+        return None
+    peak = d["sms"] * ISSUE_PER_SM_CLOCK * d["sm_max_mhz"] * 1e6 / 1e12
+    achieved = per * samples / (ms / 1e3) / 1e12
+    return {"warp_instructions_per_sample": per, "achieved": achieved, "peak": peak, "unit": "T warp-instr/s",
+            "frac": achieved / peak, "source": "profiles/issue_rate.txt"}
+
+
+def reference_cuda(w, args):
+    """The reference's own CUDA forward + TF adjoint (its kernels compiled for
+    sm_103a from its sources, launched as its backend launches them) on the
+    TF-reconstruction workload, FP32 volume (the reference stores no other
+    type), delayed TF accumulation (its default), L2 flushed before every
+    step.  None for other workloads; a reason where the kernels are absent."""
+    if args.workload != "tf_reconstruction_256" or args.res != 256 or args.image != 256:
+        return None
+    from oracle import ref_cuda as R
+    if not R.available():
+        return {"unavailable": "the reference's kernels were not built (no reference sources where the repo was built)"}
+    r = R.time_tf_reconstruction(steps=max(3, args.steps // 2), warmup=args.warmup, delayed=True, w=w)
+    r["source"] = "reference kernels (renderer/renderer_kernels.cuh:92-106, :447-468) built from its sources"
+    return r
+
+
+def grad_check(w, spec, args, vol_s, tf, cam, t_inp, K, inputs):
+    """The metric's accuracy gate on a bounded subset of the workload, through
+    the same entry points and kernels as the timed step: the first two views
+    (reference-frame cameras) or 8192 rays that hit the volume (per-pixel-ray
+    cameras), rendered with a sample record as the step does, their L2-loss
+    gradient against the target images, and the workload's gradients; then
+    the FP64 oracle on the same inputs (the stored volume's rounded values)."""
+    import torch
+    from diffdvr_gb300 import pyrenderer as pr
+    from oracle import check, oracle as O
+    dev = vol_s.device
+    if spec["camera"] == "frame":
+        nv = min(2, cam[0].shape[0])
+        sub = (cam[0][:nv].contiguous(),)
+        W, H = w.width, w.height
+        target_inputs = inputs(t_inp.volume, t_inp.tf, sub)
+        what = f"first {nv} views"
+    else:
+        rs, rd = w.ray_start.reshape(-1, 3), w.ray_dir.reshape(-1, 3)
+        t = -(rs * rd).sum(1)
+        hit = np.nonzero(np.linalg.norm(rs + t[:, None] * rd, axis=1) < 0.866)[0]
+        idx = np.sort(np.random.default_rng(0).choice(hit, size=min(8192, hit.size), replace=False))
+        W, H = idx.size, 1
+        sub = (torch.from_numpy(rs[idx].reshape(1, 1, -1, 3).copy()).to(dev),
+               torch.from_numpy(rd[idx].reshape(1, 1, -1, 3).copy()).to(dev))
+        target_inputs = inputs(t_inp.volume, t_inp.tf, sub)
+        what = f"{idx.size} rays hitting the volume"
+
+    def sized(inp):
+        inp.screen_size = pr.int2(W, H)
+        return inp
+
+    inp = sized(inputs(vol_s, tf, sub))
+    target_inputs = sized(target_inputs)
+    B = sub[0].shape[0]
+    color = torch.empty(B, H, W, 4, device=dev)
+    term = torch.empty(B, H, W, dtype=torch.int32, device=dev)
+    out = pr.RendererOutputs(color, term, torch.empty(B, H, W, pr.Renderer.checkpoint_slots(inp, K), device=dev), K)
+    out.sample_density = torch.empty(pr.Renderer.sample_density_size(inp, B), device=dev)
+    out.sample_offset = torch.empty(B, H, W, dtype=torch.int32, device=dev)
+    pr.Renderer.render_forward(inp, out)
+    target = torch.empty_like(color)
+    pr.Renderer.render_forward(target_inputs, pr.RendererOutputs(target, torch.empty_like(term)))
+    adj_color = (color - target) * (2.0 / color.numel())
+    a = pr.AdjointOutputs()
+    grads = {}
+    if "tf" in w.grads:
+        a.has_tf_derivatives = True
+        a.tf_delayed_accumulation = True
+        a.adj_tf = grads["adj_tf"] = torch.zeros(tf.shape, device=dev)
+    if "volume" in w.grads:
+        a.has_volume_derivatives = True
+        a.adj_volume = grads["adj_volume"] = torch.zeros(vol_s.shape, device=dev)
+    if "camera" in w.grads:
+        a.has_camera_derivatives = True
+        a.adj_camera_ray_start = grads["adj_ray_start"] = torch.zeros(B, H, W, 3, device=dev)
+        a.adj_camera_ray_dir = grads["adj_ray_dir"] = torch.zeros(B, H, W, 3, device=dev)
+    pr.Renderer.render_adjoint(inp, out, adj_color, a)
+    torch.cuda.synchronize()
+    vol_np = vol_s.float().cpu().numpy()
+    sc = O.Scene(width=W, height=H, volume=vol_np, tf=tf.cpu().numpy(),
+                 step_size=np.full((1, 1, 1), w.step_size, np.float32),
+                 box_min=np.asarray([w.box_min], np.float32), box_size=np.asarray([w.box_size], np.float32),
+                 filter_mode=w.filter_mode, tf_mode=w.tf_mode, blend_mode=w.blend_mode,
+                 camera_mode=2 if spec["camera"] == "frame" else 0)
+    if spec["camera"] == "frame":
+        sc.camera_matrix = sub[0].cpu().numpy()
+        sc.fov_y_radians = float(np.float32(w.fov_y))
+    else:
+        sc.ray_start, sc.ray_dir = sub[0].cpu().numpy(), sub[1].cpu().numpy()
+    t0 = time.perf_counter()
+    r = check.render_errors(sc, color.cpu().numpy(), term.cpu().numpy(), adj_color.cpu().numpy(),
+                            {k: v.double().cpu().numpy() for k, v in grads.items()})
+    r["oracle_s"] = round(time.perf_counter() - t0, 1)
+    r["subset"] = what
+    r["against"] = "FP64 oracle on the same inputs (stored volume values), L2-loss output adjoint"
+    return r
 
 
 def run_gpu(args):
@@ -524,6 +668,52 @@ def run_gpu(args):
         plain = {"samples_per_s": samples32 / (ms_plain / 1e3), "ms_per_step": ms_plain,
                  "kernels": "plain FP32 (one thread per ray, blend inversion)"}
 
+    # ---- memory-lean arm: no sample record, transmittance checkpoints only
+    checkpoint_only = None
+    if pool > 0 and not forward_method:
+        out_ck = pr.RendererOutputs(color, term, ckpt, K)
+        fwd_ev.clear()
+        adj_ev.clear()
+
+        def ck_step(record=False):
+            e = (ev(), ev(), ev(), ev()) if record else None
+            if record:
+                e[0].record()
+            pr.Renderer.render_forward(inp_s, out_ck)
+            if record:
+                e[1].record()
+            torch.sub(color, target, out=adj_color)
+            adj_color.mul_(2 * inv_n)
+            for t in g_tensors:
+                t.zero_()
+            if record:
+                e[2].record()
+            pr.Renderer.render_adjoint(inp_s, out_ck, adj_color, adj)
+            if record:
+                e[3].record()
+                fwd_ev.append((e[0], e[1]))
+                adj_ev.append((e[2], e[3]))
+
+        graph_ck = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(stream):
+            ck_step()
+            torch.cuda.synchronize()
+            with torch.cuda.graph(graph_ck, stream=stream):
+                ck_step()
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            ms_ck = timed(lambda: graph_ck.replay(), max(3, args.steps // 2), args.warmup)
+            for _ in range(3):
+                flush.zero_()
+                ck_step(record=True)
+            torch.cuda.synchronize()
+        checkpoint_only = {
+            "samples_per_s": samples / (ms_ck / 1e3), "ms_per_step": ms_ck,
+            "forward_ms": float(np.mean([a_.elapsed_time(b_) for a_, b_ in fwd_ev])),
+            "adjoint_ms": float(np.mean([a_.elapsed_time(b_) for a_, b_ in adj_ev])),
+            "checkpoint_interval": K, "checkpoint_MB": round(ckpt.numel() * 4 / 1e6, 1),
+            "path": "no sample record; the general adjoint re-marches each K-sample segment from its checkpoint"}
+
     # ---- aggregate over ranks (max time)
     ms_graph, ms_e2e = max_over_ranks([ms_graph, ms_e2e], world, dev)
     value = job_rate(samples, world, ms_graph)
@@ -550,7 +740,13 @@ def run_gpu(args):
             adj_bytes += V * s_v  # the pre-shaded record holds opacities only: colours are gathered again
         names = ("adjoint", "forward")
     dominant = (names[0], adj_bytes, adj_ms) if adj_ms >= fwd_ms else (names[1], fwd_bytes, fwd_ms)
-    achieved = dominant[1] / (dominant[2] / 1e3) / 1e9
+    # the compulsory HBM model of the measurement plan: volume, per-ray outputs
+    # and inputs, gradients and checkpoints, without the sample record this
+    # design chooses to write
+    comp_fwd, comp_adj = compulsory_bytes(w, s_v, V, P, ck_written, tf.numel(), fs.D if forward_method else 0)
+    comp = comp_adj if dominant[0] == names[0] else comp_fwd
+    achieved = comp / (dominant[2] / 1e3) / 1e9
+    achieved_rec = dominant[1] / (dominant[2] / 1e3) / 1e9
     tr = profiled_traffic()
     traffic = None
     if tr and tr.get("workload") == args.workload and tr.get("record") == record_mode and tr.get("views") == B \
@@ -599,12 +795,26 @@ def run_gpu(args):
         "kernel_ms": {names[1]: fwd_ms, names[0]: adj_ms},
         "roofline": {"bound": "hbm", "kernel": dominant[0], "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                     "algorithmic_bytes_per_launch": int(dominant[1]),
-                     "gather_model_GBps": gather_bytes / ((fwd_ms + adj_ms) / 1e3) / 1e9},
+                     "algorithmic_bytes_per_launch": int(comp),
+                     "bytes_model": "compulsory: volume once, per-ray outputs and inputs, gradients, checkpoints",
+                     "with_record": {"bytes_per_launch": int(dominant[1]), "achieved": achieved_rec,
+                                     "frac": achieved_rec / peak},
+                     "gather_model_GBps": gather_bytes / ((fwd_ms + adj_ms) / 1e3) / 1e9,
+                     "issue": issue_bound(args.workload, dominant[0], samples, dominant[2])},
         "plain_fp32": plain,
         "speedup_vs_plain_fp32": (value / plain["samples_per_s"]) if plain else None,
+        "checkpoint_only": checkpoint_only,
         "clocks": clock_summary,
     }
+    if rank == 0 and not args.no_cpu:
+        # baselines and the accuracy check: the oracle and the reference's own kernels as checkers
+        result["reference_cuda"] = reference_cuda(w, args)
+        if result["reference_cuda"] and "samples_per_s" in result["reference_cuda"]:
+            result["speedup_vs_reference_cuda"] = value / result["reference_cuda"]["samples_per_s"]
+        if not forward_method and w.filter_mode != 3:
+            chk = grad_check(w, spec, args, vol_s, tf, cam, t_inp, K, inputs)
+            result["grad_check"] = chk
+            result["grad_rel_err"] = chk.get("grad_rel_err")
     if rank == 0:
         result["cpu_baseline"] = None if args.no_cpu else cpu_baseline(w, args, vol32.cpu().numpy(), args.method)
         print(json.dumps(result))

@@ -539,3 +539,9 @@ class GpuTimer:
     def elapsed_ms(self) -> float:
         self._stop.synchronize()
         return self._start.elapsed_time(self._stop)
+
+
+# pyrenderer.Camera and pyrenderer.Orientation (bindings/bindings.cpp:514-552):
+# the reference's diffdvr.Renderer generates per-pixel rays through
+# pyrenderer.Camera.generate_rays when it optimises the camera
+from .camera import Camera, Orientation  # noqa: E402

@@ -122,6 +122,17 @@ def make_case(seed: int, tf_mode: int = 1, filter_mode: int = 1, blend_mode: int
     return case
 
 
+def pad_faces(volume: np.ndarray) -> np.ndarray:
+    """A copy of a (B)XYZ volume whose outermost two layers are equal on
+    every face, so that the trilinear position derivative is continuous
+    where rays enter the box."""
+    v = np.array(volume, copy=True)
+    v[:, 0], v[:, -1] = v[:, 1], v[:, -2]
+    v[:, :, 0], v[:, :, -1] = v[:, :, 1], v[:, :, -2]
+    v[:, :, :, 0], v[:, :, :, -1] = v[:, :, :, 1], v[:, :, :, -2]
+    return v
+
+
 def edge_cases():
     """Degenerate inputs the marcher must handle: (name, case)."""
     cases = []

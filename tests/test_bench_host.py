@@ -45,6 +45,45 @@ def test_algorithmic_bytes_of_the_general_adjoint():
     assert adj == V * s_v + P * 20 + c * 4 + R_C * 8 + V * 8 + P * 48
 
 
+def test_compulsory_bytes_of_the_measurement_plan():
+    """The roofline's primary bytes: volume once per launch, colour +
+    termination written by the forward and read back with the output adjoint
+    by the adjoint, checkpoints (4 B) written and read, gradients
+    read-modify-written once; no sample record.  At the TF-reconstruction
+    workload with every ray recorded (no checkpoints) the forward moves
+    33.6 MB + 10.5 MB."""
+    V, s_v, P, R_C = 256 ** 3, 2, 8 * 256 * 256, 64 * 4
+    w = SimpleNamespace(grads=("tf",))
+    fwd, adj = bench.compulsory_bytes(w, s_v, V, P, ck_written=0, tf_numel=R_C)
+    assert fwd == V * s_v + P * 20
+    assert fwd == pytest.approx(44.0e6, rel=0.01)
+    assert adj == V * s_v + P * 36 + R_C * 8
+    c = 1000
+    w = SimpleNamespace(grads=("tf", "volume", "camera"))
+    fwd, adj = bench.compulsory_bytes(w, s_v, V, P, ck_written=c, tf_numel=R_C)
+    assert fwd == V * s_v + P * 20 + c * 4
+    assert adj == V * s_v + P * 36 + c * 4 + R_C * 8 + V * 8 + P * 48
+    # the forward method: forward variables written once and read once by the contraction
+    w = SimpleNamespace(grads=("tf",))
+    fwd, adj = bench.compulsory_bytes(w, s_v, V, P, ck_written=0, tf_numel=R_C, D=R_C)
+    assert fwd == V * s_v + P * 20 + P * R_C * 16
+    assert adj == P * R_C * 16 + P * 16 + R_C * 8
+
+
+def test_issue_bound_from_the_committed_profile(monkeypatch, tmp_path):
+    """Warp instructions per sample x samples / time against 152 SMs x 4
+    issue slots x the maximum clock."""
+    d = bench.issue_bound("tf_reconstruction_256", "forward", 90_000_000, 0.8)
+    assert d is not None and d["unit"] == "T warp-instr/s"
+    per = d["warp_instructions_per_sample"]
+    assert d["achieved"] == pytest.approx(per * 90e6 / 0.8e-3 / 1e12)
+    assert d["peak"] == pytest.approx(152 * 4 * 2070e6 / 1e12)
+    assert 0 < d["frac"] < 1.2
+    assert bench.issue_bound("no_such_workload", "forward", 1, 1.0) is None
+    monkeypatch.setattr(bench, "ROOT", str(tmp_path))
+    assert bench.issue_bound("tf_reconstruction_256", "forward", 1, 1.0) is None
+
+
 def test_clock_record_summary():
     """Median SM clock under load, the maximum clock, and every throttle
     reason seen active in any sample of the timed region."""

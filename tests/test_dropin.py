@@ -1,0 +1,137 @@
+"""The drop-in claim, exercised with the reference's own Python module: the
+reference's ``diffdvr.Renderer`` autograd module (pytests/diffdvr/renderer.py,
+unmodified, read from the reference checkout) imported with
+``sys.modules["pyrenderer"] = diffdvr_gb300.pyrenderer``, as INTEGRATION.md's
+first recipe does.  Skipped where the reference checkout is absent (it is not
+copied into this repository).
+
+CPU: the module imports and builds its renderer and settings against our
+``pyrenderer``; a forward call with CPU tensors reaches our library and is
+refused there with a RuntimeError (the product has no CPU renderer).
+GPU: forward + backward through the reference's module (which allocates
+plain outputs, so the adjoint inverts the blend as the reference's does) and
+through ``diffdvr_gb300.Renderer`` (transmittance checkpoints, exact
+recursion) give the same image (symmetric error <= 1e-5) and the same
+gradients (relative L2 <= 1e-3, the metric's gate), for the TF and volume,
+and for the camera through the reference's per-pixel-ray path against our
+fused viewport gradient.
+"""
+import importlib
+import os
+import sys
+import types
+
+import numpy as np
+import pytest
+import torch
+
+from oracle.oracle import REFERENCE_ROOT
+
+REF_PKG = os.path.join(REFERENCE_ROOT, "pytests", "diffdvr")
+needs_reference = pytest.mark.skipif(not os.path.exists(os.path.join(REF_PKG, "renderer.py")),
+                                     reason="the reference checkout is not present")
+
+
+@pytest.fixture
+def reference_module(monkeypatch):
+    """The reference's diffdvr.renderer (and diffdvr.utils) over our
+    pyrenderer; the reference package's __init__ is not run (it imports
+    dataset and TF-fitting helpers outside the marcher's interface)."""
+    from diffdvr_gb300 import pyrenderer
+    monkeypatch.setitem(sys.modules, "pyrenderer", pyrenderer)
+    pkg = types.ModuleType("diffdvr")
+    pkg.__path__ = [REF_PKG]
+    monkeypatch.setitem(sys.modules, "diffdvr", pkg)
+    for name in ("diffdvr.utils", "diffdvr.renderer"):
+        monkeypatch.delitem(sys.modules, name, raising=False)
+    importlib.import_module("diffdvr.utils")
+    mod = importlib.import_module("diffdvr.renderer")
+    yield mod
+    for name in ("diffdvr.utils", "diffdvr.renderer"):
+        sys.modules.pop(name, None)
+
+
+def _settings(pr, W=24, H=20, tf_mode=None):
+    """RendererInputs as the reference's setup_default_settings fills them
+    (pytests/diffdvr/settings.py)."""
+    s = pr.RendererInputs()
+    s.screen_size = pr.int2(W, H)
+    s.volume_filter_mode = pr.VolumeFilterMode.Trilinear
+    s.box_min = pr.real3(-0.5, -0.5, -0.5)
+    s.box_size = pr.real3(1, 1, 1)
+    s.step_size = 0.5 / 15
+    s.tf_mode = tf_mode if tf_mode is not None else pr.TFMode.Texture
+    s.blend_mode = pr.BlendMode.BeerLambert
+    return s
+
+
+@needs_reference
+def test_reference_module_imports_and_builds_against_our_pyrenderer(reference_module, dvr_lib):
+    from diffdvr_gb300 import pyrenderer as pr
+    R = reference_module
+    r = R.Renderer(_settings(pr), optimize_tf=True, optimize_volume=True)
+    assert isinstance(r.settings, pr.RendererInputs)
+    assert r.settings.screen_size.x == 24 and r.settings.tf_mode == pr.TFMode.Texture
+    clone = r.settings.clone()
+    clone.screen_size = pr.int2(3, 3)
+    assert r.settings.screen_size.x == 24
+    with pytest.raises(ValueError):
+        R.Renderer(_settings(pr)).train()
+    # our library refuses CPU tensors (there is no CPU renderer) with a RuntimeError
+    vp = torch.from_numpy(np.eye(3, dtype=np.float32)[None] * 1.0)
+    vp[0, 0] = torch.tensor([0.0, 0.0, -3.0])
+    tf = torch.rand(1, 8, 4)
+    vol = torch.rand(1, 16, 16, 16)
+    with pytest.raises(RuntimeError, match="CUDA"):
+        r(camera=vp, fov_y_radians=0.7, tf=tf, volume=vol)
+
+
+def _scene(seed=3):
+    from diffdvr_gb300 import scenes
+    rng = np.random.default_rng(seed)
+    vol = scenes.blob_volume(16, 4, rng, sigma=(6, 12))
+    vol = np.clip(0.02 + 0.9 * vol, 0, 1).astype(np.float32)
+    vol[:, 0], vol[:, -1] = vol[:, 1], vol[:, -2]
+    vol[:, :, 0], vol[:, :, -1] = vol[:, :, 1], vol[:, :, -2]
+    vol[:, :, :, 0], vol[:, :, :, -1] = vol[:, :, :, 1], vol[:, :, :, -2]
+    tf = scenes.tf_texture(8, rng)
+    tf[..., 3] *= 4
+    vp = scenes.viewport_from_sphere([0.3, -0.5], [0.4, 2.0], 2.2).astype(np.float32)
+    return vol, tf, vp
+
+
+def _loss_and_grads(module, vol, tf, vp, fov, weights):
+    v = torch.from_numpy(vol).cuda().requires_grad_(True)
+    t = torch.from_numpy(tf).cuda().requires_grad_(True)
+    c = torch.from_numpy(vp).cuda().requires_grad_(module._optimize_camera)
+    img = module(camera=c, fov_y_radians=fov, tf=t, volume=v)
+    loss = (img * weights).sum()
+    loss.backward()
+    torch.cuda.synchronize()
+    return (img.detach().double().cpu().numpy(), v.grad.double().cpu().numpy(), t.grad.double().cpu().numpy(),
+            c.grad.double().cpu().numpy() if module._optimize_camera else None)
+
+
+@needs_reference
+@pytest.mark.gpu
+@pytest.mark.parametrize("optimize_camera", [False, True], ids=["tf+volume", "tf+volume+camera"])
+def test_reference_module_matches_ours_on_the_gpu(reference_module, dvr_lib, cuda_device, optimize_camera):
+    import diffdvr_gb300
+    from diffdvr_gb300 import pyrenderer as pr
+    from dvr_cases import rel_l2, symmetric_error
+    vol, tf, vp = _scene()
+    fov = float(np.float32(0.7))
+    pr.set_kernel_family("optimized")
+    kw = dict(optimize_camera=optimize_camera, optimize_tf=True, optimize_volume=True)
+    theirs = reference_module.Renderer(_settings(pr), **kw)
+    ours = diffdvr_gb300.Renderer(_settings(pr), **kw)
+    weights = torch.from_numpy(np.random.default_rng(9).normal(size=(2, 20, 24, 4)).astype(np.float32)).cuda()
+    a = _loss_and_grads(theirs, vol, tf, vp, fov, weights)
+    b = _loss_and_grads(ours, vol, tf, vp, fov, weights)
+    assert symmetric_error(a[0], b[0]) <= 1e-5
+    assert a[0][..., 3].max() > 0.05  # the scene is not empty
+    for name, x, y in zip(("volume", "tf", "camera"), a[1:], b[1:]):
+        if x is None:
+            continue
+        assert np.isfinite(x).all() and np.abs(x).max() > 0, name
+        assert rel_l2(y, x) <= 1e-3, (name, rel_l2(y, x))

@@ -4,31 +4,41 @@ The reference's forward and adjoint kernels are compiled from its headers into
 ``oracle/_ref/ref_kernels_sm103a.cubin`` (``oracle/ref_device.cu``), with the
 options of its runtime compiler, and launched through the CUDA driver API as
 its backend launches them (``oracle/ref_cuda.py``).  The cubin is built where
-the reference sources are; these tests skip where it is absent, and they run
-only when DVR_REFERENCE_CUDA_TESTS=1 is set: their tolerances for the
-reference's fast-math build are not yet confirmed over all modes.
+the reference sources are and travels with the repository as device code;
+these tests skip only where it is absent.
 
 The reference's runtime compiler uses --use_fast_math (approximate exp and
 division, flush to zero; renderer/kernel_loader.cpp:218-230), so its CUDA
 path is itself off the exact FP32 result: against the FP64 oracle it
 measured up to 4.6e-5 in the reference's symmetric metric on single pixels
-(texture TF, inverse-view-matrix camera).  Hence:
-* forward: the scenes of test_gpu_parity.test_forward_all_modes (which hold
-  our kernels to max(1e-5, 3 e32) of the FP64 oracle).  The reference's CUDA
-  forward is first checked against the FP64 oracle for gross errors (<= 1e-3,
-  sample counts agreeing on >= 95% of pixels).  On the pixels where the
-  sample counts of ours, the reference's CUDA forward and the FP64 oracle
-  agree, ours is within 1e-5 of the reference's CUDA forward on >= 99% of
-  pixels (>= 97% with nearest filtering, whose voxel choice is
-  rounding-sensitive) and within 1e-4 everywhere.
-* gradients: the scenes of test_gpu_parity.test_adjoint_all_modes, one
-  output adjoint for all three (zero on rays whose sample counts differ);
-  relative L2 between ours and the reference's CUDA adjoint
-  <= max(1e-3, 3 r_ref, 3 r_ours), r_* each one's relative L2 error against
-  the FP64 oracle.
-"""
-import os
+(texture TF, inverse-view-matrix camera).  The comparisons therefore hold
+ours to the reference's CUDA output within 1e-5, widened on each pixel by no
+more than the error the two sides make there against the FP64 oracle (the
+triangle inequality), with every pixel counted:
 
+* forward (the scenes of test_gpu_parity.test_forward_all_modes): on every
+  pixel, |ours - ref_cuda| <= max(1e-5, 3 e32) + e_ref in the symmetric
+  metric, e_ref = the reference CUDA output's error against FP64 on that
+  pixel and e32 = the reference FP32 CPU arithmetic's (the tolerance that
+  test_gpu_parity holds ours to against FP64).  Pixels beyond 1e-5 of the
+  reference CUDA output are counted and reported; termination mismatches
+  are counted and bounded (<= 5% of pixels) and never dropped.
+* gradients (the scenes of test_gpu_parity.test_adjoint_all_modes, one
+  output adjoint for all three, zero on the rays whose sample counts differ
+  between the three, at most 5% of them): relative L2 between ours and the
+  reference CUDA adjoint <= 1e-3 + r_ref, r_ref = the reference CUDA
+  adjoint's own relative L2 error against the FP64 oracle.
+* the reference's delayed TF accumulation (per-thread shared-memory slots,
+  one reduction per warp; renderer/renderer_tf.cuh:173-253, called from
+  renderer/renderer_kernels.cuh:442) adds a warp's whole reduction to the
+  batch entry of the warp's leading lane.  With a TF per batch entry and a
+  warp whose rays straddle two batch entries, gradient moves between the
+  two entries (the total is kept): measured 9.9% relative L2 against its
+  immediate-atomics variant on a two-entry batch of 120-pixel images.  The
+  test holds the delayed variant to the immediate one where it is exact (a
+  broadcast TF), shows the misattribution where it is not, and holds ours
+  to the immediate variant in both cases.
+"""
 import numpy as np
 import pytest
 
@@ -40,8 +50,6 @@ pytestmark = pytest.mark.gpu
 @pytest.fixture(scope="module")
 def ref_cuda(oracle_built, cuda_device):
     from oracle import ref_cuda as R
-    if os.environ.get("DVR_REFERENCE_CUDA_TESTS") != "1":
-        pytest.skip("comparison with the reference's CUDA kernels runs with DVR_REFERENCE_CUDA_TESTS=1")
     if not R.available():
         pytest.skip("the reference's CUDA kernels were not built (no reference sources where the repo was built)")
     return R
@@ -61,26 +69,32 @@ def test_reference_cuda_forward_all_modes(ref_cuda, oracle_built):
         sc = case.oracle_scene()
         rc, rt = ref_cuda.forward(sc)
         c64, t64 = O.forward(sc, "port", "f64")
+        c32, _ = O.forward(sc, "port", "f32")
+        e_ref = _pixel_errors(rc, c64)          # the reference CUDA output against FP64
+        e32 = _pixel_errors(c32, c64)           # the reference's FP32 arithmetic against FP64
         bad = []
-        ref_ok = rt == t64
-        if np.mean(~ref_ok) > 0.05 or not np.all(np.abs(rt - t64) <= 1):
-            bad.append(f"reference CUDA: sample counts differ from FP64 on {np.mean(~ref_ok):.3f}")
-        e_ref = _pixel_errors(rc[ref_ok], c64[ref_ok])
-        if e_ref.size and e_ref.max() > 1e-3:
-            bad.append(f"reference CUDA: colour error {e_ref.max():.2e} against FP64")
-        share = 0.97 if filt == 0 else 0.99
-        stats = [f"mode {(tfm, filt, blend, cam)}: reference CUDA vs FP64 max {e_ref.max() if e_ref.size else 0:.2e}"]
+        if np.mean(rt != t64) > 0.05 or not np.all(np.abs(rt - t64) <= 1):
+            bad.append(f"reference CUDA: sample counts differ from FP64 on {np.mean(rt != t64):.3f}")
+        if e_ref[rt == t64].size and e_ref[rt == t64].max() > 1e-3:
+            bad.append(f"reference CUDA: colour error {e_ref[rt == t64].max():.2e} against FP64")
+        stats = [f"mode {(tfm, filt, blend, cam)}: reference CUDA vs FP64 max {e_ref.max():.2e}"]
         for family in ("plain", "optimized"):
             _, out = gpu_forward(case, family)
             color, term = out.color.cpu().numpy(), out.terminationIndex.cpu().numpy()
-            same = (term == rt) & ref_ok
-            if np.mean(term != rt) > 0.05:
-                bad.append(f"{family}: sample counts differ on {np.mean(term != rt):.3f}")
-            pe = _pixel_errors(color[same], rc[same])
-            if pe.size:
-                stats.append(f"{family} vs reference CUDA max {pe.max():.2e}, within 1e-5 {np.mean(pe <= 1e-5):.3f}")
-            if pe.size and (np.mean(pe <= 1e-5) < share or pe.max() > 1e-4):
-                bad.append(f"{family}: {np.mean(pe <= 1e-5):.3f} of pixels within 1e-5, max {pe.max():.2e}")
+            pe = _pixel_errors(color, rc)
+            tol = np.maximum(1e-5, 3 * e32) + e_ref
+            over = pe > tol
+            beyond = pe > 1e-5
+            mism = np.mean(term != rt)
+            stats.append(f"{family} vs reference CUDA max {pe.max():.2e}, {int(beyond.sum())} of {pe.size} pixels "
+                         f"beyond 1e-5 (all within the per-pixel bound: {not over.any()}), "
+                         f"sample counts differ on {int((term != rt).sum())}")
+            if mism > 0.05:
+                bad.append(f"{family}: sample counts differ from the reference CUDA output on {mism:.3f}")
+            if over.any():
+                k = np.argmax(pe - tol)
+                bad.append(f"{family}: {int(over.sum())} pixels beyond max(1e-5, 3 e32) + e_ref; worst "
+                           f"{pe.flat[k]:.2e} > {tol.flat[k]:.2e}")
         print("; ".join(stats))  # shown in full with the failure report
         if bad:
             failures[(tfm, filt, blend, cam)] = bad
@@ -89,16 +103,18 @@ def test_reference_cuda_forward_all_modes(ref_cuda, oracle_built):
 
 def _three_adjoints(ref_cuda, O, case, inp, out, family, req, adj, gpu_kw, delayed=False):
     """Ours, the reference's CUDA adjoint and the FP64 oracle's, all with one
-    output adjoint that is zero where the sample counts differ."""
+    output adjoint that is zero where the sample counts of the three differ;
+    also returns the share of such rays."""
     sc = case.oracle_scene()
     term = out.terminationIndex.cpu().numpy()
     rc, rt = ref_cuda.forward(sc)
     c64, t64 = O.forward(sc, "port", "f64")
-    adj = np.where(((term == rt) & (rt == t64))[..., None], adj, 0.0).astype(np.float32)
+    agree = (term == rt) & (rt == t64)
+    adj = np.where(agree[..., None], adj, 0.0).astype(np.float32)
     ref = ref_cuda.adjoint(sc, rc, rt, adj, req, delayed=delayed)
     ref64 = O.adjoint(sc, c64, t64, adj, req, "port", "f64")
     got = gpu_adjoint(case, inp, out, adj, family=family, **gpu_kw)
-    return got, ref, ref64
+    return got, ref, ref64, float(np.mean(~agree))
 
 
 @pytest.mark.parametrize("family", ["plain", "optimized"])
@@ -115,16 +131,19 @@ def test_reference_cuda_adjoint_all_modes(family, ref_cuda, oracle_built):
         inp, out = gpu_forward(case, family, checkpoints=(family == "optimized"))
         adj = np.random.default_rng(7).normal(size=out.color.shape).astype(np.float32)
         req = O.AdjointRequest(volume=True, tf=True, camera=cam == 0, stepsize=True)
-        got, ref, ref64 = _three_adjoints(ref_cuda, O, case, inp, out, family, req, adj,
-                                          dict(volume=True, tf=True, camera=cam == 0, stepsize=True))
+        got, ref, ref64, masked = _three_adjoints(ref_cuda, O, case, inp, out, family, req, adj,
+                                                  dict(volume=True, tf=True, camera=cam == 0, stepsize=True))
         bad = {}
-        stats = []
+        stats = [f"{masked:.3f} of rays masked"]
+        if masked > 0.05:
+            bad["masked"] = masked
         for k in got:
             if k == "adj_stepsize" and family == "optimized":
                 continue
             r = rel_l2(got[k], ref[k])
-            tol = max(1e-3, 3 * rel_l2(ref[k], ref64[k]), 3 * rel_l2(got[k], ref64[k]))
-            stats.append(f"{k} {r:.2e} (reference CUDA vs FP64 {rel_l2(ref[k], ref64[k]):.2e})")
+            r_ref = rel_l2(ref[k], ref64[k])
+            tol = 1e-3 + r_ref
+            stats.append(f"{k} {r:.2e} (reference CUDA vs FP64 {r_ref:.2e})")
             if r > tol:
                 bad[k] = (r, tol)
         print(f"mode {(tfm, filt, blend, cam)} {family}: " + ", ".join(stats))
@@ -133,20 +152,30 @@ def test_reference_cuda_adjoint_all_modes(family, ref_cuda, oracle_built):
     assert not failures, failures
 
 
-def test_reference_cuda_delayed_tf_accumulation(ref_cuda, oracle_built):
-    """The reference's default TF adjoint (per-thread shared-memory
-    accumulation, one reduction per warp) equals its immediate-atomics
-    variant up to summation order, and the optimized family's TF-only adjoint
-    from the sample record agrees with it: texture TF (64 entries),
-    trilinear, Beer-Lambert, per-pixel rays."""
+@pytest.mark.parametrize("tf_batch", [1, 2], ids=["broadcast-tf", "tf-per-batch-entry"])
+def test_reference_cuda_delayed_tf_accumulation(tf_batch, ref_cuda, oracle_built):
+    """The reference's default TF adjoint (delayed accumulation) against its
+    immediate-atomics variant and ours: texture TF (64 entries), trilinear,
+    Beer-Lambert, per-pixel rays, two batch entries of 12x10 pixels, so the
+    fourth warp's rays straddle the two entries."""
     O = oracle_built
     case = make_case(77, tf_mode=1, filter_mode=1, blend_mode=0, camera_mode=0, R=64, opacity=0.25, pad_faces=True)
+    if tf_batch == 1:
+        case.tf = np.ascontiguousarray(case.tf[:1])
     inp, out = gpu_forward(case, "optimized", checkpoints=True, record="full")
     adj = np.random.default_rng(5).normal(size=out.color.shape).astype(np.float32)
     req = O.AdjointRequest(tf=True)
-    got, ref_del, ref64 = _three_adjoints(ref_cuda, O, case, inp, out, "optimized", req, adj, dict(tf=True),
-                                          delayed=True)
-    _, ref_imm, _ = _three_adjoints(ref_cuda, O, case, inp, out, "optimized", req, adj, dict(tf=True))
-    assert rel_l2(ref_del["adj_tf"], ref_imm["adj_tf"]) <= 1e-4
-    tol = max(1e-3, 3 * rel_l2(ref_del["adj_tf"], ref64["adj_tf"]), 3 * rel_l2(got["adj_tf"], ref64["adj_tf"]))
-    assert rel_l2(got["adj_tf"], ref_del["adj_tf"]) <= tol
+    got, ref_del, ref64, masked = _three_adjoints(ref_cuda, O, case, inp, out, "optimized", req, adj,
+                                                  dict(tf=True), delayed=True)
+    _, ref_imm, _, _ = _three_adjoints(ref_cuda, O, case, inp, out, "optimized", req, adj, dict(tf=True))
+    assert masked <= 0.05
+    r_imm = rel_l2(ref_imm["adj_tf"], ref64["adj_tf"])
+    assert rel_l2(got["adj_tf"], ref_imm["adj_tf"]) <= 1e-3 + r_imm
+    diff = rel_l2(ref_del["adj_tf"], ref_imm["adj_tf"])
+    # the total over batch entries is the same either way
+    assert rel_l2(ref_del["adj_tf"].sum(0), ref_imm["adj_tf"].sum(0)) <= 1e-4
+    print(f"tf batch {tf_batch}: reference delayed vs immediate {diff:.2e}")
+    if tf_batch == 1:
+        assert diff <= 1e-4
+    else:
+        assert diff > 1e-2, "the reference's delayed accumulation no longer moves gradient between batch entries"
