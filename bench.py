@@ -99,6 +99,8 @@ def parse():
     ap.add_argument("--interval", type=int, default=0, help="transmittance checkpoint interval (workload default)")
     ap.add_argument("--method", choices=["adjoint", "forward"], default="adjoint",
                     help="gradient method: adjoint (the headline) or forward-mode derivatives")
+    ap.add_argument("--window", choices=["on", "off"], default="on",
+                    help="volume gradients from the record through the window adjoint (on) or the general kernel")
     ap.add_argument("--record", choices=["full", "auto", "none"], default="auto",
                     help="sample record: a pool for every ray; one for every ray if that fits in a quarter of "
                          "the free device memory, else as large as that; or none")
@@ -504,6 +506,7 @@ def run_gpu(args):
     # target image: the target volume (absorption reconstruction) or the TF perturbed
     target = torch.empty_like(color)
     pr.set_kernel_family("optimized")
+    pr.set_window_adjoint(args.window == "on")
     if spec["estimate"] in ("const0.1", "half"):
         t_inp = inputs(vol_target32.to(sdt), tf, cam)
     else:
@@ -781,7 +784,7 @@ def run_gpu(args):
                    "tf_storage": "f32", "views": B, "image": [H, W], "volume": list(w.volume.shape[1:]),
                    "gradients": sorted(grads), "samples_per_step": samples, "rays_hit": rays_hit,
                    "method": args.method, "forward_derivatives": fs.D if forward_method else None,
-                   "checkpoint_interval": K, "sample_record": record_mode,
+                   "checkpoint_interval": K, "sample_record": record_mode, "window_adjoint": args.window,
                    "recorded_rays": recorded_rays, "record_pool_MB": round(pool * 4 / 1e6, 1),
                    "l2": "flushed (256 MB write) before every timed step",
                    "graph": "forward+loss+adjoint captured in one CUDA graph",
@@ -907,17 +910,30 @@ def run_gpu_batched(args):
             d["adj"].adj_tf.zero_()
             d["adj"].adj_volume.zero_()
 
+    # tile shapes per size class from the autotuner (a fresh cache: every run searches)
+    from diffdvr_gb300.autotune import SHAPE_NAMES, TileTuner
+    import tempfile
+    tuner = TileTuner(cache_path=os.path.join(tempfile.mkdtemp(prefix="dvr_tune_"), "tiles.json"))
+    with torch.cuda.stream(stream):
+        pr.Renderer.render_forward_batched(ins, outs)
+        loss_grads()
+        t0 = time.perf_counter()
+        fwd_shapes, adj_shapes = tuner.tune(ins, outs, adjs, aos, storage=args.storage)
+        torch.cuda.synchronize()
+        tune_s = time.perf_counter() - t0
+    shapes = {"forward": list(fwd_shapes), "adjoint": list(adj_shapes)}
+
     def step(record=False):
         if record:
             e = (ev(), ev(), ev(), ev())
             e[0].record()
-        pr.Renderer.render_forward_batched(ins, outs)
+        pr.Renderer.render_forward_batched(ins, outs, shapes["forward"])
         if record:
             e[1].record()
         loss_grads()
         if record:
             e[2].record()
-        pr.Renderer.render_adjoint_batched(ins, outs, adjs, aos)
+        pr.Renderer.render_adjoint_batched(ins, outs, adjs, aos, shapes["adjoint"])
         if record:
             e[3].record()
             fwd_ev.append((e[0], e[1]))
@@ -969,6 +985,34 @@ def run_gpu_batched(args):
     fwd_ms = float(np.mean([a.elapsed_time(b) for a, b in fwd_ev]))
     adj_ms = float(np.mean([a.elapsed_time(b) for a, b in adj_ev]))
 
+    # ---- the same step with the fixed 16x8 tile, for the tuner's gain
+    tuned = dict(shapes)
+    shapes["forward"], shapes["adjoint"] = [0] * len(I), [0] * len(I)
+    fwd_ev.clear()
+    adj_ev.clear()
+    graph_fixed = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(stream):
+        step()
+        torch.cuda.synchronize()
+        with torch.cuda.graph(graph_fixed, stream=stream):
+            step()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        ms_fixed = timed(lambda: graph_fixed.replay(), args.steps, args.warmup)
+        for _ in range(3):
+            flush.zero_()
+            step(record=True)
+        torch.cuda.synchronize()
+    tile_tuning = {
+        "classes": len(set(tuner.cache.get(tuner._device(), {}).keys())), "tuning_s": round(tune_s, 2),
+        "search": tuner.report, "tuned_ms_per_step": ms_graph, "fixed_16x8_ms_per_step": ms_fixed,
+        "gain": ms_fixed / ms_graph,
+        "fixed_16x8_kernel_ms": {"forward": float(np.mean([a.elapsed_time(b) for a, b in fwd_ev])),
+                                 "adjoint": float(np.mean([a.elapsed_time(b) for a, b in adj_ev]))},
+        "forward_shapes": [SHAPE_NAMES[t] for t in tuned["forward"]],
+        "adjoint_shapes": [SHAPE_NAMES[t] for t in tuned["adjoint"]]}
+    shapes.update(tuned)
+
     # ---- e2e: the batched public API with every input copied from pinned host memory
     host = [{k: d[k].cpu().pin_memory() for k in ("vol_s", "tf", "rs", "rd", "target")} for d in I]
     devc = [{k: torch.empty_like(d[k]) for k in ("vol_s", "tf", "rs", "rd", "target")} for d in I]
@@ -981,11 +1025,11 @@ def run_gpu_batched(args):
         for h, c in zip(host, devc):
             for k in h:
                 c[k].copy_(h[k], non_blocking=True)
-        pr.Renderer.render_forward_batched(ins_e2e, outs)
+        pr.Renderer.render_forward_batched(ins_e2e, outs, shapes["forward"])
         loss_grads([c["target"] for c in devc])
         for j, d in enumerate(I):
             loss_d[j] = (d["adj_color"] * d["adj_color"]).sum() / (4 * d["inv_n"] * d["inv_n"])
-        pr.Renderer.render_adjoint_batched(ins_e2e, outs, adjs, aos)
+        pr.Renderer.render_adjoint_batched(ins_e2e, outs, adjs, aos, shapes["adjoint"])
         loss_host.copy_(loss_d, non_blocking=True)
         for gh, d in zip(grad_host, I):
             gh.copy_(d["adj"].adj_tf, non_blocking=True)
@@ -1041,6 +1085,7 @@ def run_gpu_batched(args):
                 "path": "pyrenderer.Renderer.render_forward_batched/render_adjoint_batched, pinned host inputs"},
         "gpu_launches": 2 * launches * args.steps,
         "kernel_ms": {"forward": fwd_ms, "adjoint": adj_ms},
+        "tile_tuning": tile_tuning,
         "roofline": {"bound": "hbm", "kernel": dominant[0], "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_launch": int(dominant[1]),

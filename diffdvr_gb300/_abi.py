@@ -140,10 +140,21 @@ SIGNATURES = {
     "dvr_set_sync_mode": (ctypes.c_int, [ctypes.c_int32]),
     "dvr_get_sync_mode": (ctypes.c_int, []),
     "dvr_abi_version": (ctypes.c_int, []),
+    "dvr_set_window_adjoint": (ctypes.c_int, [ctypes.c_int32]),
+    "dvr_get_window_adjoint": (ctypes.c_int, []),
+    "dvr_last_adjoint_path": (ctypes.c_int, []),
+    "dvr_render_forward_batched_tiled": (ctypes.c_int, [_P(DvrRendererInputs), _P(DvrRendererOutputs),
+                                                        _P(ctypes.c_int32), ctypes.c_int32, ctypes.c_void_p]),
+    "dvr_render_adjoint_batched_tiled": (ctypes.c_int, [_P(DvrRendererInputs), _P(DvrRendererOutputs), _P(DvrTensor),
+                                                        _P(DvrAdjointOutputs), _P(ctypes.c_int32), ctypes.c_int32,
+                                                        ctypes.c_void_p]),
 }
 
+# DvrAdjointPath
+ADJOINT_PATHS = {0: "none", 1: "plain", 2: "general", 3: "record", 4: "window", 5: "preshaded"}
+
 _LIB = None
-ABI_VERSION = 4
+ABI_VERSION = 5
 
 
 def library_path() -> str:

@@ -45,8 +45,9 @@ std::vector<int> cost_order(const RenderParams* ps, int n) {
 }
 
 // items (batch entries x tiles) of one instance
-int64_t instance_items(const RenderParams& p) {
-  return int64_t(p.B) * ((p.W + kTileW - 1) / kTileW) * ((p.H + kTileH - 1) / kTileH);
+int64_t instance_items(const RenderParams& p, int shape) {
+  const int tw = tile_w(shape), th = tile_h(shape);
+  return int64_t(p.B) * ((p.W + tw - 1) / tw) * ((p.H + th - 1) / th);
 }
 
 template <int TF>
@@ -132,8 +133,8 @@ int* acquire_counter(int device, cudaStream_t s, cudaError_t& err) {
   return err == cudaSuccess ? c : nullptr;
 }
 
-cudaError_t launch_batched_forward(const RenderParams* ps, int n, int filter, int tf_mode, int blend, int,
-                                   const LaunchInfo&, cudaStream_t s) {
+cudaError_t launch_batched_forward(const RenderParams* ps, const unsigned char* shapes, int n, int filter, int tf_mode,
+                                   int blend, int, const LaunchInfo&, cudaStream_t s) {
   const std::vector<int> order = cost_order(ps, n);
   for (int first = 0; first < n; first += kBatchMax) {
     BatchForwardTable t{};
@@ -143,7 +144,8 @@ cudaError_t launch_batched_forward(const RenderParams* ps, int n, int filter, in
     for (int j = 0; j < t.n; ++j) {
       const RenderParams& p = ps[order[first + j]];
       t.p[j] = p;
-      items += instance_items(p);
+      t.shape[j] = shapes[order[first + j]];
+      items += instance_items(p, t.shape[j]);
       if (items > 0x7fffffff) return cudaErrorInvalidConfiguration;
       t.item_end[j] = int(items);
       smem = std::max(smem, size_t(p.R) * p.C * sizeof(float));
@@ -161,8 +163,8 @@ cudaError_t launch_batched_forward(const RenderParams* ps, int n, int filter, in
   return cudaSuccess;
 }
 
-cudaError_t launch_batched_adjoint(const RenderParams* ps, const AdjointParams* as, int n, int filter, int tf_mode,
-                                   int blend, int, const LaunchInfo&, cudaStream_t s) {
+cudaError_t launch_batched_adjoint(const RenderParams* ps, const AdjointParams* as, const unsigned char* shapes, int n,
+                                   int filter, int tf_mode, int blend, int, const LaunchInfo&, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   const std::vector<int> order = cost_order(ps, n);
   const bool tg = as[0].has_tf != 0, vg = as[0].has_volume != 0;
@@ -175,7 +177,8 @@ cudaError_t launch_batched_adjoint(const RenderParams* ps, const AdjointParams* 
       const int i = order[first + j];
       t.p[j] = ps[i];
       t.a[j] = as[i];
-      items += instance_items(ps[i]);
+      t.shape[j] = shapes[i];
+      items += instance_items(ps[i], t.shape[j]);
       if (items > 0x7fffffff) return cudaErrorInvalidConfiguration;
       t.item_end[j] = int(items);
       const int seg = ps[i].ckpt.p ? ps[i].ckpt_interval : 0;

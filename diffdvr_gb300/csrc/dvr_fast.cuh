@@ -30,7 +30,7 @@
 
 namespace dvr {
 
-constexpr int kTileW = 16, kTileH = 8, kFastThreads = 128;
+constexpr int kFastThreads = 128;
 
 // Batched launches carry their instance descriptors in the kernel parameter
 // (up to 32 KB since CUDA 12.1), so a batched call needs no staging copy and
@@ -38,25 +38,36 @@ constexpr int kTileW = 16, kTileH = 8, kFastThreads = 128;
 // (instance, batch entry, tile) item; instances are ordered by decreasing
 // cost and item_end[i] is the end of instance i's items.
 constexpr int kBatchMax = 24;  // instances per launch: 24 * (752 + 400) B of descriptors fit
+
+// Tile shapes of the batched launches: every warp covers an 8x4 pixel patch
+// and the four warps of a block sit side by side in tile_warps_x(shape)
+// columns (DvrTileShape): 16x8 (2 x 2 warps), 32x4 (4 x 1), 8x16 (1 x 4).
+__host__ __device__ constexpr int tile_warps_x(int shape) { return shape == 1 ? 4 : (shape == 2 ? 1 : 2); }
+__host__ __device__ constexpr int tile_w(int shape) { return 8 * tile_warps_x(shape); }
+__host__ __device__ constexpr int tile_h(int shape) { return 4 * (4 / tile_warps_x(shape)); }
+
 struct BatchForwardTable {
   int n;
   int item_end[kBatchMax];
+  unsigned char shape[kBatchMax];  // tile shape of each instance
   RenderParams p[kBatchMax];
 };
 struct BatchAdjointTable {
   int n;
   int item_end[kBatchMax];
+  unsigned char shape[kBatchMax];
   RenderParams p[kBatchMax];
   AdjointParams a[kBatchMax];
 };
 static_assert(sizeof(BatchAdjointTable) <= 32764, "kernel parameter limit");
 
-__device__ __forceinline__ void batch_item(const int* item_end, int n, const RenderParams* ps, int item, int& inst,
-                                           int& b, int& tx, int& ty) {
+__device__ __forceinline__ void batch_item(const int* item_end, const unsigned char* shapes, int n,
+                                           const RenderParams* ps, int item, int& inst, int& b, int& tx, int& ty) {
   inst = 0;
   while (inst + 1 < n && item >= item_end[inst]) ++inst;
   const int local = item - (inst > 0 ? item_end[inst - 1] : 0);
-  const int tiles_x = (ps[inst].W + kTileW - 1) / kTileW, tiles_y = (ps[inst].H + kTileH - 1) / kTileH;
+  const int tw = tile_w(shapes[inst]), th = tile_h(shapes[inst]);
+  const int tiles_x = (ps[inst].W + tw - 1) / tw, tiles_y = (ps[inst].H + th - 1) / th;
   const int per_b = tiles_x * tiles_y;
   b = local / per_b;
   const int r = local - b * per_b;
@@ -65,11 +76,13 @@ __device__ __forceinline__ void batch_item(const int* item_end, int n, const Ren
 }
 constexpr int kMaxSegment = 64;  // largest checkpoint interval
 
-// Maps thread -> pixel within a 16x8 tile: warp w covers an 8x4 patch.
-__device__ __forceinline__ void tile_pixel(int tid, int& px, int& py) {
-  const int w = tid >> 5, l = tid & 31;
-  px = ((w & 1) << 3) + (l & 7);
-  py = ((w >> 1) << 2) + (l >> 3);
+// Maps thread -> pixel within a tile of the given shape: warp w covers an
+// 8x4 patch, the warps sit in tile_warps_x(shape) columns.  Shape 0 is the
+// 16x8 tile of the window kernel.
+__device__ __forceinline__ void tile_pixel(int tid, int& px, int& py, int shape = 0) {
+  const int w = tid >> 5, l = tid & 31, wx = tile_warps_x(shape);
+  px = (w % wx) * 8 + (l & 7);
+  py = (w / wx) * 4 + (l >> 3);
 }
 
 template <typename VT>
@@ -165,11 +178,12 @@ struct Sampler {
 
 // ----------------------------------------------------------------- forward
 template <int FILTER, int TF, int BLEND, typename VT>
-__device__ __forceinline__ void fast_forward_tile(const RenderParams& p, int b, int tx, int ty, float* s_tf) {
+__device__ __forceinline__ void fast_forward_tile(const RenderParams& p, int b, int tx, int ty, float* s_tf,
+                                                  int shape) {
   constexpr int C = TfChannels<TF>::C;
   int px, py;
-  tile_pixel(threadIdx.x, px, py);
-  const int x = tx * kTileW + px, y = ty * kTileH + py;
+  tile_pixel(threadIdx.x, px, py, shape);
+  const int x = tx * tile_w(shape) + px, y = ty * tile_h(shape) + py;
   if (x >= p.W || y >= p.H) return;
   FastRay r;
   fast_setup(p, x, y, b, r);
@@ -203,19 +217,6 @@ __device__ __forceinline__ void fast_forward_tile(const RenderParams& p, int b, 
   static_cast<int*>(p.term.p)[b * p.term.s[0] + y * p.term.s[1] + x * p.term.s[2]] = k;
 }
 
-template <int FILTER, int TF, int BLEND, typename VT>
-__global__ void __launch_bounds__(kFastThreads) fast_forward_kernel(const RenderParams p, int tiles_x, int tiles_y) {
-  extern __shared__ float4 fast_smem4[];
-  float* s_tf = reinterpret_cast<float*>(fast_smem4);
-  const int tiles_per_b = tiles_x * tiles_y;
-  const int b = blockIdx.x / tiles_per_b;
-  const int rem = blockIdx.x - b * tiles_per_b;
-  const int ty = rem / tiles_x, tx = rem - ty * tiles_x;
-  stage_tf(p, b, s_tf);
-  __syncthreads();
-  fast_forward_tile<FILTER, TF, BLEND, VT>(p, b, tx, ty, s_tf);
-}
-
 // Batched variant: one block per work item (instance, batch entry, tile) of
 // a list ordered by decreasing estimated cost; the instance descriptors live
 // in device memory.
@@ -224,11 +225,11 @@ __global__ void __launch_bounds__(kFastThreads) fast_forward_batched_kernel(cons
   extern __shared__ float4 fast_smem4[];
   float* s_tf = reinterpret_cast<float*>(fast_smem4);
   int inst, b, tx, ty;
-  batch_item(t.item_end, t.n, t.p, int(blockIdx.x), inst, b, tx, ty);
+  batch_item(t.item_end, t.shape, t.n, t.p, int(blockIdx.x), inst, b, tx, ty);
   const RenderParams& p = t.p[inst];
   stage_tf(p, b, s_tf);
   __syncthreads();
-  fast_forward_tile<FILTER, TF, BLEND, VT>(p, b, tx, ty, s_tf);
+  fast_forward_tile<FILTER, TF, BLEND, VT>(p, b, tx, ty, s_tf, t.shape[inst]);
 }
 
 // ----------------------------------------------------------------- adjoint
@@ -789,13 +790,13 @@ __device__ __forceinline__ void fast_reverse_step(const RenderParams& p, const A
 
 template <int FILTER, int TF, int BLEND, bool VOLGRAD, bool TFGRAD, typename VT>
 __device__ __forceinline__ void fast_adjoint_tile(const RenderParams& p, const AdjointParams& a, int b, int tx, int ty,
-                                                  float* s_tf, float* s_grad, float* s_lane, int s_lane_slots,
-                                                  int* s_lo, float* s_seg) {
+                                                  int shape, float* s_tf, float* s_grad, float* s_lane,
+                                                  int s_lane_slots, int* s_lo, float* s_seg) {
   constexpr int C = TfChannels<TF>::C;
   constexpr unsigned kFull = 0xffffffffu;
   int px, py;
-  tile_pixel(threadIdx.x, px, py);
-  const int x = tx * kTileW + px, y = ty * kTileH + py;
+  tile_pixel(threadIdx.x, px, py, shape);
+  const int x = tx * tile_w(shape) + px, y = ty * tile_h(shape) + py;
   // every lane stays in the loops below (pixels outside the image have no
   // samples) so that the warp can reconverge explicitly after each step
   const bool valid = x < p.W && y < p.H;
@@ -925,7 +926,7 @@ __host__ __device__ inline size_t fast_adjoint_smem(int tf_mode, int R, int C, b
 
 template <int FILTER, int TF, int BLEND, bool VOLGRAD, bool TFGRAD, typename VT>
 __device__ __forceinline__ void fast_adjoint_block(const RenderParams& p, const AdjointParams& a, int b, int tx,
-                                                   int ty) {
+                                                   int ty, int shape) {
   extern __shared__ float4 fast_smem4[];
   constexpr int C = TfChannels<TF>::C;
   float* smem = reinterpret_cast<float*>(fast_smem4);
@@ -938,7 +939,7 @@ __device__ __forceinline__ void fast_adjoint_block(const RenderParams& p, const 
     for (int e = threadIdx.x; e < L.seg - L.warp; e += blockDim.x) s_grad[e] = 0.f;
   }
   __syncthreads();
-  fast_adjoint_tile<FILTER, TF, BLEND, VOLGRAD, TFGRAD, VT>(p, a, b, tx, ty, smem + L.tf, s_grad, smem + L.lane,
+  fast_adjoint_tile<FILTER, TF, BLEND, VOLGRAD, TFGRAD, VT>(p, a, b, tx, ty, shape, smem + L.tf, s_grad, smem + L.lane,
                                                             L.slots, reinterpret_cast<int*>(smem + L.lo),
                                                             smem + L.seg);
   if constexpr (TFGRAD) {
@@ -949,20 +950,10 @@ __device__ __forceinline__ void fast_adjoint_block(const RenderParams& p, const 
 }
 
 template <int FILTER, int TF, int BLEND, bool VOLGRAD, bool TFGRAD, typename VT>
-__global__ void __launch_bounds__(kFastThreads) fast_adjoint_kernel(const RenderParams p, const AdjointParams a,
-                                                                     int tiles_x, int tiles_y) {
-  const int tiles_per_b = tiles_x * tiles_y;
-  const int b = blockIdx.x / tiles_per_b;
-  const int rem = blockIdx.x - b * tiles_per_b;
-  const int ty = rem / tiles_x, tx = rem - ty * tiles_x;
-  fast_adjoint_block<FILTER, TF, BLEND, VOLGRAD, TFGRAD, VT>(p, a, b, tx, ty);
-}
-
-template <int FILTER, int TF, int BLEND, bool VOLGRAD, bool TFGRAD, typename VT>
 __global__ void __launch_bounds__(kFastThreads) fast_adjoint_batched_kernel(const __grid_constant__ BatchAdjointTable t) {
   int inst, b, tx, ty;
-  batch_item(t.item_end, t.n, t.p, int(blockIdx.x), inst, b, tx, ty);
-  fast_adjoint_block<FILTER, TF, BLEND, VOLGRAD, TFGRAD, VT>(t.p[inst], t.a[inst], b, tx, ty);
+  batch_item(t.item_end, t.shape, t.n, t.p, int(blockIdx.x), inst, b, tx, ty);
+  fast_adjoint_block<FILTER, TF, BLEND, VOLGRAD, TFGRAD, VT>(t.p[inst], t.a[inst], b, tx, ty, t.shape[inst]);
 }
 
 }  // namespace dvr

@@ -6,6 +6,7 @@
 #pragma once
 #include "dvr_record.cuh"
 #include "dvr_warpray.cuh"
+#include "dvr_window.cuh"
 #include "dvr_kernels.h"
 
 namespace dvr {
@@ -191,6 +192,71 @@ static cudaError_t fast_adjoint_record_go(const RenderParams& p, const AdjointPa
   return cudaGetLastError();
 }
 
+// The window kernel (dvr_window.cuh) adds its gradient window to global
+// memory in 16-byte groups and stages the volume in 16-byte rows: both
+// tensors must be z-contiguous with 16-byte aligned rows.
+static bool rows_aligned(const void* base, const int64_t* st, int Z, int per16) {
+  return st[3] == 1 && st[0] % per16 == 0 && st[1] % per16 == 0 && st[2] % per16 == 0 && Z % per16 == 0 &&
+         (reinterpret_cast<uintptr_t>(base) & 15u) == 0;
+}
+constexpr int kWinGradCap = 6144;    // floats of the gradient window (24 KB)
+constexpr int kWinVolBytes = 16384;  // bytes of the staged volume window
+
+// Volume-gradient adjoint from the sample record: the window kernel over
+// 16x8 tiles, then the general kernel over the rays without a record.
+template <int TF, int BLEND, typename VT>
+static cudaError_t fast_adjoint_window_go(const RenderParams& p, const AdjointParams& a, const RayOrder& order,
+                                          int* counter, size_t gsmem, const LaunchInfo& li, cudaStream_t s) {
+  constexpr int C = TfChannels<TF>::C;
+  const bool tfgrad = a.has_tf != 0;
+  const bool stage = (a.has_camera || a.has_stepsize) &&
+                     rows_aligned(p.volume.p, p.volume.s, p.Z, 16 / int(sizeof(VT)));
+  const int copies = p.tf.s[0] == 0 ? 1 : p.B;
+  const int vol_cap = kWinVolBytes / int(sizeof(VT));
+  const WinSmem S(TF, p.R, C, tfgrad, copies, kWinGradCap, stage ? kWinVolBytes : 0);
+  const size_t wsmem = size_t(S.total) * sizeof(float);
+  if (wsmem > size_t(li.max_smem_optin)) return cudaErrorInvalidConfiguration;
+  const WinTiles tiles = WinTiles::make(p.W, p.H, p.B);
+  auto launch = [&](auto wk, auto gk) -> cudaError_t {
+    cudaError_t e = set_smem(wk, wsmem);
+    if (e != cudaSuccess) return e;
+    e = set_smem(gk, gsmem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wk, kFastThreads, wsmem) != cudaSuccess || per_sm < 1)
+      per_sm = 1;
+    const int wgrid = std::max(1, std::min(tiles.total(), per_sm * li.num_sms));
+    const int ggrid = li.num_sms;
+    // scratch: leftover ray list, the two kernels' TF-gradient slices
+    const size_t left_bytes = (size_t(order.total()) * sizeof(int) + 255) & ~size_t(255);
+    const size_t wtf = tfgrad ? ((size_t(wgrid) * p.R * C * sizeof(float) + 255) & ~size_t(255)) : 0;
+    const size_t gtf = tfgrad ? size_t(ggrid) * p.R * C * sizeof(float) : 0;
+    char* scratch = static_cast<char*>(acquire_scratch(li.device, s, left_bytes + wtf + gtf, e));
+    if (!scratch) return e;
+    int* leftover = reinterpret_cast<int*>(scratch);
+    wk<<<wgrid, kFastThreads, wsmem, s>>>(p, a, tiles, order, counter,
+                                          tfgrad ? reinterpret_cast<float*>(scratch + left_bytes) : nullptr,
+                                          leftover, kWinGradCap, vol_cap);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    int* counter2 = acquire_counter(li.device, s, e);
+    if (!counter2) return e;
+    gk<<<ggrid, kFastThreads, gsmem, s>>>(p, a, order, counter2,
+                                          tfgrad ? reinterpret_cast<float*>(scratch + left_bytes + wtf) : nullptr,
+                                          leftover, counter + 1);
+    return cudaGetLastError();
+  };
+  if (tfgrad)
+    return stage ? launch(window_adjoint_kernel<TF, BLEND, true, true, VT>,
+                          fast_adjoint_persistent_kernel<kTrilinear, TF, BLEND, true, true, VT>)
+                 : launch(window_adjoint_kernel<TF, BLEND, true, false, VT>,
+                          fast_adjoint_persistent_kernel<kTrilinear, TF, BLEND, true, true, VT>);
+  return stage ? launch(window_adjoint_kernel<TF, BLEND, false, true, VT>,
+                        fast_adjoint_persistent_kernel<kTrilinear, TF, BLEND, true, false, VT>)
+               : launch(window_adjoint_kernel<TF, BLEND, false, false, VT>,
+                        fast_adjoint_persistent_kernel<kTrilinear, TF, BLEND, true, false, VT>);
+}
+
 template <int FILTER, int TF, int BLEND, typename VT>
 static cudaError_t fast_adjoint_go(const RenderParams& p, const AdjointParams& a, const LaunchInfo& li,
                                    cudaStream_t s) {
@@ -229,8 +295,18 @@ static cudaError_t fast_adjoint_go(const RenderParams& p, const AdjointParams& a
       const bool per_batch = a.adj_tf.s[0] != 0;
       (void)per_batch;
       const size_t rsmem = size_t(record_smem_floats(p.R, C, copies)) * sizeof(float);
-      if (rsmem <= size_t(li.max_smem_optin))
+      if (rsmem <= size_t(li.max_smem_optin)) {
+        last_adjoint_path() = DVR_PATH_RECORD;
         return fast_adjoint_record_go<FILTER, BLEND, VT>(p, a, order, counter, rsmem, smem, li, s);
+      }
+    }
+  }
+  if constexpr (FILTER == kTrilinear) {
+    // volume gradients from the sample record: the window kernel
+    if (volgrad && p.dens && p.ckpt.p && !a.has_viewport && window_adjoint_on() &&
+        rows_aligned(a.adj_volume.p, a.adj_volume.s, p.Z, 4)) {
+      last_adjoint_path() = DVR_PATH_WINDOW;
+      return fast_adjoint_window_go<TF, BLEND, VT>(p, a, order, counter, smem, li, s);
     }
   }
   if (volgrad)

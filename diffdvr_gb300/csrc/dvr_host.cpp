@@ -29,6 +29,8 @@ namespace {
 
 thread_local std::string g_last_error;
 std::atomic<int> g_family{DVR_KERNELS_OPTIMIZED};
+std::atomic<int> g_window{0};
+thread_local int g_adjoint_path = DVR_PATH_NONE;
 std::atomic<int> g_sync{0};
 
 struct DvrError : std::runtime_error {
@@ -660,6 +662,9 @@ cudaError_t dispatch_forward_gradients(const Checked& c, const FwdGradParams& g,
 
 }  // namespace
 
+int& last_adjoint_path() { return g_adjoint_path; }
+bool window_adjoint_on() { return g_window.load() != 0; }
+
 int render_adjoint_into(const DvrRendererInputs* inputs, const DvrRendererOutputs* outputs_from_forward,
                         const DvrTensor* adj_color, const DvrAdjointOutputs* adj_outputs, void* cuda_stream,
                         ScratchSource source) {
@@ -712,6 +717,7 @@ extern "C" int dvr_render_forward(const DvrRendererInputs* inputs, const DvrRend
 extern "C" int dvr_render_adjoint(const DvrRendererInputs* inputs, const DvrRendererOutputs* outputs_from_forward,
                                   const DvrTensor* adj_color, const DvrAdjointOutputs* adj_outputs,
                                   void* cuda_stream) {
+  g_adjoint_path = DVR_PATH_NONE;
   return guarded([&] {
     if (!inputs || !outputs_from_forward || !adj_color || !adj_outputs)
       fail(DVR_E_INVALID_ARGUMENT, "arguments must not be NULL");
@@ -722,12 +728,28 @@ extern "C" int dvr_render_adjoint(const DvrRendererInputs* inputs, const DvrRend
     const LaunchInfo li = launch_info(c.device);
     const bool plain = use_plain(c, &a);
     cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+    g_adjoint_path = c.filter == DVR_FILTER_PRESHADED ? DVR_PATH_PRESHADED : plain ? DVR_PATH_PLAIN : DVR_PATH_GENERAL;
     after_launch(dispatch_adjoint(c, a, plain, li, s), s, "adjoint");
   });
 }
 
+// Tile shape of each instance (DvrTileShape), default 16x8.
+std::vector<unsigned char> tile_shapes(const int32_t* shapes, int n) {
+  std::vector<unsigned char> out(n, 0);
+  for (int i = 0; shapes && i < n; ++i) {
+    if (shapes[i] < DVR_TILE_16x8 || shapes[i] > DVR_TILE_8x16) fail(DVR_E_INVALID_ARGUMENT, "unknown tile shape");
+    out[i] = static_cast<unsigned char>(shapes[i]);
+  }
+  return out;
+}
+
 extern "C" int dvr_render_forward_batched(const DvrRendererInputs* inputs, const DvrRendererOutputs* outputs,
                                           int32_t n, void* cuda_stream) {
+  return dvr_render_forward_batched_tiled(inputs, outputs, nullptr, n, cuda_stream);
+}
+
+extern "C" int dvr_render_forward_batched_tiled(const DvrRendererInputs* inputs, const DvrRendererOutputs* outputs,
+                                                const int32_t* shapes, int32_t n, void* cuda_stream) {
   return guarded([&] {
     if (n < 0 || (n > 0 && (!inputs || !outputs))) fail(DVR_E_INVALID_ARGUMENT, "invalid instance list");
     if (n == 0) return;
@@ -749,7 +771,9 @@ extern "C" int dvr_render_forward_batched(const DvrRendererInputs* inputs, const
     std::vector<RenderParams> ps(n);
     for (int i = 0; i < n; ++i) ps[i] = cs[i].p;
     cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
-    after_launch(launch_batched_forward(ps.data(), n, cs[0].filter, cs[0].tf_mode, cs[0].blend, cs[0].device, li, s),
+    const std::vector<unsigned char> ts = tile_shapes(shapes, n);
+    after_launch(launch_batched_forward(ps.data(), ts.data(), n, cs[0].filter, cs[0].tf_mode, cs[0].blend,
+                                        cs[0].device, li, s),
                  s, "batched forward");
   });
 }
@@ -757,6 +781,14 @@ extern "C" int dvr_render_forward_batched(const DvrRendererInputs* inputs, const
 extern "C" int dvr_render_adjoint_batched(const DvrRendererInputs* inputs,
                                           const DvrRendererOutputs* outputs_from_forward, const DvrTensor* adj_colors,
                                           const DvrAdjointOutputs* adj_outputs, int32_t n, void* cuda_stream) {
+  return dvr_render_adjoint_batched_tiled(inputs, outputs_from_forward, adj_colors, adj_outputs, nullptr, n,
+                                          cuda_stream);
+}
+
+extern "C" int dvr_render_adjoint_batched_tiled(const DvrRendererInputs* inputs,
+                                                const DvrRendererOutputs* outputs_from_forward,
+                                                const DvrTensor* adj_colors, const DvrAdjointOutputs* adj_outputs,
+                                                const int32_t* shapes, int32_t n, void* cuda_stream) {
   return guarded([&] {
     if (n < 0 || (n > 0 && (!inputs || !outputs_from_forward || !adj_colors || !adj_outputs)))
       fail(DVR_E_INVALID_ARGUMENT, "invalid instance list");
@@ -784,8 +816,9 @@ extern "C" int dvr_render_adjoint_batched(const DvrRendererInputs* inputs,
     std::vector<RenderParams> ps(n);
     for (int i = 0; i < n; ++i) ps[i] = cs[i].p;
     cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
-    after_launch(launch_batched_adjoint(ps.data(), as.data(), n, cs[0].filter, cs[0].tf_mode, cs[0].blend,
-                                        cs[0].device, li, s),
+    const std::vector<unsigned char> ts = tile_shapes(shapes, n);
+    after_launch(launch_batched_adjoint(ps.data(), as.data(), ts.data(), n, cs[0].filter, cs[0].tf_mode,
+                                        cs[0].blend, cs[0].device, li, s),
                  s, "batched adjoint");
   });
 }
@@ -1077,3 +1110,6 @@ extern "C" int dvr_get_kernel_family(void) { return g_family.load(); }
 extern "C" int dvr_set_sync_mode(int32_t sync) { return g_sync.exchange(sync ? 1 : 0); }
 extern "C" int dvr_get_sync_mode(void) { return g_sync.load(); }
 extern "C" int dvr_abi_version(void) { return DVR_ABI_VERSION; }
+extern "C" int dvr_set_window_adjoint(int32_t enable) { return g_window.exchange(enable ? 1 : 0); }
+extern "C" int dvr_get_window_adjoint(void) { return g_window.load(); }
+extern "C" int dvr_last_adjoint_path(void) { return g_adjoint_path; }

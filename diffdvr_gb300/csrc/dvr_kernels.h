@@ -3,6 +3,7 @@
 // compiles them in parallel; dvr_host.cu dispatches on the TF mode.
 #pragma once
 #include <cuda_runtime.h>
+#include "diffdvr_gb300.h"
 #include "dvr_params.h"
 
 namespace dvr {
@@ -10,6 +11,11 @@ namespace dvr {
 // Viewport derivatives are summed per batch entry in shared memory: at most
 // this many entries (9 floats each).
 constexpr int kMaxViewportBatch = 256;
+
+// Which adjoint kernels the last call on this thread launched (DvrAdjointPath)
+// and the window-adjoint switch (dvr_set_window_adjoint).
+int& last_adjoint_path();
+bool window_adjoint_on();
 
 struct LaunchInfo {
   int num_sms;

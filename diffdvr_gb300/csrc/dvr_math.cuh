@@ -45,4 +45,11 @@ template <> struct Storage<__nv_bfloat16> {
   static __device__ __forceinline__ float load(const __nv_bfloat16* p) { return __bfloat162float(__ldg(p)); }
 };
 
+// Conversion of one stored value to FP32 without a read-only global load:
+// for copies of the volume staged in shared memory (Storage<T>::load reads
+// through the non-coherent global path, which is for global memory only).
+__device__ __forceinline__ float to_float(float v) { return v; }
+__device__ __forceinline__ float to_float(__half v) { return __half2float(v); }
+__device__ __forceinline__ float to_float(__nv_bfloat16 v) { return __bfloat162float(v); }
+
 }  // namespace dvr

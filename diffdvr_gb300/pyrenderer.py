@@ -382,8 +382,11 @@ class Renderer:
                                                           ctypes.byref(cg), _stream_of(forward_variables)))
 
     @staticmethod
-    def render_forward_batched(inputs: Sequence[RendererInputs], outputs: Sequence[RendererOutputs]) -> None:
-        """Renders instances of different volume/image sizes in one launch."""
+    def render_forward_batched(inputs: Sequence[RendererInputs], outputs: Sequence[RendererOutputs],
+                               tile_shapes: Optional[Sequence[int]] = None) -> None:
+        """Renders instances of different volume/image sizes in one launch.
+        tile_shapes: a DvrTileShape per instance (0 = 16x8, 1 = 32x4, 2 =
+        8x16), e.g. from diffdvr_gb300.autotune; None = 16x8 for all."""
         lib = _abi.load()
         n = len(inputs)
         if len(outputs) != n:
@@ -391,11 +394,12 @@ class Renderer:
         ci = (_abi.DvrRendererInputs * max(n, 1))(*[_inputs(i) for i in inputs])
         co = (_abi.DvrRendererOutputs * max(n, 1))(*[_outputs(o) for o in outputs])
         stream = _stream_of(inputs[0].volume) if n else 0
-        _abi.check(lib.dvr_render_forward_batched(ci, co, n, stream))
+        _abi.check(lib.dvr_render_forward_batched_tiled(ci, co, _shapes(tile_shapes, n), n, stream))
 
     @staticmethod
     def render_adjoint_batched(inputs: Sequence[RendererInputs], outputs_from_forward: Sequence[RendererOutputs],
-                               adj_colors: Sequence[torch.Tensor], adj_outputs: Sequence[AdjointOutputs]) -> None:
+                               adj_colors: Sequence[torch.Tensor], adj_outputs: Sequence[AdjointOutputs],
+                               tile_shapes: Optional[Sequence[int]] = None) -> None:
         lib = _abi.load()
         n = len(inputs)
         if not (len(outputs_from_forward) == len(adj_colors) == len(adj_outputs) == n):
@@ -405,7 +409,7 @@ class Renderer:
         ca = (_abi.DvrTensor * max(n, 1))(*[_tensor(a, "adj_color") for a in adj_colors])
         cg = (_abi.DvrAdjointOutputs * max(n, 1))(*[_adjoint_outputs(a) for a in adj_outputs])
         stream = _stream_of(inputs[0].volume) if n else 0
-        _abi.check(lib.dvr_render_adjoint_batched(ci, co, ca, cg, n, stream))
+        _abi.check(lib.dvr_render_adjoint_batched_tiled(ci, co, ca, cg, _shapes(tile_shapes, n), n, stream))
 
     @staticmethod
     def checkpoint_slots(inputs: RendererInputs, interval: int = 16) -> int:
@@ -513,6 +517,27 @@ def set_kernel_cache_file(filename: str) -> None:
 
 def set_cuda_debug_mode(debug: bool) -> None:
     pass
+
+
+def _shapes(tile_shapes, n: int):
+    """ctypes int32 array of n tile shapes, or None."""
+    if tile_shapes is None:
+        return None
+    if len(tile_shapes) != n:
+        raise RuntimeError("tile_shapes must hold one shape per instance")
+    return (ctypes.c_int32 * max(n, 1))(*[int(t) for t in tile_shapes])
+
+
+def set_window_adjoint(enable: bool) -> bool:
+    """Volume gradients from the sample record through the window adjoint
+    or the general per-ray adjoint; returns the previous setting."""
+    return bool(_abi.load().dvr_set_window_adjoint(int(bool(enable))))
+
+
+def last_adjoint_path() -> str:
+    """The kernels the last render_adjoint call on this thread ran: "plain",
+    "general", "record", "window", "preshaded" or "none"."""
+    return _abi.ADJOINT_PATHS.get(_abi.load().dvr_last_adjoint_path(), "none")
 
 
 def cleanup() -> None:

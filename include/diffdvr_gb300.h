@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define DVR_ABI_VERSION 4
+#define DVR_ABI_VERSION 5
 
 /* ---- status codes ---- */
 #define DVR_OK 0
@@ -234,6 +234,22 @@ int dvr_render_adjoint_batched(const DvrRendererInputs* inputs, const DvrRendere
                                const DvrTensor* adj_colors, const DvrAdjointOutputs* adj_outputs, int32_t n,
                                void* cuda_stream);
 
+/* Tile shapes of the batched launches: one block of 128 rays per tile, every
+ * warp an 8x4 pixel patch, the four warps side by side (16x8: 2x2, 32x4: 4x1,
+ * 8x16: 1x4). */
+enum DvrTileShape { DVR_TILE_16x8 = 0, DVR_TILE_32x4 = 1, DVR_TILE_8x16 = 2 };
+/* dvr_render_forward_batched / dvr_render_adjoint_batched with a tile shape
+ * per instance: tile_shapes holds n DvrTileShape values (NULL = 16x8 for
+ * every instance), for example chosen per size class by the autotuner of
+ * the Python package (diffdvr_gb300.autotune).  No counterpart in the
+ * reference, whose only launch tuning is an occupancy-based block size
+ * (renderer/renderer_cuda.cpp:97-108). */
+int dvr_render_forward_batched_tiled(const DvrRendererInputs* inputs, const DvrRendererOutputs* outputs,
+                                     const int32_t* tile_shapes, int32_t n, void* cuda_stream);
+int dvr_render_adjoint_batched_tiled(const DvrRendererInputs* inputs, const DvrRendererOutputs* outputs_from_forward,
+                                     const DvrTensor* adj_colors, const DvrAdjointOutputs* adj_outputs,
+                                     const int32_t* tile_shapes, int32_t n, void* cuda_stream);
+
 /* Mirrors renderer::ForwardDifferencesSettingsHost (renderer/renderer.h:73-93):
  * which variables forward-mode differentiation traces, each given the index
  * of its derivative in [0, D); -1 = not traced. */
@@ -291,6 +307,29 @@ const char* dvr_last_error(void);
 /* Kernel family selection (process-wide).  Returns the previous value. */
 int dvr_set_kernel_family(int32_t family);
 int dvr_get_kernel_family(void);
+
+/* Volume gradients from the sample record: nonzero = the window adjoint
+ * (tiles of rays walked back to front in slabs of equal ray distance, each
+ * slab's volume gradient accumulated in shared memory and added to global
+ * memory once per touched group of four voxels, the volume staged in shared
+ * memory by bulk copies where camera or step-size gradients need corner
+ * densities), 0 = the general per-ray adjoint, which scatters with atomics on
+ * every cell exit as the reference does.  Process-wide.  Returns the previous
+ * value.  No counterpart in the reference. */
+int dvr_set_window_adjoint(int32_t enable);
+int dvr_get_window_adjoint(void);
+
+/* Which kernels the last dvr_render_adjoint call on the calling thread ran
+ * (DvrAdjointPath).  No counterpart in the reference. */
+enum DvrAdjointPath {
+  DVR_PATH_NONE = 0,     /* no call yet, or the call failed before launching */
+  DVR_PATH_PLAIN = 1,    /* plain family */
+  DVR_PATH_GENERAL = 2,  /* general per-ray kernel (checkpoints or blend inversion) */
+  DVR_PATH_RECORD = 3,   /* record kernel (TF gradient of a texture TF from the sample record) */
+  DVR_PATH_WINDOW = 4,   /* window kernel (volume gradient from the sample record) */
+  DVR_PATH_PRESHADED = 5 /* pre-shaded kernels */
+};
+int dvr_last_adjoint_path(void);
 
 /* In sync mode every launch is followed by cudaStreamSynchronize and a launch
  * error check, for debugging (renderer::Renderer::setCudaSyncMode,
