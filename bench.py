@@ -99,8 +99,9 @@ def parse():
     ap.add_argument("--interval", type=int, default=0, help="transmittance checkpoint interval (workload default)")
     ap.add_argument("--method", choices=["adjoint", "forward"], default="adjoint",
                     help="gradient method: adjoint (the headline) or forward-mode derivatives")
-    ap.add_argument("--window", choices=["on", "off"], default="on",
-                    help="volume gradients from the record through the window adjoint (on) or the general kernel")
+    ap.add_argument("--window", choices=["on", "off"], default="off",
+                    help="volume gradients from the record through the window adjoint (on) or the general kernel "
+                         "(off, the library's default)")
     ap.add_argument("--record", choices=["full", "auto", "none"], default="auto",
                     help="sample record: a pool for every ray; one for every ray if that fits in a quarter of "
                          "the free device memory, else as large as that; or none")

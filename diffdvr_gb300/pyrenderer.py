@@ -530,7 +530,8 @@ def _shapes(tile_shapes, n: int):
 
 def set_window_adjoint(enable: bool) -> bool:
     """Volume gradients from the sample record through the window adjoint
-    or the general per-ray adjoint; returns the previous setting."""
+    or the general per-ray adjoint (the default, measured faster); returns
+    the previous setting."""
     return bool(_abi.load().dvr_set_window_adjoint(int(bool(enable))))
 
 
