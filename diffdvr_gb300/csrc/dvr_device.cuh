@@ -256,10 +256,21 @@ struct TfGlobal {
   __device__ __forceinline__ f4 rgba(int r) const { return mk4(at(r, 0), at(r, 1), at(r, 2), at(r, 3)); }
 };
 // TF accessor over a dense R*C copy in shared memory (optimized kernels).
+// For a piecewise-linear TF (C = 5) it records whether the control-point
+// positions are non-decreasing, which lets linear_interval search them in
+// log2(R) steps.
 template <int C>
 struct TfShared {
   const float* p;
   int R;
+  bool sorted = false;
+  __device__ __forceinline__ TfShared(const float* p_, int R_) : p(p_), R(R_) {
+    if constexpr (C == 5) {
+      bool s = true;
+      for (int i = 0; i + 1 < R; ++i) s &= p[i * C + 4] <= p[(i + 1) * C + 4];
+      sorted = s;
+    }
+  }
   __device__ __forceinline__ float at(int r, int c) const { return p[r * C + c]; }
   __device__ __forceinline__ f4 rgba(int r) const {
     if constexpr (C == 4) {
@@ -277,8 +288,31 @@ template <> struct TfChannels<kTfTexture> { static constexpr int C = 4; };
 template <> struct TfChannels<kTfLinear> { static constexpr int C = 5; };
 template <> struct TfChannels<kTfGaussian> { static constexpr int C = 6; };
 
+// Interval of a piecewise-linear TF: the first i in [0, R-2) whose next
+// control point lies above the density, else R-2
+// (renderer/renderer_tf.cuh:294-300).
 template <class A>
 __device__ __forceinline__ int linear_interval(const A& tf, float density) {
+  int i;
+  for (i = 0; i < tf.R - 2; ++i)
+    if (tf.at(i + 1, 4) > density) break;
+  return i;
+}
+// The same from a shared-memory TF: with non-decreasing positions "next
+// point above the density" is monotone in i, so a binary search over
+// [0, R-2] finds the same first i (a NaN density, above no point, gives
+// R-2 either way) in ceil(log2(R-1)) steps that every lane takes alike;
+// unsorted positions keep the reference's scan.
+__device__ __forceinline__ int linear_interval(const TfShared<5>& tf, float density) {
+  if (tf.sorted) {
+    int lo = 0, hi = tf.R - 2;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (tf.at(mid + 1, 4) > density) hi = mid;
+      else lo = mid + 1;
+    }
+    return lo;
+  }
   int i;
   for (i = 0; i < tf.R - 2; ++i)
     if (tf.at(i + 1, 4) > density) break;

@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(kFastThreads) fast_adjoint_persistent_kernel(c
           vg.cx = -1;
           vg.reset();
           vol.p = static_cast<const VT*>(p.volume.p) + b * p.volume.s[0];
-          tf.p = s_tf + (copies > 1 ? b : 0) * p.R * C;
+          tf = TfShared<C>(s_tf + (copies > 1 ? b : 0) * p.R * C, p.R);
           adjv = VOLGRAD ? static_cast<float*>(a.adj_volume.p) + b * a.adj_volume.s[0] : nullptr;
           ckpt_ray = p.ckpt.p != nullptr && n <= (p.ckpt_slots + 1) * K;
           drow = nullptr;

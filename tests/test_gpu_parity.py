@@ -82,6 +82,31 @@ def test_forward_all_modes(family, oracle_built, cuda_device):
     assert not failures, failures
 
 
+@pytest.mark.parametrize("sort", [True, False], ids=["sorted-positions", "unsorted-positions"])
+def test_linear_tf_interval_search(sort, oracle_built, cuda_device):
+    """The optimized kernels search a piecewise-linear TF's control points
+    by bisection when their positions are non-decreasing, and keep the
+    reference's first-match scan when they are not
+    (renderer/renderer_tf.cuh:294-300): 16 points, forward and adjoint
+    (TF, volume and ray gradients) against the FP64 oracle, whose scan
+    defines the interval either way."""
+    O = oracle_built
+    case = make_case(57, tf_mode=2, R=16, shape=(18, 20, 22), W=30, H=24, B=2, opacity=0.4, pad_faces=True)
+    if not sort:
+        rng = np.random.default_rng(3)
+        for b in range(case.tf.shape[0]):
+            case.tf[b, 1:-1, 4] = rng.permutation(case.tf[b, 1:-1, 4])
+        assert np.any(np.diff(case.tf[..., 4], axis=1) < 0)
+    inp, out = gpu_forward(case, "optimized", checkpoints=True)
+    _compare_forward(case, out.color.cpu().numpy(), out.terminationIndex.cpu().numpy(), O)
+    adj = np.random.default_rng(8).normal(size=out.color.shape)
+    req = O.AdjointRequest(volume=True, tf=True, camera=True)
+    ref, adj = reference_adjoint(case, O, out.terminationIndex.cpu().numpy(), adj, req)
+    got = gpu_adjoint(case, inp, out, adj, volume=True, tf=True, camera=True)
+    bad = _grad_errors(got, ref)
+    assert not bad, bad
+
+
 @pytest.mark.parametrize("family", FAMILIES)
 def test_forward_matches_reference_fixtures(family, oracle_built, cuda_device):
     """Against the reference's own FP64 and FP32 CPU renders (fixtures), with
