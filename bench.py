@@ -880,6 +880,7 @@ def run_gpu_batched(args):
         d["out"] = pr.RendererOutputs(d["color"], d["term"],
                                       torch.empty(1, w.height, w.width, slots, device=dev), K)
         d["slots"] = slots
+        d["pool"] = pr.Renderer.sample_density_size(d["inp"], 1) if args.record != "none" else 0
         a = pr.AdjointOutputs()
         a.has_tf_derivatives = True
         a.tf_delayed_accumulation = True
@@ -896,6 +897,14 @@ def run_gpu_batched(args):
                                    pr.RendererOutputs(d["target"], torch.empty_like(d["term"])))
         d["inv_n"] = 1.0 / d["color"].numel()
         I.append(d)
+    # sample records (every ray its fixed run of its instance's pool), when they fit
+    pool_total = sum(d["pool"] for d in I)
+    free, _ = torch.cuda.mem_get_info(dev)
+    use_record = pool_total > 0 and (args.record == "full" or pool_total * 4 <= free // 4)
+    if use_record:
+        for d in I:
+            d["out"].sample_density = torch.empty(d["pool"], device=dev)
+            d["out"].sample_offset = torch.empty(1, d["w"].height, d["w"].width, dtype=torch.int32, device=dev)
     torch.cuda.synchronize()
     ins, outs = [d["inp"] for d in I], [d["out"] for d in I]
     adjs, aos = [d["adj_color"] for d in I], [d["adj"] for d in I]
@@ -1053,7 +1062,7 @@ def run_gpu_batched(args):
         P = w.width * w.height
         ck = int(torch.clamp((d["term"].to(torch.int64) - 1) // K, min=0).clamp_max(d["slots"]).sum().item())
         S = int(d["term"].to(torch.int64).sum().item())
-        f, a = algorithmic_bytes(w, d["vol_s"].element_size(), V, P, S, ck, False, False, d["tf"].numel())
+        f, a = algorithmic_bytes(w, d["vol_s"].element_size(), V, P, S, ck, use_record, False, d["tf"].numel())
         fwd_bytes += f
         adj_bytes += a
     dominant = ("adjoint", adj_bytes, adj_ms) if adj_ms >= fwd_ms else ("forward", fwd_bytes, fwd_ms)
@@ -1078,6 +1087,8 @@ def run_gpu_batched(args):
                    "volume_edges": [int(d["w"].volume.shape[1]) for d in I],
                    "image_edges": [int(d["w"].width) for d in I], "gradients": ["tf", "volume"],
                    "samples_per_step": samples, "checkpoint_interval": K,
+                   "sample_record": "full" if use_record else "none",
+                   "record_pool_MB": round(pool_total * 4 / 1e6, 1) if use_record else 0,
                    "l2": "flushed (256 MB write) before every timed step",
                    "graph": "batched forward + loss gradients + batched adjoint captured in one CUDA graph",
                    "parallelism": f"replicas x{world}"},

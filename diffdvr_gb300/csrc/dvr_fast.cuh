@@ -197,6 +197,19 @@ __device__ __forceinline__ void fast_forward_tile(const RenderParams& p, int b, 
   const int K = p.ckpt_interval;
   int next_ck = K, slot = 0;
   const int kmax = max_samples(r.tmin, r.tmax, r.step);
+  // sample record: every ray owns a fixed run of the pool (pool / rays
+  // groups of 4 floats, in pixel order), so no counter is needed; a ray
+  // whose samples do not fit gets offset -1 and is re-marched by the adjoint
+  float2* rec = nullptr;
+  if (p.dens) {
+    const int64_t rays = int64_t(p.B) * p.H * p.W;
+    const int64_t cap = p.dens_units / rays;
+    const int64_t g = ((int64_t(b) * p.H + y) * p.W + x) * cap;
+    const bool fits = int64_t((kmax + 1) >> 1) <= cap && g <= 0x7fffffff;
+    static_cast<int*>(p.dens_off.p)[b * p.dens_off.s[0] + y * p.dens_off.s[1] + x * p.dens_off.s[2]] =
+        fits ? int(g) : -1;
+    if (fits) rec = reinterpret_cast<float2*>(p.dens + 4 * g);
+  }
   int k;
   for (k = 0; k < kmax; ++k) {
     const float t = r.tmin + k * r.step;
@@ -208,6 +221,7 @@ __device__ __forceinline__ void fast_forward_tile(const RenderParams& p, int b, 
       next_ck += K;
     }
     const float density = smp.sample(vol, fast_pos(r, t));
+    if (rec) rec[k] = make_float2(density, acc.w);
     acc = blend<BLEND>(acc, tf_eval<TF>(tf, density), r.step);
   }
   float* col = static_cast<float*>(p.color.p) + b * p.color.s[0] + y * p.color.s[1] + x * p.color.s[2];
@@ -889,20 +903,35 @@ __device__ __forceinline__ void fast_adjoint_tile(const RenderParams& p, const A
                             : nullptr;
   float* seg_d = s_seg + threadIdx.x;  // [offset][thread]
   float* seg_a = s_seg + K * blockDim.x + threadIdx.x;
+  // the forward's sample record, when the ray has one: density and incoming
+  // opacity of every sample, no re-march
+  const float2* drow = nullptr;
+  if (ckpt_ok && p.dens) {
+    const int g = static_cast<const int*>(p.dens_off.p)[b * p.dens_off.s[0] + y * p.dens_off.s[1] +
+                                                        x * p.dens_off.s[2]];
+    if (g >= 0 && int64_t(g) + ((n + 1) >> 1) <= p.dens_units)
+      drow = reinterpret_cast<const float2*>(p.dens + 4 * size_t(g));
+  }
   for (int j = nseg_max - 1; j >= 0; --j) {
     const int k0 = j * K;
     const int k1 = j < nseg ? min(n, k0 + K) : k0;
-    // re-march the segment from its checkpoint
-    float alpha = (j > 0 && j < nseg) ? ck[(j - 1) * p.ckpt.s[3]] : 0.f;
+    // re-march the segment from its checkpoint, or read it from the record
+    float alpha = (j > 0 && j < nseg && !drow) ? ck[(j - 1) * p.ckpt.s[3]] : 0.f;
     for (int kk = 0; kk < K; ++kk) {
       const int k = k0 + kk;
       if (k < k1) {
-        const float t = r.tmin + k * r.step;
-        const float density = smp.sample(vol, fast_pos(r, t));
-        const float a_k = blend_alpha<BLEND>(tf_eval<TF>(tf, density).w, r.step);
-        seg_d[kk * blockDim.x] = density;
-        seg_a[kk * blockDim.x] = alpha;
-        alpha = alpha + (1 - alpha) * a_k;
+        if (drow) {
+          const float2 v = __ldg(drow + k);
+          seg_d[kk * blockDim.x] = v.x;
+          seg_a[kk * blockDim.x] = v.y;
+        } else {
+          const float t = r.tmin + k * r.step;
+          const float density = smp.sample(vol, fast_pos(r, t));
+          const float a_k = blend_alpha<BLEND>(tf_eval<TF>(tf, density).w, r.step);
+          seg_d[kk * blockDim.x] = density;
+          seg_a[kk * blockDim.x] = alpha;
+          alpha = alpha + (1 - alpha) * a_k;
+        }
       }
       __syncwarp();
     }

@@ -759,7 +759,6 @@ extern "C" int dvr_render_forward_batched_tiled(const DvrRendererInputs* inputs,
       if (cs[i].filter == DVR_FILTER_PRESHADED)
         fail(DVR_E_UNSUPPORTED, "pre-shaded volumes are rendered by the single-instance entry points");
       check_outputs(outputs[i], cs[i], true);
-      if (cs[i].p.dens) fail(DVR_E_UNSUPPORTED, "the batched entry points do not record sample_density");
       if (i > 0 && (cs[i].filter != cs[0].filter || cs[i].tf_mode != cs[0].tf_mode || cs[i].blend != cs[0].blend ||
                     cs[i].p.vol_storage != cs[0].p.vol_storage || cs[i].p.tf_storage != cs[0].p.tf_storage ||
                     cs[i].device != cs[0].device))
@@ -800,7 +799,6 @@ extern "C" int dvr_render_adjoint_batched_tiled(const DvrRendererInputs* inputs,
       if (cs[i].filter == DVR_FILTER_PRESHADED)
         fail(DVR_E_UNSUPPORTED, "pre-shaded volumes are rendered by the single-instance entry points");
       check_outputs(outputs_from_forward[i], cs[i], false);
-      if (cs[i].p.dens) fail(DVR_E_UNSUPPORTED, "the batched entry points do not record sample_density");
       as[i] = check_adjoint(adj_colors[i], adj_outputs[i], cs[i]);
       if (as[i].has_viewport)
         fail(DVR_E_UNSUPPORTED, "the batched entry points do not compute viewport derivatives");

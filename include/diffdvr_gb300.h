@@ -140,7 +140,11 @@ typedef struct DvrRendererInputs {
  *    float of a pair is the sample's alpha (there is no density), and the
  *    adjoint reads the record when the image has few rays.  N = B*H*W*S with
  *    S = 4 * dvr_checkpoint_slots(length, step, 2) holds every ray.
- *    Written and read by the optimized single-instance entry points only. */
+ *    Written and read by the optimized entry points.  The batched entry
+ *    points give every ray a fixed run of the pool instead of claiming room
+ *    in launch order: pool / (B*H*W) groups of 4 floats, in pixel order;
+ *    rays with more samples than that get offset -1; they write checkpoints
+ *    for every ray. */
 typedef struct DvrRendererOutputs {
   DvrTensor color;
   DvrTensor termination_index;

@@ -283,7 +283,12 @@ def test_reduced_precision_storage(dtype, oracle_built, cuda_device):
     assert not bad, bad
 
 
-def test_batched_uneven_matches_single_instances(cuda_device):
+@pytest.mark.parametrize("record", [None, "full", 0.4], ids=["checkpoints", "full-record", "partial-record"])
+def test_batched_uneven_matches_single_instances(record, cuda_device):
+    """Three instances of different sizes through the batched entry points
+    against single-instance calls; with a sample record every ray owns a
+    fixed run of its instance's pool (rays that do not fit in a pool of 40%
+    get offset -1 and are re-marched from checkpoints)."""
     from diffdvr_gb300 import pyrenderer as pr
     cases = [make_case(61, tf_mode=3, shape=(9, 10, 11), W=20, H=12, B=1),
              make_case(62, tf_mode=3, shape=(17, 13, 15), W=33, H=17, B=2),
@@ -295,9 +300,26 @@ def test_batched_uneven_matches_single_instances(cuda_device):
         B = c.batch()
         ck = torch.empty(B, c.height, c.width, pr.Renderer.checkpoint_slots(inp), device="cuda")
         ins.append(inp)
-        outs.append(pr.RendererOutputs(torch.empty(B, c.height, c.width, 4, device="cuda"),
-                                       torch.empty(B, c.height, c.width, dtype=torch.int32, device="cuda"), ck, 32))
+        o = pr.RendererOutputs(torch.empty(B, c.height, c.width, 4, device="cuda"),
+                               torch.empty(B, c.height, c.width, dtype=torch.int32, device="cuda"), ck, 32)
+        if record is not None:
+            full = pr.Renderer.sample_density_size(inp, B)
+            n = full if record == "full" else max(4, int(full * record) // 4 * 4)
+            o.sample_density = torch.full((n,), float("nan"), device="cuda")
+            o.sample_offset = torch.full((B, c.height, c.width), -7, dtype=torch.int32, device="cuda")
+        outs.append(o)
     pr.Renderer.render_forward_batched(ins, outs)
+    if record is not None:
+        for c, o in zip(cases, outs):
+            off = o.sample_offset.cpu().numpy()
+            rays = off.size
+            cap = o.sample_density.numel() // 4 // rays
+            want = np.arange(rays).reshape(off.shape) * cap
+            hit = (o.terminationIndex.cpu().numpy() > 0) & (off >= 0)
+            assert np.array_equal(off[off >= 0], want[off >= 0])
+            assert (off >= -1).all() and (hit.any())
+            if record == "full":
+                assert (off[o.terminationIndex.cpu().numpy() > 0] >= 0).all()
     torch.cuda.synchronize()
     # the single-instance forward composites each warp's 32 samples with a scan,
     # the batched one sample by sample: equal up to rounding (a sample at the
