@@ -147,8 +147,7 @@ __device__ __forceinline__ void fast_setup(const RenderParams& p, int x, int y, 
 }
 
 __device__ __forceinline__ float3 fast_pos(const FastRay& r, float t) {
-  const float2 xy = __ffma2_rn(make_float2(t, t), make_float2(r.dp.x, r.dp.y), make_float2(r.p0.x, r.p0.y));
-  return make_float3(xy.x, xy.y, fmaf(t, r.dp.z, r.p0.z));
+  return make_float3(fmaf(t, r.dp.x, r.p0.x), fmaf(t, r.dp.y, r.p0.y), fmaf(t, r.dp.z, r.p0.z));
 }
 
 // Density at a position, with a one-cell cache (cx < 0: empty).
@@ -540,24 +539,9 @@ struct TfGradAccum<kTfLinear, TFGRAD> {
     st.slots = slots;
     st.R = R;
   }
-  int interval = -1;  // the interval of the last eval_cached, for the adjoint of the same sample
-  // The TF at density (tf_eval), keeping its control-point interval for adjoint().
-  template <class A>
-  __device__ __forceinline__ f4 eval_cached(const A& tf, float density) {
-    interval = linear_interval(tf, density);
-    const int i = interval;
-    const f4 a = tf.rgba(i), c = tf.rgba(i + 1);
-    const float p0 = tf.at(i, 4), p1 = tf.at(i + 1, 4);
-    const float d = clampf(density, p0, p1);
-    const float fr = (d - p0) / (p1 - p0);
-    const float2 xy = lerp2(make_float2(a.x, a.y), make_float2(c.x, c.y), make_float2(fr, fr));
-    const float2 zw = lerp2(make_float2(a.z, a.w), make_float2(c.z, c.w), make_float2(fr, fr));
-    return mk4(xy.x, xy.y, zw.x, zw.y);
-  }
   template <class A>
   __device__ __forceinline__ float adjoint(const A& tf, float density, f4 adj, float* wc) {
-    const int i = interval >= 0 ? interval : linear_interval(tf, density);
-    interval = -1;
+    const int i = linear_interval(tf, density);
     const f4 a = tf.rgba(i), c = tf.rgba(i + 1);
     const float p0 = tf.at(i, 4), p1 = tf.at(i + 1, 4);
     const float d2 = clampf(density, p0, p1);
@@ -594,38 +578,6 @@ struct TfGradAccum<kTfGaussian, TFGRAD> {
   float acc[kGaussRegs][6];
   LaneStore<6> st;
   bool regs = true;
-  // the Gaussians of the last eval_cached (R <= kGaussRegs), which the
-  // adjoint of the same sample reuses instead of evaluating them again
-  float ni_[kGaussRegs];
-  bool cached = false;
-  // The TF at density (the sum of tf_eval, in its order), keeping each
-  // Gaussian's value for adjoint().
-  template <class A>
-  __device__ __forceinline__ f4 eval_cached(const A& tf, float density) {
-    f4 c = mk4(0, 0, 0, 0);
-    for (int i = 0; i < tf.R; ++i) {
-      const f4 ci = tf.rgba(i);
-      const float ni = gauss(density, tf.at(i, 4), tf.at(i, 5));
-      if (regs) {
-#pragma unroll
-        for (int r = 0; r < kGaussRegs; ++r)
-          if (r == i) ni_[r] = ni;
-      }
-      c.x += ci.x * ni;
-      c.y += ci.y * ni;
-      c.z += ci.z * ni;
-      c.w += ci.w * ni;
-    }
-    cached = regs;
-    return c;
-  }
-  __device__ __forceinline__ float cached_gauss(int i) const {
-    float v = 0.f;
-#pragma unroll
-    for (int r = 0; r < kGaussRegs; ++r)
-      if (r == i) v = ni_[r];
-    return v;
-  }
   __device__ __forceinline__ void bind(float* lane_base, int T, int tid, int slots, int R) {
 #pragma unroll
     for (int i = 0; i < kGaussRegs; ++i)
@@ -645,7 +597,7 @@ struct TfGradAccum<kTfGaussian, TFGRAD> {
       const f4 ci = tf.rgba(i);
       const float mu = tf.at(i, 4), sigma = tf.at(i, 5);
       const float s2 = sigma * sigma;
-      const float ni = cached ? cached_gauss(i) : gauss(density, mu, sigma);
+      const float ni = gauss(density, mu, sigma);
       const float f1 = (mu - density) / s2 * ni;
       const float d1 = dot4(adj, mk4(ci.x * f1, ci.y * f1, ci.z * f1, ci.w * f1));
       adj_density += d1;
@@ -671,7 +623,6 @@ struct TfGradAccum<kTfGaussian, TFGRAD> {
         }
       }
     }
-    cached = false;
     return adj_density;
   }
   __device__ __forceinline__ void set_evict_target(float* base, int64_t sr, int64_t sc) {
@@ -802,10 +753,7 @@ __device__ __forceinline__ void fast_reverse_step(const RenderParams& p, const A
                                                   float* adjv, int k, float density, float alpha_in, f4& adj_acc,
                                                   f3& adj_start, f3& adj_dir, float& adj_step, bool need_pos_grad) {
   const float t = r.tmin + k * r.step;
-  f4 cur;
-  // Gaussian and piecewise-linear TFs keep what the adjoint of the same sample needs again
-  if constexpr (TF == kTfGaussian || TF == kTfLinear) cur = tacc.eval_cached(tf, density);
-  else cur = tf_eval<TF>(tf, density);
+  const f4 cur = tf_eval<TF>(tf, density);
   const float alpha = blend_alpha<BLEND>(cur.w, r.step);
   f4 adj_cur;
   adj_step += blend_adjoint_core<BLEND>(alpha_in, cur, r.step, alpha, adj_acc, adj_cur);
