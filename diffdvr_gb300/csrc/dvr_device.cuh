@@ -208,9 +208,14 @@ __device__ __forceinline__ void fetch_corners(const VolumeRef<VT>& v, int ix, in
   d[7] = v.at(hx, hy, hz);
 }
 
+// lerp(lerp(lerp(d0, d4, fx), lerp(d2, d6, fx), fy),
+//      lerp(lerp(d1, d5, fx), lerp(d3, d7, fx), fy), fz)
+// with the x and y lerps paired: corners 0/1, 2/3, 4/5, 6/7 are z-neighbours.
 __device__ __forceinline__ float trilerp(const float* d, float fx, float fy, float fz) {
-  return lerp1(lerp1(lerp1(d[0], d[4], fx), lerp1(d[2], d[6], fx), fy),
-               lerp1(lerp1(d[1], d[5], fx), lerp1(d[3], d[7], fx), fy), fz);
+  const float2 x_lo = lerp2(make_float2(d[0], d[1]), make_float2(d[4], d[5]), make_float2(fx, fx));
+  const float2 x_hi = lerp2(make_float2(d[2], d[3]), make_float2(d[6], d[7]), make_float2(fx, fx));
+  const float2 y = lerp2(x_lo, x_hi, make_float2(fy, fy));
+  return lerp1(y.x, y.y, fz);
 }
 
 // Trilinear density and its gradient with respect to the volume position.
@@ -336,7 +341,9 @@ __device__ __forceinline__ f4 tf_eval(const A& tf, float density) {
     const int di = int(floorf(d));
     const float df = d - di;
     const f4 a = tf.rgba(clampi(di, 0, R - 1)), c = tf.rgba(clampi(di + 1, 0, R - 1));
-    return mk4(lerp1(a.x, c.x, df), lerp1(a.y, c.y, df), lerp1(a.z, c.z, df), lerp1(a.w, c.w, df));
+    const float2 xy = lerp2(make_float2(a.x, a.y), make_float2(c.x, c.y), make_float2(df, df));
+    const float2 zw = lerp2(make_float2(a.z, a.w), make_float2(c.z, c.w), make_float2(df, df));
+    return mk4(xy.x, xy.y, zw.x, zw.y);
   } else if constexpr (TF == kTfLinear) {
     const int i = linear_interval(tf, density);
     const f4 a = tf.rgba(i), c = tf.rgba(i + 1);

@@ -147,7 +147,8 @@ __device__ __forceinline__ void fast_setup(const RenderParams& p, int x, int y, 
 }
 
 __device__ __forceinline__ float3 fast_pos(const FastRay& r, float t) {
-  return make_float3(fmaf(t, r.dp.x, r.p0.x), fmaf(t, r.dp.y, r.p0.y), fmaf(t, r.dp.z, r.p0.z));
+  const float2 xy = __ffma2_rn(make_float2(t, t), make_float2(r.dp.x, r.dp.y), make_float2(r.p0.x, r.p0.y));
+  return make_float3(xy.x, xy.y, fmaf(t, r.dp.z, r.p0.z));
 }
 
 // Density at a position, with a one-cell cache (cx < 0: empty).

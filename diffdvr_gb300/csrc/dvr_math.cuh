@@ -20,6 +20,12 @@ __host__ __device__ __forceinline__ f4 mk4(float x, float y, float z, float w) {
 __device__ __forceinline__ float dot3(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 __device__ __forceinline__ float dot4(f4 a, f4 b) { return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w; }
 __device__ __forceinline__ float lerp1(float a, float b, float t) { return a + t * (b - a); }
+// Two lerps as one pair of packed FP32 operations (FADD2, FFMA2 on sm_100
+// and later): per element the subtraction and the fused multiply-add that
+// lerp1 compiles to, half the instructions.
+__device__ __forceinline__ float2 lerp2(float2 a, float2 b, float2 t) {
+  return __ffma2_rn(t, __fadd2_rn(b, make_float2(-a.x, -a.y)), a);
+}
 __device__ __forceinline__ float rminf(float a, float b) { return a < b ? a : b; }
 __device__ __forceinline__ float rmaxf(float a, float b) { return a > b ? a : b; }
 __device__ __forceinline__ float clampf(float v, float lo, float hi) { return fmaxf(lo, fminf(v, hi)); }

@@ -87,8 +87,14 @@ struct TexelPairAtomic {
     i = i0;
     const bool same = i1 == i0;
     const float q0 = same ? k0 + k1 : k0, q1 = same ? 0.f : k1;
-    a0 = mk4(fmaf(v.x, q0, a0.x), fmaf(v.y, q0, a0.y), fmaf(v.z, q0, a0.z), fmaf(v.w, q0, a0.w));
-    a1 = mk4(fmaf(v.x, q1, a1.x), fmaf(v.y, q1, a1.y), fmaf(v.z, q1, a1.z), fmaf(v.w, q1, a1.w));
+    // the same fused multiply-adds, two channels per packed instruction
+    const float2 vxy = make_float2(v.x, v.y), vzw = make_float2(v.z, v.w);
+    const float2 a0xy = __ffma2_rn(vxy, make_float2(q0, q0), make_float2(a0.x, a0.y));
+    const float2 a0zw = __ffma2_rn(vzw, make_float2(q0, q0), make_float2(a0.z, a0.w));
+    const float2 a1xy = __ffma2_rn(vxy, make_float2(q1, q1), make_float2(a1.x, a1.y));
+    const float2 a1zw = __ffma2_rn(vzw, make_float2(q1, q1), make_float2(a1.z, a1.w));
+    a0 = mk4(a0xy.x, a0xy.y, a0zw.x, a0zw.y);
+    a1 = mk4(a1xy.x, a1xy.y, a1zw.x, a1zw.y);
   }
 };
 
@@ -103,7 +109,9 @@ __device__ __forceinline__ void record_reverse_step(const TfShared<4>& tf, float
   const float df = dd - di;
   const int i0 = clampi(di, 0, R - 1), i1 = clampi(di + 1, 0, R - 1);
   const f4 t0 = tf.rgba(i0), t1 = tf.rgba(i1);
-  const f4 cur = mk4(lerp1(t0.x, t1.x, df), lerp1(t0.y, t1.y, df), lerp1(t0.z, t1.z, df), lerp1(t0.w, t1.w, df));
+  const float2 xy = lerp2(make_float2(t0.x, t0.y), make_float2(t1.x, t1.y), make_float2(df, df));
+  const float2 zw = lerp2(make_float2(t0.z, t0.w), make_float2(t1.z, t1.w), make_float2(df, df));
+  const f4 cur = mk4(xy.x, xy.y, zw.x, zw.y);
   const float a_k = blend_alpha<BLEND>(cur.w, step);
   f4 adj_cur;
   blend_adjoint_core<BLEND>(a_in, cur, step, a_k, adj_acc, adj_cur);

@@ -130,8 +130,9 @@ __global__ void __launch_bounds__(kFastThreads) fast_forward_warp_kernel(const R
           if (at && slot < p.ckpt_slots) ck[slot * p.ckpt.s[3]] = a_in;
         }
         const float w = (1.f - a_in) * a;
-        cr = fmaf(w, c.x, cr);
-        cg = fmaf(w, c.y, cg);
+        const float2 rg = __ffma2_rn(make_float2(w, w), make_float2(c.x, c.y), make_float2(cr, cg));
+        cr = rg.x;
+        cg = rg.y;
         cb = fmaf(w, c.z, cb);
       }
       if (f < 32) {
