@@ -99,6 +99,8 @@ def parse():
     ap.add_argument("--interval", type=int, default=0, help="transmittance checkpoint interval (workload default)")
     ap.add_argument("--method", choices=["adjoint", "forward"], default="adjoint",
                     help="gradient method: adjoint (the headline) or forward-mode derivatives")
+    ap.add_argument("--gather", choices=["auto", "direct", "cells", "texture"], default="auto",
+                    help="how the forward reads a trilinear sample's corners (pyrenderer.set_forward_gather)")
     ap.add_argument("--window", choices=["on", "off"], default="off",
                     help="volume gradients from the record through the window adjoint (on) or the general kernel "
                          "(off, the library's default)")
@@ -508,6 +510,7 @@ def run_gpu(args):
     target = torch.empty_like(color)
     pr.set_kernel_family("optimized")
     pr.set_window_adjoint(args.window == "on")
+    pr.set_forward_gather(args.gather)
     if spec["estimate"] in ("const0.1", "half"):
         t_inp = inputs(vol_target32.to(sdt), tf, cam)
     else:
@@ -785,7 +788,7 @@ def run_gpu(args):
                    "tf_storage": "f32", "views": B, "image": [H, W], "volume": list(w.volume.shape[1:]),
                    "gradients": sorted(grads), "samples_per_step": samples, "rays_hit": rays_hit,
                    "method": args.method, "forward_derivatives": fs.D if forward_method else None,
-                   "checkpoint_interval": K, "sample_record": record_mode, "window_adjoint": args.window,
+                   "checkpoint_interval": K, "sample_record": record_mode, "window_adjoint": args.window, "forward_gather": args.gather,
                    "recorded_rays": recorded_rays, "record_pool_MB": round(pool * 4 / 1e6, 1),
                    "l2": "flushed (256 MB write) before every timed step",
                    "graph": "forward+loss+adjoint captured in one CUDA graph",

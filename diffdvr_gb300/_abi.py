@@ -142,6 +142,8 @@ SIGNATURES = {
     "dvr_abi_version": (ctypes.c_int, []),
     "dvr_set_window_adjoint": (ctypes.c_int, [ctypes.c_int32]),
     "dvr_get_window_adjoint": (ctypes.c_int, []),
+    "dvr_set_forward_gather": (ctypes.c_int, [ctypes.c_int32]),
+    "dvr_get_forward_gather": (ctypes.c_int, []),
     "dvr_last_adjoint_path": (ctypes.c_int, []),
     "dvr_render_forward_batched_tiled": (ctypes.c_int, [_P(DvrRendererInputs), _P(DvrRendererOutputs),
                                                         _P(ctypes.c_int32), ctypes.c_int32, ctypes.c_void_p]),
@@ -151,10 +153,11 @@ SIGNATURES = {
 }
 
 # DvrAdjointPath
+FORWARD_GATHERS = {"auto": 0, "direct": 1, "cells": 2, "texture": 3}
 ADJOINT_PATHS = {0: "none", 1: "plain", 2: "general", 3: "record", 4: "window", 5: "preshaded"}
 
 _LIB = None
-ABI_VERSION = 5
+ABI_VERSION = 6
 
 
 def library_path() -> str:

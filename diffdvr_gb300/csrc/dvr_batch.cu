@@ -86,6 +86,16 @@ struct ScratchSlot {
 std::mutex g_scratch_mutex;
 std::vector<ScratchSlot> g_scratch;
 
+struct GatherTextureSlot {
+  int device = -1;
+  cudaStream_t stream = nullptr;
+  int W = 0, H = 0, bits = 0;
+  cudaArray_t array = nullptr;
+  cudaTextureObject_t tex = 0;
+};
+std::mutex g_texture_mutex;
+std::vector<GatherTextureSlot> g_textures;
+
 }  // namespace
 
 void* acquire_scratch(int device, cudaStream_t s, size_t bytes, cudaError_t& err, int which) {
@@ -113,6 +123,57 @@ void* acquire_scratch(int device, cudaStream_t s, size_t bytes, cudaError_t& err
     slot->bytes = want;
   }
   return slot->ptr;
+}
+
+cudaError_t acquire_gather_texture(int device, cudaStream_t s, int W, int H, int bits, cudaArray_t& array,
+                                   cudaTextureObject_t& tex) {
+  std::lock_guard<std::mutex> lock(g_texture_mutex);
+  GatherTextureSlot* slot = nullptr;
+  for (auto& e : g_textures)
+    if (e.device == device && e.stream == s) slot = &e;
+  if (!slot) {
+    g_textures.push_back(GatherTextureSlot{device, s});
+    slot = &g_textures.back();
+  }
+  if (slot->array && (slot->W != W || slot->H != H || slot->bits != bits)) {
+    // earlier launches on this stream may still read the old texture
+    const cudaError_t err = cudaStreamSynchronize(s);
+    if (err != cudaSuccess) return err;
+    cudaDestroyTextureObject(slot->tex);
+    cudaFreeArray(slot->array);
+    slot->array = nullptr;
+    slot->tex = 0;
+  }
+  if (!slot->array) {
+    const cudaChannelFormatDesc desc = bits == 32 ? cudaCreateChannelDesc<float>()
+                                                  : cudaCreateChannelDesc<unsigned short>();
+    cudaError_t err = cudaMallocArray(&slot->array, &desc, size_t(W), size_t(H), cudaArrayTextureGather);
+    if (err != cudaSuccess) {
+      slot->array = nullptr;
+      return err;
+    }
+    cudaResourceDesc res{};
+    res.resType = cudaResourceTypeArray;
+    res.res.array.array = slot->array;
+    cudaTextureDesc td{};
+    td.addressMode[0] = td.addressMode[1] = cudaAddressModeClamp;
+    td.filterMode = cudaFilterModePoint;
+    td.readMode = cudaReadModeElementType;
+    td.normalizedCoords = 0;
+    err = cudaCreateTextureObject(&slot->tex, &res, &td, nullptr);
+    if (err != cudaSuccess) {
+      cudaFreeArray(slot->array);
+      slot->array = nullptr;
+      slot->tex = 0;
+      return err;
+    }
+    slot->W = W;
+    slot->H = H;
+    slot->bits = bits;
+  }
+  array = slot->array;
+  tex = slot->tex;
+  return cudaSuccess;
 }
 
 int* acquire_counter(int device, cudaStream_t s, cudaError_t& err) {

@@ -11,6 +11,7 @@
 // inside the box, so int(q) >= 0.  Built per forward call by one pass over the
 // volume (V x 16 bytes written for BF16/FP16, V x 32 for FP32).
 #pragma once
+#include <type_traits>
 #include "dvr_fast.cuh"
 
 namespace dvr {
@@ -102,6 +103,111 @@ __global__ void build_cells_kernel(const RenderParams p, int bv, CellWords<VT>* 
                          raw16(c[4]) | (unsigned(raw16(c[5])) << 16), raw16(c[6]) | (unsigned(raw16(c[7])) << 16));
     }
     cells[i] = out;
+  }
+}
+
+
+// Gather texture: the volume's x slabs (Y x Z voxels of every volume batch
+// entry) tiled into one 2D CUDA array created with the gather flag, each slab
+// inside a one-texel apron that repeats its edge voxels.  Slab s sits at tile
+// column s & (2^tshift - 1), tile row s >> tshift; voxel (y, z) of a slab at
+// texel (1 + z, 1 + y) of its tile.  tex2Dgather returns the four texels of a
+// 2x2 footprint, so a trilinear sample reads its eight corners with two
+// texture instructions, one per slab, and no per-corner address arithmetic.
+// With the slab index clamped to [0, X-1] and the footprint start clamped to
+// [-1, size-1] (the apron), the texels read are exactly the clamped corners of
+// VolumeFast::corners for every cell index (renderer/renderer_interpolation.cuh:193-207).
+// Texture fetches clamp their coordinates to the array, so no index reads
+// outside it.  Raw storage bits are kept: BF16 and FP16 as 16-bit unsigned
+// texels, FP32 as 32-bit float texels.
+struct TexGather {
+  cudaTextureObject_t tex;
+  int tshift;  // tiles per texture row = 2^tshift
+  int tw, th;  // tile size in texels: Z + 2, Y + 2
+};
+
+template <typename VT>
+__device__ __forceinline__ float texel_value(unsigned short raw);
+template <>
+__device__ __forceinline__ float texel_value<__nv_bfloat16>(unsigned short raw) {
+  return __uint_as_float(unsigned(raw) << 16);
+}
+template <>
+__device__ __forceinline__ float texel_value<__half>(unsigned short raw) {
+  return __half2float(__ushort_as_half(raw));
+}
+
+// The four corners (y, z) of one slab in the corner order of
+// VolumeFast::corners: (ly lz), (ly hz), (hy lz), (hy hz).  tex2Dgather
+// returns the footprint counter-clockwise from the texel at (u0, v1):
+// x = (u0, v1), y = (u1, v1), z = (u1, v0), w = (u0, v0).
+template <typename VT>
+__device__ __forceinline__ void gather_slab(cudaTextureObject_t tex, float u, float v, float* d) {
+  if constexpr (sizeof(VT) == 4) {
+    const float4 g = tex2Dgather<float4>(tex, u, v, 0);
+    d[0] = g.w; d[1] = g.z; d[2] = g.x; d[3] = g.y;
+  } else {
+    const ushort4 g = tex2Dgather<ushort4>(tex, u, v, 0);
+    d[0] = texel_value<VT>(g.w); d[1] = texel_value<VT>(g.z);
+    d[2] = texel_value<VT>(g.x); d[3] = texel_value<VT>(g.y);
+  }
+}
+
+// The gather texture seen from one volume batch entry.
+template <typename VT>
+struct TexVolume {
+  TexGather g;
+  int s0;  // slab of x = 0 of this batch entry
+  int X1, Y1, Z1;
+  // Texture coordinate of the footprint whose first texel is (tile origin +
+  // (cz2 - 1, cy2 - 1)): the texel corner between the four, exact in FP32
+  // (integers below 2^23 converted with the 2^23 bias).
+  __device__ __forceinline__ float2 coord(int x, int cz2, int cy2) const {
+    const int s = s0 + x;
+    const int iu = (s & ((1 << g.tshift) - 1)) * g.tw + cz2;
+    const int iv = (s >> g.tshift) * g.th + cy2;
+    return __fadd2_rn(make_float2(__int_as_float(iu + 0x4B000000), __int_as_float(iv + 0x4B000000)),
+                      make_float2(-8388608.f, -8388608.f));
+  }
+  __device__ __forceinline__ void corners(int ix, int iy, int iz, float* d) const {
+    const int lx = min(max(ix, 0), X1), hx = min(max(ix + 1, 0), X1);
+    // footprint start in [-1, size-1]: texel 1 + start and the next one
+    const int cy2 = min(max(iy, -1), Y1) + 2, cz2 = min(max(iz, -1), Z1) + 2;
+    const float2 a = coord(lx, cz2, cy2), b = coord(hx, cz2, cy2);
+    gather_slab<VT>(g.tex, a.x, a.y, d);
+    gather_slab<VT>(g.tex, b.x, b.y, d + 4);
+  }
+  __device__ __forceinline__ float sample(float3 q) const {
+    const int ix = int(q.x), iy = int(q.y), iz = int(q.z);
+    float d[8];
+    corners(ix, iy, iz, d);
+    return trilerp(d, q.x - float(ix), q.y - float(iy), q.z - float(iz));
+  }
+};
+
+// Writes the tiled, aproned slab image (W x H texels, row-major, pitch W)
+// that is then copied into the gather texture's array: one thread per texel;
+// texels of tiles past the last slab are zero.
+template <typename VT>
+__global__ void build_gather_image_kernel(const RenderParams p, int bv, int tshift, int W, int H,
+                                          typename std::conditional<sizeof(VT) == 4, float, unsigned short>::type* out) {
+  const int X = p.X, Y = p.Y, Z = p.Z, tw = Z + 2, th = Y + 2;
+  const int64_t slabs = int64_t(X) * bv;
+  const int64_t n = int64_t(W) * H;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    const int v = int(i / W), u = int(i - int64_t(v) * W);
+    const int tc = u / tw, tr = v / th;
+    const int64_t s = (int64_t(tr) << tshift) + tc;
+    typename std::conditional<sizeof(VT) == 4, float, unsigned short>::type val = 0;
+    if (s < slabs) {
+      const int b = int(s / X), x = int(s - int64_t(b) * X);
+      const int z = min(max(u - tc * tw - 1, 0), Z - 1), y = min(max(v - tr * th - 1, 0), Y - 1);
+      const VT e = static_cast<const VT*>(p.volume.p)[b * p.volume.s[0] + x * p.volume.s[1] + y * p.volume.s[2] +
+                                                      z * p.volume.s[3]];
+      if constexpr (sizeof(VT) == 4) val = e;
+      else val = raw16(e);
+    }
+    out[i] = val;
   }
 }
 

@@ -94,6 +94,44 @@ static int persistent_grid(K kernel, size_t smem, int64_t rays, const LaunchInfo
   return int(need < cap ? (need > 0 ? need : 1) : cap);
 }
 
+// Builds the slab gather texture of the volume (TexGather): the tiled,
+// aproned slab image is written to scratch and copied into the texture's
+// array.  cudaErrorNotSupported when the slabs exceed the gather texture's
+// size limits (the caller then reads the volume directly).
+template <typename VT>
+static cudaError_t build_gather_texture(const RenderParams& p, int bv, const LaunchInfo& li, cudaStream_t s,
+                                        TexGather& tg) {
+  int max_w = 0, max_h = 0;
+  cudaError_t err = cudaDeviceGetAttribute(&max_w, cudaDevAttrMaxTexture2DGatherWidth, li.device);
+  if (err != cudaSuccess) return err;
+  err = cudaDeviceGetAttribute(&max_h, cudaDevAttrMaxTexture2DGatherHeight, li.device);
+  if (err != cudaSuccess) return err;
+  const int64_t slabs = int64_t(p.X) * bv, tw = p.Z + 2, th = p.Y + 2;
+  int shift = 0;
+  while (shift < 16 && ((slabs + (int64_t(1) << shift) - 1) >> shift) * th > max_h) ++shift;
+  const int64_t per_row = std::min<int64_t>(int64_t(1) << shift, slabs);
+  const int64_t W = per_row * tw, H = ((slabs + (int64_t(1) << shift) - 1) >> shift) * th;
+  if (W > max_w || H > max_h) return cudaErrorNotSupported;
+  constexpr int bytes = sizeof(VT) == 4 ? 4 : 2;
+  cudaArray_t array = nullptr;
+  err = acquire_gather_texture(li.device, s, int(W), int(H), bytes * 8, array, tg.tex);
+  if (err != cudaSuccess) return err;
+  using Texel = typename std::conditional<sizeof(VT) == 4, float, unsigned short>::type;
+  auto* image = static_cast<Texel*>(acquire_scratch(li.device, s, size_t(W) * H * bytes, err, 1));
+  if (!image) return err;
+  const int blocks = int(std::min<int64_t>((W * H + 255) / 256, int64_t(li.num_sms) * 16));
+  build_gather_image_kernel<VT><<<blocks, 256, 0, s>>>(p, bv, shift, int(W), int(H), image);
+  err = cudaGetLastError();
+  if (err != cudaSuccess) return err;
+  err = cudaMemcpy2DToArrayAsync(array, 0, 0, image, size_t(W) * bytes, size_t(W) * bytes, size_t(H),
+                                 cudaMemcpyDeviceToDevice, s);
+  if (err != cudaSuccess) return err;
+  tg.tshift = shift;
+  tg.tw = int(tw);
+  tg.th = int(th);
+  return cudaSuccess;
+}
+
 template <int TF, typename VT>
 cudaError_t launch_fast_forward_vt(const RenderParams& p, int filter, int blend, const LaunchInfo& li,
                                    cudaStream_t s) {
@@ -110,19 +148,29 @@ cudaError_t launch_fast_forward_vt(const RenderParams& p, int filter, int blend,
   if (!order_ints) return err;
   err = order_rays_by_work(p, nullptr, order_ints, li, s);
   if (err != cudaSuccess) return err;
-  // trilinear filtering reads the cell-corner volume, built here, when the
-  // cells fit in L2 with room to spare (64 MB of its 129 MB) or the volume
-  // itself is too large for L2 (one 16-byte sector per sample then replaces
-  // about four); in between (a volume that stays L2-resident, cells that
-  // would not) the corners are gathered directly.  Measured: 128^3 forward
-  // 2.38 -> 1.84 ms, 512^3 10.1 -> 9.4 ms; 256^3 BF16 0.84 ms direct, 0.96
-  // with cells.
+  // Trilinear corners (DvrForwardGather).  AUTO: the cell-corner volume when
+  // the cells fit in L2 with room to spare (64 MB of its 129 MB) or the
+  // volume itself is too large for L2 (one 16-byte sector per sample then
+  // replaces about four); in between (a volume that stays L2-resident, cells
+  // that would not) the corners are gathered directly.  Measured: 128^3
+  // forward 2.38 -> 1.84 ms, 512^3 10.1 -> 9.4 ms; 256^3 BF16 0.84 ms direct,
+  // 0.96 with cells.
   const CellWords<VT>* cells = nullptr;
+  TexGather tg{};
+  int gather = kGatherDirect;
   if (filter != kNearest) {
+    const int mode = forward_gather_mode();
     const int bv = p.volume.s[0] != 0 ? p.B : 1;
     const size_t n = size_t(p.X) * p.Y * p.Z * bv;
     const size_t cell_bytes = n * sizeof(CellWords<VT>), raw_bytes = n * sizeof(VT);
-    if (cell_bytes <= (size_t(64) << 20) || (raw_bytes > (size_t(64) << 20) && cell_bytes <= (size_t(8) << 30))) {
+    if (mode == DVR_GATHER_TEXTURE) {
+      err = build_gather_texture<VT>(p, bv, li, s, tg);
+      if (err == cudaSuccess) gather = kGatherTexture;
+      else if (err != cudaErrorNotSupported) return err;
+    }
+    const bool cells_auto =
+        cell_bytes <= (size_t(64) << 20) || (raw_bytes > (size_t(64) << 20) && cell_bytes <= (size_t(8) << 30));
+    if (gather == kGatherDirect && (mode == DVR_GATHER_CELLS || (mode != DVR_GATHER_DIRECT && cells_auto))) {
       auto* c = static_cast<CellWords<VT>*>(acquire_scratch(li.device, s, cell_bytes, err, 1));
       if (!c) return err;
       const int blocks = int(std::min<size_t>((n + 255) / 256, size_t(li.num_sms) * 16));
@@ -130,6 +178,7 @@ cudaError_t launch_fast_forward_vt(const RenderParams& p, int filter, int blend,
       err = cudaGetLastError();
       if (err != cudaSuccess) return err;
       cells = c;
+      gather = kGatherCells;
     }
   }
   auto go = [&](auto kernel) {
@@ -137,17 +186,20 @@ cudaError_t launch_fast_forward_vt(const RenderParams& p, int filter, int blend,
     if (e != cudaSuccess) return e;
     // one warp per ray: as many warps as fit, up to one per ray
     kernel<<<persistent_grid(kernel, smem, order.total() * 32, li), kFastThreads, smem, s>>>(
-        p, order, counter, order_ints + work_order_list_offset, order_ints + work_order_count_offset, cells);
+        p, order, counter, order_ints + work_order_list_offset, order_ints + work_order_count_offset, cells, tg);
     return cudaGetLastError();
   };
   if (filter == kNearest)
-    return blend == kBeerLambert ? go(fast_forward_warp_kernel<kNearest, TF, kBeerLambert, VT, false>)
-                                 : go(fast_forward_warp_kernel<kNearest, TF, kAlphaBlend, VT, false>);
-  if (cells)
-    return blend == kBeerLambert ? go(fast_forward_warp_kernel<kTrilinear, TF, kBeerLambert, VT, true>)
-                                 : go(fast_forward_warp_kernel<kTrilinear, TF, kAlphaBlend, VT, true>);
-  return blend == kBeerLambert ? go(fast_forward_warp_kernel<kTrilinear, TF, kBeerLambert, VT, false>)
-                               : go(fast_forward_warp_kernel<kTrilinear, TF, kAlphaBlend, VT, false>);
+    return blend == kBeerLambert ? go(fast_forward_warp_kernel<kNearest, TF, kBeerLambert, VT, kGatherDirect>)
+                                 : go(fast_forward_warp_kernel<kNearest, TF, kAlphaBlend, VT, kGatherDirect>);
+  if (gather == kGatherCells)
+    return blend == kBeerLambert ? go(fast_forward_warp_kernel<kTrilinear, TF, kBeerLambert, VT, kGatherCells>)
+                                 : go(fast_forward_warp_kernel<kTrilinear, TF, kAlphaBlend, VT, kGatherCells>);
+  if (gather == kGatherTexture)
+    return blend == kBeerLambert ? go(fast_forward_warp_kernel<kTrilinear, TF, kBeerLambert, VT, kGatherTexture>)
+                                 : go(fast_forward_warp_kernel<kTrilinear, TF, kAlphaBlend, VT, kGatherTexture>);
+  return blend == kBeerLambert ? go(fast_forward_warp_kernel<kTrilinear, TF, kBeerLambert, VT, kGatherDirect>)
+                               : go(fast_forward_warp_kernel<kTrilinear, TF, kAlphaBlend, VT, kGatherDirect>);
 }
 
 // TF-gradient-only adjoint of a texture TF from the sample-density record:

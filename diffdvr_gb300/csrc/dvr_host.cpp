@@ -30,6 +30,7 @@ namespace {
 thread_local std::string g_last_error;
 std::atomic<int> g_family{DVR_KERNELS_OPTIMIZED};
 std::atomic<int> g_window{0};
+std::atomic<int> g_gather{DVR_GATHER_AUTO};
 thread_local int g_adjoint_path = DVR_PATH_NONE;
 std::atomic<int> g_sync{0};
 
@@ -664,6 +665,7 @@ cudaError_t dispatch_forward_gradients(const Checked& c, const FwdGradParams& g,
 
 int& last_adjoint_path() { return g_adjoint_path; }
 bool window_adjoint_on() { return g_window.load() != 0; }
+int forward_gather_mode() { return g_gather.load(); }
 
 int render_adjoint_into(const DvrRendererInputs* inputs, const DvrRendererOutputs* outputs_from_forward,
                         const DvrTensor* adj_color, const DvrAdjointOutputs* adj_outputs, void* cuda_stream,
@@ -1110,4 +1112,9 @@ extern "C" int dvr_get_sync_mode(void) { return g_sync.load(); }
 extern "C" int dvr_abi_version(void) { return DVR_ABI_VERSION; }
 extern "C" int dvr_set_window_adjoint(int32_t enable) { return g_window.exchange(enable ? 1 : 0); }
 extern "C" int dvr_get_window_adjoint(void) { return g_window.load(); }
+extern "C" int dvr_set_forward_gather(int32_t mode) {
+  if (mode < DVR_GATHER_AUTO || mode > DVR_GATHER_TEXTURE) return DVR_E_INVALID_ARGUMENT;
+  return g_gather.exchange(mode);
+}
+extern "C" int dvr_get_forward_gather(void) { return g_gather.load(); }
 extern "C" int dvr_last_adjoint_path(void) { return g_adjoint_path; }

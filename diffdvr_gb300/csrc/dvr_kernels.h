@@ -16,6 +16,8 @@ constexpr int kMaxViewportBatch = 256;
 // and the window-adjoint switch (dvr_set_window_adjoint).
 int& last_adjoint_path();
 bool window_adjoint_on();
+// The forward's corner-gather mode (DvrForwardGather, dvr_set_forward_gather).
+int forward_gather_mode();
 
 struct LaunchInfo {
   int num_sms;
@@ -34,6 +36,14 @@ int* acquire_counter(int device, cudaStream_t s, cudaError_t& err);
 // growing synchronises the stream).  Not zeroed.  Slots are independent
 // buffers (0: ray order and TF-gradient slices, 1: cell-corner volume).
 void* acquire_scratch(int device, cudaStream_t s, size_t bytes, cudaError_t& err, int slot = 0);
+
+// A 2D CUDA array of W x H texels (bits = 16: unsigned 16-bit, 32: float)
+// created with the gather flag, and its texture object (point filtering,
+// clamped unnormalised coordinates, element reads), owned by the library and
+// reused by later launches on stream s while the size stays the same
+// (replacing it synchronises the stream).
+cudaError_t acquire_gather_texture(int device, cudaStream_t s, int W, int H, int bits, cudaArray_t& array,
+                                   cudaTextureObject_t& tex);
 
 // Scratch handed in by the caller instead of the library's pools: `counter`
 // (one int, zeroed here on the stream before each launch) and `tf` (TF-gradient

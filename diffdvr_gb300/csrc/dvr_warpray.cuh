@@ -37,14 +37,19 @@ __device__ __forceinline__ float sample_density(const VolumeFast<VT>& v, float3 
 // opacity a, then b: a + (1 - a) b
 __device__ __forceinline__ float over(float a, float b) { return a + (1.f - a) * b; }
 
+// How a trilinear sample reads its eight corners.
+enum { kGatherDirect = 0, kGatherCells = 1, kGatherTexture = 2 };
+
 // ray_list[0 .. *ray_count): the rays with samples (longest first); the
-// ordering pass has already finished the others.  CELLS: trilinear samples
-// read the cell-corner volume `cells`, else they gather the corners directly.
-template <int FILTER, int TF, int BLEND, typename VT, bool CELLS>
+// ordering pass has already finished the others.  GATHER: trilinear samples
+// load the corners directly from the volume, read the cell-corner volume
+// `cells`, or gather them from the slab texture `tg`.
+template <int FILTER, int TF, int BLEND, typename VT, int GATHER>
 __global__ void __launch_bounds__(kFastThreads) fast_forward_warp_kernel(const RenderParams p, const RayOrder order,
                                                                          int* counter, const int* ray_list,
                                                                          const int* ray_count,
-                                                                         const CellWords<VT>* cells) {
+                                                                         const CellWords<VT>* cells,
+                                                                         const TexGather tg) {
   extern __shared__ float4 fast_smem4[];
   constexpr int C = TfChannels<TF>::C;
   float* s_tf = reinterpret_cast<float*>(fast_smem4);
@@ -86,6 +91,7 @@ __global__ void __launch_bounds__(kFastThreads) fast_forward_warp_kernel(const R
                              int(p.volume.s[2]), int(p.volume.s[3]), p.X - 1, p.Y - 1, p.Z - 1};
     const size_t vb = p.volume.s[0] != 0 ? size_t(b) * p.X * p.Y * p.Z : 0;
     const CellVolume<VT> cv{cells ? cells + vb : nullptr, p.X - 1, p.Y - 1, p.Z - 1};
+    const TexVolume<VT> tv{tg, p.volume.s[0] != 0 ? b * p.X : 0, p.X - 1, p.Y - 1, p.Z - 1};
     const TfShared<C> tf{s_tf + (copies > 1 ? b : 0) * p.R * C, p.R};
     // a recorded ray carries its opacities in the record: no checkpoints
     float* ck = p.ckpt.p && !rec
@@ -102,7 +108,8 @@ __global__ void __launch_bounds__(kFastThreads) fast_forward_warp_kernel(const R
       float density = 0.f, a = 0.f;
       f4 c = mk4(0, 0, 0, 0);
       if (in_ray) {
-        if constexpr (CELLS) density = cv.sample(fast_pos(q, t));
+        if constexpr (GATHER == kGatherCells) density = cv.sample(fast_pos(q, t));
+        else if constexpr (GATHER == kGatherTexture) density = tv.sample(fast_pos(q, t));
         else density = sample_density<FILTER, VT>(vol, fast_pos(q, t));
         c = tf_eval<TF>(tf, density);
         a = blend_alpha<BLEND>(c.w, q.step);

@@ -535,6 +535,17 @@ def set_window_adjoint(enable: bool) -> bool:
     return bool(_abi.load().dvr_set_window_adjoint(int(bool(enable))))
 
 
+def set_forward_gather(mode: str) -> str:
+    """How the forward reads a trilinear sample's eight corners: "auto"
+    (default), "direct" (eight loads), "cells" (one cell record per sample)
+    or "texture" (two gathers from the slab texture); returns the previous
+    mode."""
+    if mode not in _abi.FORWARD_GATHERS:
+        raise RuntimeError(f"unknown forward gather mode {mode!r}")
+    prev = _abi.load().dvr_set_forward_gather(_abi.FORWARD_GATHERS[mode])
+    return {v: k for k, v in _abi.FORWARD_GATHERS.items()}[prev]
+
+
 def last_adjoint_path() -> str:
     """The kernels the last render_adjoint call on this thread ran: "plain",
     "general", "record", "window", "preshaded" or "none"."""

@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define DVR_ABI_VERSION 5
+#define DVR_ABI_VERSION 6
 
 /* ---- status codes ---- */
 #define DVR_OK 0
@@ -324,6 +324,21 @@ int dvr_get_kernel_family(void);
  * counterpart in the reference. */
 int dvr_set_window_adjoint(int32_t enable);
 int dvr_get_window_adjoint(void);
+
+/* How the optimized single-instance forward reads the eight corners of a
+ * trilinear sample (DvrForwardGather).  Process-wide.  Returns the previous
+ * value, or DVR_E_INVALID_ARGUMENT for an unknown mode.  No counterpart in the
+ * reference (its kernels load the corners directly). */
+enum DvrForwardGather {
+  DVR_GATHER_AUTO = 0,    /* the mode measured fastest for the volume's size */
+  DVR_GATHER_DIRECT = 1,  /* eight loads from the volume */
+  DVR_GATHER_CELLS = 2,   /* one 16-byte cell record per sample, built per call */
+  DVR_GATHER_TEXTURE = 3  /* two tex2Dgather fetches per sample from the slab
+                             texture, built per call; AUTO/DIRECT where the
+                             slabs do not fit the texture's size limits */
+};
+int dvr_set_forward_gather(int32_t mode);
+int dvr_get_forward_gather(void);
 
 /* Which kernels the last dvr_render_adjoint call on the calling thread ran
  * (DvrAdjointPath).  No counterpart in the reference. */

@@ -26,7 +26,7 @@ def test_library_exports_every_header_symbol(dvr_lib):
     for n in names:
         assert hasattr(dvr_lib, n), n
     assert set(names) == set(_abi.SIGNATURES)
-    assert dvr_lib.dvr_abi_version() == 5
+    assert dvr_lib.dvr_abi_version() == 6
 
 
 def _fake(shape, dtype=_abi.DVR_FLOAT32, cuda=True, ptr=0x100000):
@@ -422,7 +422,7 @@ int main(void) {
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     r = subprocess.run([str(exe)], capture_output=True, text=True)
-    assert r.returncode == 0 and r.stdout.strip() == "ok 5", (r.returncode, r.stdout, r.stderr)
+    assert r.returncode == 0 and r.stdout.strip() == "ok 6", (r.returncode, r.stdout, r.stderr)
 
 
 def test_missing_library_fails_loudly(monkeypatch, tmp_path):

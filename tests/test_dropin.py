@@ -135,3 +135,73 @@ def test_reference_module_matches_ours_on_the_gpu(reference_module, dvr_lib, cud
             continue
         assert np.isfinite(x).all() and np.abs(x).max() > 0, name
         assert rel_l2(y, x) <= 1e-3, (name, rel_l2(y, x))
+
+
+def _pure_calls(vol, tf, vp, fov, weights, optimize_camera):
+    """The reference module's forward + backward written out as plain
+    pyrenderer calls (renderer.py:264-359 of the reference's pytests): plain
+    outputs (colour and termination index only, so the adjoint inverts the
+    blend), per-pixel rays from Camera.generate_rays when the camera is
+    optimized, their gradients chained to the viewport by torch."""
+    from diffdvr_gb300 import pyrenderer as pr
+    from diffdvr_gb300.camera import Camera
+    B, H, W = weights.shape[:3]
+    v = torch.from_numpy(vol).cuda()
+    t = torch.from_numpy(tf).cuda()
+    c = torch.from_numpy(vp).cuda().requires_grad_(optimize_camera)
+    inputs = _settings(pr)
+    inputs.volume, inputs.tf = v, t
+    if optimize_camera:
+        rs, rd = Camera.generate_rays(c, fov, W, H)
+        inputs.camera_mode = pr.CameraMode.RayStartDir
+        inputs.camera = pr.CameraPerPixelRays(rs.detach().contiguous(), rd.detach().contiguous())
+    else:
+        inputs.camera_mode = pr.CameraMode.ReferenceFrame
+        inputs.camera = pr.CameraReferenceFrame(c.detach(), fov)
+    out = pr.RendererOutputs(torch.empty(B, H, W, 4, device="cuda"),
+                             torch.empty(B, H, W, device="cuda", dtype=torch.int32))
+    pr.Renderer.render_forward(inputs, out)
+    adj = pr.AdjointOutputs()
+    adj.has_volume_derivatives, adj.adj_volume = True, torch.zeros_like(v)
+    adj.has_tf_derivatives, adj.adj_tf = True, torch.zeros_like(t)
+    if optimize_camera:
+        adj.has_camera_derivatives = True
+        adj.adj_camera_ray_start = torch.zeros_like(inputs.camera.ray_start)
+        adj.adj_camera_ray_dir = torch.zeros_like(inputs.camera.ray_dir)
+    pr.Renderer.render_adjoint(inputs, out, weights.contiguous(), adj)
+    cam = None
+    if optimize_camera:
+        torch.autograd.backward([rs, rd], [adj.adj_camera_ray_start, adj.adj_camera_ray_dir])
+        cam = c.grad.double().cpu().numpy()
+    torch.cuda.synchronize()
+    return (out.color.double().cpu().numpy(), adj.adj_volume.double().cpu().numpy(),
+            adj.adj_tf.double().cpu().numpy(), cam)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("optimize_camera", [False, True], ids=["tf+volume", "tf+volume+camera"])
+def test_module_matches_pure_pyrenderer_calls_on_the_gpu(dvr_lib, cuda_device, optimize_camera):
+    """Without the reference checkout (it does not travel to GPU hosts): the
+    autograd module against the same step written as pyrenderer calls, with
+    the gates of the reference-module test above."""
+    import diffdvr_gb300
+    from diffdvr_gb300 import pyrenderer as pr
+    from dvr_cases import rel_l2, symmetric_error
+    vol, tf, vp = _scene()
+    fov = float(np.float32(0.7))
+    prev = pr.set_kernel_family("optimized")
+    try:
+        weights = torch.from_numpy(np.random.default_rng(9).normal(size=(2, 20, 24, 4)).astype(np.float32)).cuda()
+        ours = diffdvr_gb300.Renderer(_settings(pr), optimize_camera=optimize_camera, optimize_tf=True,
+                                      optimize_volume=True)
+        a = _pure_calls(vol, tf, vp, fov, weights, optimize_camera)
+        b = _loss_and_grads(ours, vol, tf, vp, fov, weights)
+    finally:
+        pr.set_kernel_family(prev)
+    assert symmetric_error(a[0], b[0]) <= 1e-5
+    assert a[0][..., 3].max() > 0.05  # the scene is not empty
+    for name, x, y in zip(("volume", "tf", "camera"), a[1:], b[1:]):
+        if x is None:
+            continue
+        assert np.isfinite(x).all() and np.abs(x).max() > 0, name
+        assert rel_l2(y, x) <= 1e-3, (name, rel_l2(y, x))
