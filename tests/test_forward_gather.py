@@ -24,7 +24,9 @@ def _render(case, mode, dtype, record=None):
     from diffdvr_gb300 import pyrenderer as pr
     prev = pr.set_forward_gather(mode)
     try:
-        _, out = gpu_forward(case, "optimized", volume_dtype=dtype, checkpoints=record is None, record=record)
+        # a sample record needs the checkpoint buffer beside it (rays that
+        # find the pool full checkpoint instead)
+        _, out = gpu_forward(case, "optimized", volume_dtype=dtype, checkpoints=True, record=record)
     finally:
         pr.set_forward_gather(prev)
     res = {"color": out.color, "term": out.terminationIndex}
