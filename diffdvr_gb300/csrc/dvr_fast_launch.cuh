@@ -149,12 +149,13 @@ cudaError_t launch_fast_forward_vt(const RenderParams& p, int filter, int blend,
   err = order_rays_by_work(p, nullptr, order_ints, li, s);
   if (err != cudaSuccess) return err;
   // Trilinear corners (DvrForwardGather).  AUTO: the cell-corner volume when
-  // the cells fit in L2 with room to spare (64 MB of its 129 MB) or the
-  // volume itself is too large for L2 (one 16-byte sector per sample then
-  // replaces about four); in between (a volume that stays L2-resident, cells
-  // that would not) the corners are gathered directly.  Measured: 128^3
-  // forward 2.38 -> 1.84 ms, 512^3 10.1 -> 9.4 ms; 256^3 BF16 0.84 ms direct,
-  // 0.96 with cells.
+  // the cells fit in L2 with room to spare (64 MB of its 129 MB); else the
+  // slab gather texture; where the slabs exceed the texture's size limits,
+  // the cell-corner volume when the volume itself is too large for L2 (one
+  // 16-byte sector per sample then replaces about four), else direct loads.
+  // Measured forward (GB300, BF16): 128^3 cells 1.85 ms, texture 1.92 (64
+  // views of 256^2); 256^3 texture 0.75 ms, direct 0.80, cells 0.82 (8 views
+  // of 256^2); 512^3 texture 25.1 ms, cells 27.8 (16 views of 1024^2).
   const CellWords<VT>* cells = nullptr;
   TexGather tg{};
   int gather = kGatherDirect;
@@ -163,13 +164,14 @@ cudaError_t launch_fast_forward_vt(const RenderParams& p, int filter, int blend,
     const int bv = p.volume.s[0] != 0 ? p.B : 1;
     const size_t n = size_t(p.X) * p.Y * p.Z * bv;
     const size_t cell_bytes = n * sizeof(CellWords<VT>), raw_bytes = n * sizeof(VT);
-    if (mode == DVR_GATHER_TEXTURE) {
+    const bool cells_in_l2 = cell_bytes <= (size_t(64) << 20);
+    if (mode == DVR_GATHER_TEXTURE || (mode == DVR_GATHER_AUTO && !cells_in_l2)) {
       err = build_gather_texture<VT>(p, bv, li, s, tg);
       if (err == cudaSuccess) gather = kGatherTexture;
       else if (err != cudaErrorNotSupported) return err;
     }
     const bool cells_auto =
-        cell_bytes <= (size_t(64) << 20) || (raw_bytes > (size_t(64) << 20) && cell_bytes <= (size_t(8) << 30));
+        cells_in_l2 || (raw_bytes > (size_t(64) << 20) && cell_bytes <= (size_t(8) << 30));
     if (gather == kGatherDirect && (mode == DVR_GATHER_CELLS || (mode != DVR_GATHER_DIRECT && cells_auto))) {
       auto* c = static_cast<CellWords<VT>*>(acquire_scratch(li.device, s, cell_bytes, err, 1));
       if (!c) return err;

@@ -330,7 +330,9 @@ int dvr_get_window_adjoint(void);
  * value, or DVR_E_INVALID_ARGUMENT for an unknown mode.  No counterpart in the
  * reference (its kernels load the corners directly). */
 enum DvrForwardGather {
-  DVR_GATHER_AUTO = 0,    /* the mode measured fastest for the volume's size */
+  DVR_GATHER_AUTO = 0,    /* the mode measured fastest for the volume's size:
+                             CELLS when the cell records fit in 64 MB, else
+                             TEXTURE (CELLS or DIRECT beyond its limits) */
   DVR_GATHER_DIRECT = 1,  /* eight loads from the volume */
   DVR_GATHER_CELLS = 2,   /* one 16-byte cell record per sample, built per call */
   DVR_GATHER_TEXTURE = 3  /* two tex2Dgather fetches per sample from the slab
