@@ -76,33 +76,41 @@ __device__ __forceinline__ unsigned short raw16(T v) {
   return *reinterpret_cast<const unsigned short*>(&v);
 }
 
-// One thread per cell of every volume batch entry.
+// One warp per (batch entry, x, y) row of cells, lanes along z: the row's
+// index arithmetic is done once per warp, and the corner loads and the cell
+// stores of a warp are contiguous in z.
 template <typename VT>
 __global__ void build_cells_kernel(const RenderParams p, int bv, CellWords<VT>* cells) {
   const int X = p.X, Y = p.Y, Z = p.Z;
-  const size_t V = size_t(X) * Y * Z;
-  const size_t n = V * bv;
-  for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) {
-    const int b = int(i / V);
-    size_t r = i - size_t(b) * V;
-    const int z = int(r % Z);
-    r /= Z;
-    const int y = int(r % Y), x = int(r / Y);
+  const int lane = threadIdx.x & 31;
+  const int64_t rows = int64_t(bv) * X * Y;
+  const int64_t warps = int64_t(gridDim.x) * (blockDim.x >> 5);
+  const int64_t sx = p.volume.s[1], sy = p.volume.s[2], sz = p.volume.s[3];
+  for (int64_t row = blockIdx.x * int64_t(blockDim.x >> 5) + (threadIdx.x >> 5); row < rows; row += warps) {
+    const int64_t bx = row / Y;
+    const int y = int(row - bx * Y);
+    const int b = int(bx / X), x = int(bx - int64_t(b) * X);
     const VT* v = static_cast<const VT*>(p.volume.p) + b * p.volume.s[0];
-    const int64_t sx = p.volume.s[1], sy = p.volume.s[2], sz = p.volume.s[3];
-    const int hx = min(x + 1, X - 1), hy = min(y + 1, Y - 1), hz = min(z + 1, Z - 1);
-    const VT c[8] = {v[x * sx + y * sy + z * sz],   v[x * sx + y * sy + hz * sz],  v[x * sx + hy * sy + z * sz],
-                     v[x * sx + hy * sy + hz * sz], v[hx * sx + y * sy + z * sz],  v[hx * sx + y * sy + hz * sz],
-                     v[hx * sx + hy * sy + z * sz], v[hx * sx + hy * sy + hz * sz]};
-    CellWords<VT> out;
-    if constexpr (sizeof(VT) == 4) {
-      out.lo = make_float4(c[0], c[1], c[2], c[3]);
-      out.hi = make_float4(c[4], c[5], c[6], c[7]);
-    } else {
-      out.w = make_uint4(raw16(c[0]) | (unsigned(raw16(c[1])) << 16), raw16(c[2]) | (unsigned(raw16(c[3])) << 16),
-                         raw16(c[4]) | (unsigned(raw16(c[5])) << 16), raw16(c[6]) | (unsigned(raw16(c[7])) << 16));
+    const int hx = min(x + 1, X - 1), hy = min(y + 1, Y - 1);
+    const VT* r00 = v + x * sx + y * sy;
+    const VT* r01 = v + x * sx + hy * sy;
+    const VT* r10 = v + hx * sx + y * sy;
+    const VT* r11 = v + hx * sx + hy * sy;
+    CellWords<VT>* dst = cells + row * Z;
+    for (int z = lane; z < Z; z += 32) {
+      const int hz = min(z + 1, Z - 1);
+      const VT c[8] = {r00[z * sz], r00[hz * sz], r01[z * sz], r01[hz * sz],
+                       r10[z * sz], r10[hz * sz], r11[z * sz], r11[hz * sz]};
+      CellWords<VT> out;
+      if constexpr (sizeof(VT) == 4) {
+        out.lo = make_float4(c[0], c[1], c[2], c[3]);
+        out.hi = make_float4(c[4], c[5], c[6], c[7]);
+      } else {
+        out.w = make_uint4(raw16(c[0]) | (unsigned(raw16(c[1])) << 16), raw16(c[2]) | (unsigned(raw16(c[3])) << 16),
+                           raw16(c[4]) | (unsigned(raw16(c[5])) << 16), raw16(c[6]) | (unsigned(raw16(c[7])) << 16));
+      }
+      dst[z] = out;
     }
-    cells[i] = out;
   }
 }
 
@@ -186,28 +194,36 @@ struct TexVolume {
 };
 
 // Writes the tiled, aproned slab image (W x H texels, row-major, pitch W)
-// that is then copied into the gather texture's array: one thread per texel;
-// texels of tiles past the last slab are zero.
+// that is then copied into the gather texture's array: one warp per texel row
+// of one tile (blockIdx.x = tile column, warps over texel rows), lanes along
+// z, so the row's index arithmetic is done once per warp and the volume reads
+// and image writes of a warp are contiguous.  Texels of tiles past the last
+// slab are zero.
 template <typename VT>
 __global__ void build_gather_image_kernel(const RenderParams p, int bv, int tshift, int W, int H,
                                           typename std::conditional<sizeof(VT) == 4, float, unsigned short>::type* out) {
+  using Texel = typename std::conditional<sizeof(VT) == 4, float, unsigned short>::type;
   const int X = p.X, Y = p.Y, Z = p.Z, tw = Z + 2, th = Y + 2;
+  const int lane = threadIdx.x & 31;
+  const int tc = blockIdx.x;
   const int64_t slabs = int64_t(X) * bv;
-  const int64_t n = int64_t(W) * H;
-  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
-    const int v = int(i / W), u = int(i - int64_t(v) * W);
-    const int tc = u / tw, tr = v / th;
+  for (int v = blockIdx.y * (blockDim.x >> 5) + (threadIdx.x >> 5); v < H; v += gridDim.y * (blockDim.x >> 5)) {
+    const int tr = v / th;
     const int64_t s = (int64_t(tr) << tshift) + tc;
-    typename std::conditional<sizeof(VT) == 4, float, unsigned short>::type val = 0;
-    if (s < slabs) {
-      const int b = int(s / X), x = int(s - int64_t(b) * X);
-      const int z = min(max(u - tc * tw - 1, 0), Z - 1), y = min(max(v - tr * th - 1, 0), Y - 1);
-      const VT e = static_cast<const VT*>(p.volume.p)[b * p.volume.s[0] + x * p.volume.s[1] + y * p.volume.s[2] +
-                                                      z * p.volume.s[3]];
-      if constexpr (sizeof(VT) == 4) val = e;
-      else val = raw16(e);
+    Texel* row = out + int64_t(v) * W + int64_t(tc) * tw;
+    if (s >= slabs) {
+      for (int u = lane; u < tw; u += 32) row[u] = 0;
+      continue;
     }
-    out[i] = val;
+    const int b = int(s / X), x = int(s - int64_t(b) * X);
+    const int y = min(max(v - tr * th - 1, 0), Y - 1);
+    const VT* src = static_cast<const VT*>(p.volume.p) + b * p.volume.s[0] + x * p.volume.s[1] + y * p.volume.s[2];
+    const int64_t sz = p.volume.s[3];
+    for (int u = lane; u < tw; u += 32) {
+      const VT e = src[min(max(u - 1, 0), Z - 1) * sz];
+      if constexpr (sizeof(VT) == 4) row[u] = e;
+      else row[u] = raw16(e);
+    }
   }
 }
 

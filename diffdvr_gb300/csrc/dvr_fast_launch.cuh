@@ -119,8 +119,9 @@ static cudaError_t build_gather_texture(const RenderParams& p, int bv, const Lau
   using Texel = typename std::conditional<sizeof(VT) == 4, float, unsigned short>::type;
   auto* image = static_cast<Texel*>(acquire_scratch(li.device, s, size_t(W) * H * bytes, err, 1));
   if (!image) return err;
-  const int blocks = int(std::min<int64_t>((W * H + 255) / 256, int64_t(li.num_sms) * 16));
-  build_gather_image_kernel<VT><<<blocks, 256, 0, s>>>(p, bv, shift, int(W), int(H), image);
+  // a block per tile column and 8 texel rows (one per warp)
+  const dim3 grid(unsigned(per_row), unsigned(std::min<int64_t>((H + 7) / 8, 65535)));
+  build_gather_image_kernel<VT><<<grid, 256, 0, s>>>(p, bv, shift, int(W), int(H), image);
   err = cudaGetLastError();
   if (err != cudaSuccess) return err;
   err = cudaMemcpy2DToArrayAsync(array, 0, 0, image, size_t(W) * bytes, size_t(W) * bytes, size_t(H),
@@ -175,7 +176,8 @@ cudaError_t launch_fast_forward_vt(const RenderParams& p, int filter, int blend,
     if (gather == kGatherDirect && (mode == DVR_GATHER_CELLS || (mode != DVR_GATHER_DIRECT && cells_auto))) {
       auto* c = static_cast<CellWords<VT>*>(acquire_scratch(li.device, s, cell_bytes, err, 1));
       if (!c) return err;
-      const int blocks = int(std::min<size_t>((n + 255) / 256, size_t(li.num_sms) * 16));
+      // one warp per row of Z cells, 8 rows per block
+      const int blocks = int(std::min<size_t>((n / p.Z + 7) / 8, size_t(li.num_sms) * 32));
       build_cells_kernel<VT><<<blocks, 256, 0, s>>>(p, bv, c);
       err = cudaGetLastError();
       if (err != cudaSuccess) return err;
