@@ -193,6 +193,25 @@ struct TexVolume {
   }
 };
 
+// The volume as the general adjoint reads it: trilinear corners from the
+// slab gather texture when the call built one (tex), else loaded directly;
+// single voxels (nearest filtering) always directly.  Both give the same
+// values.
+template <typename VT>
+struct AdjVolume {
+  VolumeFast<VT> v;
+  TexVolume<VT> t;
+  bool tex;
+  int X1, Y1, Z1;
+  __device__ __forceinline__ AdjVolume(const VolumeFast<VT>& v_, const TexVolume<VT>& t_, bool tex_)
+      : v(v_), t(t_), tex(tex_), X1(v_.X1), Y1(v_.Y1), Z1(v_.Z1) {}
+  __device__ __forceinline__ float at(int x, int y, int z) const { return v.at(x, y, z); }
+  __device__ __forceinline__ void corners(int ix, int iy, int iz, float* d) const {
+    if (tex) t.corners(ix, iy, iz, d);
+    else v.corners(ix, iy, iz, d);
+  }
+};
+
 // Writes the tiled, aproned slab image (W x H texels, row-major, pitch W)
 // that is then copied into the gather texture's array: one warp per texel row
 // of one tile (blockIdx.x = tile column, warps over texel rows), lanes along

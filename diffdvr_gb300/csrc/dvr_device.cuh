@@ -7,6 +7,7 @@
 // plain kernels reproduce the reference bit for bit up to the exp/rsqrt
 // instruction accuracy.
 #pragma once
+#include <type_traits>
 #include "dvr_math.cuh"
 #include "dvr_params.h"
 
@@ -229,6 +230,20 @@ __device__ __forceinline__ float trilerp_grad(const float* d, float fx, float fy
   return lerp1(lo, hi, fz);
 }
 
+// Adds adj times the trilinear weight of each corner (corner order of
+// VolumeFast::corners) to g.
+__device__ __forceinline__ void add_corner_weights(float* g, float adj, float fx, float fy, float fz) {
+  const float gx = 1 - fx, gy = 1 - fy, gz = 1 - fz;
+  g[0] += adj * (gx * gy * gz);
+  g[1] += adj * (gx * gy * fz);
+  g[2] += adj * (gx * fy * gz);
+  g[3] += adj * (gx * fy * fz);
+  g[4] += adj * (fx * gy * gz);
+  g[5] += adj * (fx * gy * fz);
+  g[6] += adj * (fx * fy * gz);
+  g[7] += adj * (fx * fy * fz);
+}
+
 // Gradient of the trilinear interpolant w.r.t. the eight corners and the
 // position, in the reference's accumulation order 000,100,010,110,001,101,011,111
 // (renderer/renderer_interpolation.cuh:360-387).  acc may be nullptr.
@@ -397,17 +412,32 @@ __device__ __forceinline__ float tf_adjoint(const A& tf, float density, f4 adj, 
     const f4 a = tf.rgba(i), c = tf.rgba(i + 1);
     const float p0 = tf.at(i, 4), p1 = tf.at(i + 1, 4);
     const float d2 = clampf(density, p0, p1);
-    const float fr = (d2 - p0) / (p1 - p0);
     const float adj_fr = dot4(adj, mk4(c.x - a.x, c.y - a.y, c.z - a.z, c.w - a.w));
-    const float den = (p1 - p0) * (p1 - p0);
-    if constexpr (WithTfGrad) {
-      const float w0 = 1 - fr;
-      sink.add4(i, mk4(adj.x * w0, adj.y * w0, adj.z * w0, adj.w * w0));
-      sink.add(i, 4, adj_fr * (d2 - p1) / den);
-      sink.add4(i + 1, mk4(adj.x * fr, adj.y * fr, adj.z * fr, adj.w * fr));
-      sink.add(i + 1, 4, adj_fr * (p0 - d2) / den);
+    if constexpr (std::is_same<A, TfShared<5>>::value) {
+      // optimized kernels: one reciprocal of the interval instead of four
+      // divisions (the results differ from the quotients by rounding only)
+      const float inv = 1.f / (p1 - p0);
+      const float fr = (d2 - p0) * inv;
+      if constexpr (WithTfGrad) {
+        const float w0 = 1 - fr, inv2 = inv * inv;
+        sink.add4(i, mk4(adj.x * w0, adj.y * w0, adj.z * w0, adj.w * w0));
+        sink.add(i, 4, adj_fr * (d2 - p1) * inv2);
+        sink.add4(i + 1, mk4(adj.x * fr, adj.y * fr, adj.z * fr, adj.w * fr));
+        sink.add(i + 1, 4, adj_fr * (p0 - d2) * inv2);
+      }
+      return adj_fr * inv;
+    } else {
+      const float fr = (d2 - p0) / (p1 - p0);
+      const float den = (p1 - p0) * (p1 - p0);
+      if constexpr (WithTfGrad) {
+        const float w0 = 1 - fr;
+        sink.add4(i, mk4(adj.x * w0, adj.y * w0, adj.z * w0, adj.w * w0));
+        sink.add(i, 4, adj_fr * (d2 - p1) / den);
+        sink.add4(i + 1, mk4(adj.x * fr, adj.y * fr, adj.z * fr, adj.w * fr));
+        sink.add(i + 1, 4, adj_fr * (p0 - d2) / den);
+      }
+      return adj_fr / (p1 - p0);
     }
-    return adj_fr / (p1 - p0);
   } else {
     float adj_density = 0;
     for (int i = 0; i < tf.R; ++i) {

@@ -130,7 +130,7 @@ __device__ __forceinline__ void stage_tf(const RenderParams& p, int b, float* s_
 struct FastRay {
   float3 p0, dp;       // volume position = p0 + t * dp
   float step, tmin, tmax;
-  f3 dir, voxel;
+  f3 dir, voxel, inv_voxel;  // inv_voxel = 1 / voxel: position derivatives scale by it
 };
 
 __device__ __forceinline__ void fast_setup(const RenderParams& p, int x, int y, int b, FastRay& fr) {
@@ -144,6 +144,7 @@ __device__ __forceinline__ void fast_setup(const RenderParams& p, int x, int y, 
   fr.tmax = r.tmax;
   fr.dir = r.dir;
   fr.voxel = r.voxel;
+  fr.inv_voxel = mk3(1.f / r.voxel.x, 1.f / r.voxel.y, 1.f / r.voxel.z);
 }
 
 __device__ __forceinline__ float3 fast_pos(const FastRay& r, float t) {
@@ -157,7 +158,9 @@ struct Sampler {
   int cx = -1, cy = -1, cz = -1;
   float d[8];
   float fx, fy, fz;
-  __device__ __forceinline__ float sample(const VolumeFast<VT>& v, float3 q) {
+  // V: VolumeFast, or any accessor with at(), corners() and X1/Y1/Z1
+  template <class V>
+  __device__ __forceinline__ float sample(const V& v, float3 q) {
     if constexpr (FILTER == kNearest) {
       const int ix = nearest_coord(q.x, v.X1 + 1), iy = nearest_coord(q.y, v.Y1 + 1), iz = nearest_coord(q.z, v.Z1 + 1);
       if (ix != cx || iy != cy || iz != cz) {
@@ -746,9 +749,9 @@ struct VolGradCell {
 
 // One reverse step shared by both adjoint variants.  Returns the step's
 // position-chain contribution to d(loss)/d(step) via adj_step.
-template <int FILTER, int TF, int BLEND, bool VOLGRAD, bool TFGRAD, typename VT, class A>
+template <int FILTER, int TF, int BLEND, bool VOLGRAD, bool TFGRAD, typename VT, class A, class V>
 __device__ __forceinline__ void fast_reverse_step(const RenderParams& p, const AdjointParams& a, const FastRay& r,
-                                                  const VolumeFast<VT>& vol, const A& tf,
+                                                  const V& vol, const A& tf,
                                                   TfGradAccum<TF, TFGRAD>& tacc, float* s_grad_warp,
                                                   Sampler<FILTER, VT>& smp, VolGradCell<FILTER, VOLGRAD>& vg,
                                                   float* adjv, int k, float density, float alpha_in, f4& adj_acc,
@@ -784,21 +787,19 @@ __device__ __forceinline__ void fast_reverse_step(const RenderParams& p, const A
         vol.corners(ix, iy, iz, smp.d);
         smp.cx = ix; smp.cy = iy; smp.cz = iz;
       }
-      const f3 adj_vp = trilerp_adjoint(smp.d, fx, fy, fz, adj_density, VOLGRAD ? vg.g : nullptr);
-      const f3 adj_w = mk3(adj_vp.x / r.voxel.x, adj_vp.y / r.voxel.y, adj_vp.z / r.voxel.z);
+      // position derivative in difference form (the same derivative as the
+      // reference's per-corner sums, renderer/renderer_interpolation.cuh:360-387,
+      // in about half the instructions), scaled to world units
+      f3 g;
+      trilerp_grad(smp.d, fx, fy, fz, g);
+      if constexpr (VOLGRAD) add_corner_weights(vg.g, adj_density, fx, fy, fz);
+      const f3 adj_w = mk3(adj_density * g.x * r.inv_voxel.x, adj_density * g.y * r.inv_voxel.y,
+                           adj_density * g.z * r.inv_voxel.z);
       adj_start.x += adj_w.x; adj_start.y += adj_w.y; adj_start.z += adj_w.z;
       adj_dir.x += adj_w.x * t; adj_dir.y += adj_w.y * t; adj_dir.z += adj_w.z * t;
       adj_step += dot3(adj_w, r.dir) * k;
     } else if constexpr (VOLGRAD) {
-      const float gx = 1 - fx, gy = 1 - fy, gz = 1 - fz;
-      vg.g[0] += adj_density * (gx * gy * gz);
-      vg.g[1] += adj_density * (gx * gy * fz);
-      vg.g[2] += adj_density * (gx * fy * gz);
-      vg.g[3] += adj_density * (gx * fy * fz);
-      vg.g[4] += adj_density * (fx * gy * gz);
-      vg.g[5] += adj_density * (fx * gy * fz);
-      vg.g[6] += adj_density * (fx * fy * gz);
-      vg.g[7] += adj_density * (fx * fy * fz);
+      add_corner_weights(vg.g, adj_density, fx, fy, fz);
     }
   }
 }

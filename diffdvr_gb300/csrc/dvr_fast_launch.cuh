@@ -94,6 +94,19 @@ static int persistent_grid(K kernel, size_t smem, int64_t rays, const LaunchInfo
   return int(need < cap ? (need > 0 ? need : 1) : cap);
 }
 
+// Volume batch entries of a call (1 for a broadcast volume).
+static inline int volume_entries(const RenderParams& p) { return p.volume.s[0] != 0 ? p.B : 1; }
+
+// Whether a trilinear call reads its corners from the slab gather texture
+// (DvrForwardGather): TEXTURE, or AUTO with cell records larger than 64 MB
+// (smaller ones stay in L2 and are read as cells by the forward).
+template <typename VT>
+static bool texture_gather_wanted(const RenderParams& p) {
+  const int mode = forward_gather_mode();
+  const size_t cell_bytes = size_t(p.X) * p.Y * p.Z * volume_entries(p) * sizeof(CellWords<VT>);
+  return mode == DVR_GATHER_TEXTURE || (mode == DVR_GATHER_AUTO && cell_bytes > (size_t(64) << 20));
+}
+
 // Builds the slab gather texture of the volume (TexGather): the tiled,
 // aproned slab image is written to scratch and copied into the texture's
 // array.  cudaErrorNotSupported when the slabs exceed the gather texture's
@@ -166,7 +179,7 @@ cudaError_t launch_fast_forward_vt(const RenderParams& p, int filter, int blend,
     const size_t n = size_t(p.X) * p.Y * p.Z * bv;
     const size_t cell_bytes = n * sizeof(CellWords<VT>), raw_bytes = n * sizeof(VT);
     const bool cells_in_l2 = cell_bytes <= (size_t(64) << 20);
-    if (mode == DVR_GATHER_TEXTURE || (mode == DVR_GATHER_AUTO && !cells_in_l2)) {
+    if (texture_gather_wanted<VT>(p)) {
       err = build_gather_texture<VT>(p, bv, li, s, tg);
       if (err == cudaSuccess) gather = kGatherTexture;
       else if (err != cudaErrorNotSupported) return err;
@@ -244,7 +257,7 @@ static cudaError_t fast_adjoint_record_go(const RenderParams& p, const AdjointPa
   if (!counter2) return e;
   gen<<<ggrid, kFastThreads, gsmem, s>>>(p, a, order, counter2,
                                          reinterpret_cast<float*>(scratch + order_bytes + left_bytes), leftover,
-                                         counter + 1);
+                                         counter + 1, TexGather{});
   return cudaGetLastError();
 }
 
@@ -299,7 +312,7 @@ static cudaError_t fast_adjoint_window_go(const RenderParams& p, const AdjointPa
     if (!counter2) return e;
     gk<<<ggrid, kFastThreads, gsmem, s>>>(p, a, order, counter2,
                                           tfgrad ? reinterpret_cast<float*>(scratch + left_bytes + wtf) : nullptr,
-                                          leftover, counter + 1);
+                                          leftover, counter + 1, TexGather{});
     return cudaGetLastError();
   };
   if (tfgrad)
@@ -340,9 +353,20 @@ static cudaError_t fast_adjoint_go(const RenderParams& p, const AdjointParams& a
     int* order_ints = reinterpret_cast<int*>(scratch);
     e = order_rays_by_work(p, &a, order_ints, li, s);
     if (e != cudaSuccess) return e;
+    // the slab gather texture serves the re-march of rays without a record
+    // and the corner reads of position derivatives; with a record and no
+    // position derivatives the kernel reads no volume (only the rare rays
+    // the pool could not hold do, from the volume directly)
+    TexGather tg{};
+    if (FILTER == kTrilinear && (!p.dens || a.has_camera || a.has_stepsize || a.has_viewport) &&
+        texture_gather_wanted<VT>(p)) {
+      e = build_gather_texture<VT>(p, volume_entries(p), li, s, tg);
+      if (e == cudaErrorNotSupported) tg = TexGather{};
+      else if (e != cudaSuccess) return e;
+    }
     kernel<<<grid, kFastThreads, smem, s>>>(p, a, order, counter, tfgrad ? reinterpret_cast<float*>(scratch + list_bytes)
                                                                        : nullptr,
-                                            order_ints + work_order_list_offset, nullptr);
+                                            order_ints + work_order_list_offset, nullptr, tg);
     return cudaGetLastError();
   };
   if constexpr (TF == kTfTexture) {
@@ -405,7 +429,7 @@ static cudaError_t fast_adjoint_into_go(const RenderParams& p, const AdjointPara
     cudaError_t e = set_smem(kernel, smem);
     if (e != cudaSuccess) return e;
     const int grid = int(std::min<int64_t>(persistent_grid(kernel, smem, order.total(), li), fit));
-    kernel<<<grid, kFastThreads, smem, s>>>(p, a, order, sc.counter, sc.tf, nullptr, nullptr);
+    kernel<<<grid, kFastThreads, smem, s>>>(p, a, order, sc.counter, sc.tf, nullptr, nullptr, TexGather{});
     return cudaGetLastError();
   };
   if (volgrad)

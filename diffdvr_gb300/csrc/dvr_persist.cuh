@@ -14,7 +14,7 @@
 // checkpoint and runs the reverse recursion over it; lanes may be on different
 // rays and segment indices.  The per-step math is that of dvr_fast.cuh.
 #pragma once
-#include "dvr_fast.cuh"
+#include "dvr_cells.cuh"
 
 namespace dvr {
 
@@ -72,7 +72,8 @@ __global__ void __launch_bounds__(kFastThreads) fast_adjoint_persistent_kernel(c
                                                                                 const RayOrder order, int* counter,
                                                                                 float* tf_scratch,
                                                                                 const int* ray_list,
-                                                                                const int* ray_count) {
+                                                                                const int* ray_count,
+                                                                                const TexGather tg) {
   extern __shared__ float4 fast_smem4[];
   if (ray_count && *ray_count == 0) return;  // an empty list: nothing to add
   constexpr int C = TfChannels<TF>::C;
@@ -120,8 +121,10 @@ __global__ void __launch_bounds__(kFastThreads) fast_adjoint_persistent_kernel(c
   f3 adj_start = mk3(0, 0, 0), adj_dir = mk3(0, 0, 0);
   Sampler<FILTER, VT> smp;
   VolGradCell<FILTER, VOLGRAD> vg;
-  VolumeFast<VT> vol{static_cast<const VT*>(p.volume.p), int(p.volume.s[1]), int(p.volume.s[2]),
-                     int(p.volume.s[3]), p.X - 1, p.Y - 1, p.Z - 1};
+  // trilinear corners from the slab gather texture when the call built one
+  AdjVolume<VT> vol(VolumeFast<VT>{static_cast<const VT*>(p.volume.p), int(p.volume.s[1]), int(p.volume.s[2]),
+                                   int(p.volume.s[3]), p.X - 1, p.Y - 1, p.Z - 1},
+                    TexVolume<VT>{tg, 0, p.X - 1, p.Y - 1, p.Z - 1}, tg.tex != 0);
   TfShared<C> tf{s_tf, p.R};
   float* adjv = nullptr;
   const float* ck = nullptr;
@@ -175,7 +178,8 @@ __global__ void __launch_bounds__(kFastThreads) fast_adjoint_persistent_kernel(c
           smp.cx = -1;
           vg.cx = -1;
           vg.reset();
-          vol.p = static_cast<const VT*>(p.volume.p) + b * p.volume.s[0];
+          vol.v.p = static_cast<const VT*>(p.volume.p) + b * p.volume.s[0];
+          vol.t.s0 = p.volume.s[0] != 0 ? b * p.X : 0;
           tf = TfShared<C>(s_tf + (copies > 1 ? b : 0) * p.R * C, p.R);
           adjv = VOLGRAD ? static_cast<float*>(a.adj_volume.p) + b * a.adj_volume.s[0] : nullptr;
           ckpt_ray = p.ckpt.p != nullptr && n <= (p.ckpt_slots + 1) * K;

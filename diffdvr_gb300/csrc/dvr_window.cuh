@@ -454,8 +454,11 @@ __global__ void __launch_bounds__(kFastThreads) window_adjoint_kernel(const Rend
             scy = iy;
             scz = iz;
           }
-          const f3 adj_vp = trilerp_adjoint(d8, fx, fy, fz, adj_density, vg.g);
-          const f3 adj_w = mk3(adj_vp.x / r.voxel.x, adj_vp.y / r.voxel.y, adj_vp.z / r.voxel.z);
+          f3 g;
+          trilerp_grad(d8, fx, fy, fz, g);
+          add_corner_weights(vg.g, adj_density, fx, fy, fz);
+          const f3 adj_w = mk3(adj_density * g.x * r.inv_voxel.x, adj_density * g.y * r.inv_voxel.y,
+                               adj_density * g.z * r.inv_voxel.z);
           adj_start.x += adj_w.x; adj_start.y += adj_w.y; adj_start.z += adj_w.z;
           adj_dir.x += adj_w.x * t; adj_dir.y += adj_w.y * t; adj_dir.z += adj_w.z * t;
           adj_step += dot3(adj_w, r.dir) * k;

@@ -5,8 +5,16 @@ reference's headers (``oracle/ref_device.cu``) through the CUDA driver API,
 the way the reference's CUDA backend does: the forward and adjoint kernels
 take their parameter blocks by value, with the block size and grid that
 ``cuOccupancyMaxPotentialBlockSize`` gives (renderer/kernel_loader.cpp:514-515,
-renderer/renderer_cuda.cpp:85-118) and, for the delayed TF accumulation,
-``R*C`` floats of shared memory per thread (renderer/renderer_cuda.cpp:273-307).
+renderer/renderer_cuda.cpp:85-118).
+
+The reference's delayed TF accumulation (per-thread shared-memory TF
+gradients reduced over each warp, renderer/renderer_tf.cuh:173-253 and its
+siblings) is never launched: its warp reduction
+(renderer/cooperative_groups.cuh:161-212) passes the shuffle's value where
+the member mask belongs (:206) whenever a warp's active threads are not a
+power of two in number, and kernels built with it raised "an illegal
+instruction was encountered" on the GB300.  The TF gradients come from the
+reference's immediate-atomics variant.
 
 The parameter blocks are filled on the GPU by ``ref_build_params`` from the
 plain-C structs of ``dvr_oracle.h``; every block is read back through the
@@ -55,8 +63,6 @@ def adjoint_kernel_name(scene: O.Scene, stepsize: bool, camera: bool, tf: bool, 
 class _Driver:
     """The few CUDA driver calls the reference's backend makes, via ctypes."""
 
-    _OCC_CB = ctypes.CFUNCTYPE(ctypes.c_size_t, ctypes.c_int)
-
     def __init__(self):
         import torch
         if not torch.cuda.is_available():
@@ -99,15 +105,6 @@ class _Driver:
             self.functions[name] = (f, block.value, grid.value)
         return self.functions[name]
 
-    def occupancy_with_smem(self, f, bytes_per_thread: int):
-        """(block, grid) when each thread of a block needs bytes_per_thread of shared memory."""
-        cb = self._OCC_CB(lambda block: bytes_per_thread * block)
-        grid, block = ctypes.c_int(), ctypes.c_int()
-        self._check(self.lib.cuOccupancyMaxPotentialBlockSize(
-            ctypes.byref(grid), ctypes.byref(block), f, ctypes.cast(cb, ctypes.c_void_p), 0, 0),
-            "cuOccupancyMaxPotentialBlockSize")
-        return block.value, grid.value
-
     def launch(self, f, grid: int, block: int, smem: int, stream: int, args: list) -> None:
         params = (ctypes.c_void_p * len(args))(*[ctypes.cast(ctypes.pointer(a), ctypes.c_void_p) for a in args])
         self._check(self.lib.cuLaunchKernel(f, grid, 1, 1, block, 1, 1, smem, ctypes.c_void_p(stream), params, None),
@@ -146,7 +143,7 @@ class Call:
     the current stream and nothing else (the gradient buffers are zeroed by
     the caller, as the reference requires)."""
 
-    def __init__(self, scene: O.Scene, adjoint: Optional[O.AdjointRequest] = None, delayed: bool = False,
+    def __init__(self, scene: O.Scene, adjoint: Optional[O.AdjointRequest] = None,
                  color=None, term=None, adj_color=None):
         import torch
         self.drv = driver()
@@ -211,8 +208,7 @@ class Call:
                 out.adj_stepsize = _dev_tensor(self.grads["adj_stepsize"], keep)
             if self.adj_color is None:
                 raise ValueError("the adjoint needs adj_color")
-            self.adjoint_name = adjoint_kernel_name(scene, req.stepsize, req.camera, req.tf, delayed, req.volume)
-        self.delayed = delayed
+            self.adjoint_name = adjoint_kernel_name(scene, req.stepsize, req.camera, req.tf, False, req.volume)
         self.adj_out = out
         tc = _dev_tensor(self.color, keep)
         tt = _dev_tensor(self.term, keep)
@@ -238,16 +234,8 @@ class Call:
         self.fwd_cfg = (max(1, min(-(-n // bs), mg)), bs, 0)
         if self.adjoint_name is not None:
             f, bs, mg = self.drv.function(self.adjoint_name)
-            smem = 0
-            if delayed:
-                R, C = int(scene.tf.shape[1]), int(scene.tf.shape[2])
-                bs, mg = self.drv.occupancy_with_smem(f, 4 * R * C)
-                if bs <= 0:
-                    raise RuntimeError("delayed TF accumulation: not even one warp fits the shared memory")
-                smem = 4 * R * C * bs
-                assert smem >= 4 * R * C * bs  # thread t uses floats [t*R*C, (t+1)*R*C)
             self.adj_fn = f
-            self.adj_cfg = (max(1, min(-(-n // bs), mg)), bs, smem)
+            self.adj_cfg = (max(1, min(-(-n // bs), mg)), bs, 0)
 
     def run_forward(self) -> None:
         import torch
@@ -271,29 +259,50 @@ def forward(scene: O.Scene):
     return c.color.cpu().numpy(), c.term.cpu().numpy()
 
 
-def adjoint(scene: O.Scene, color: np.ndarray, term: np.ndarray, adj_color: np.ndarray, req: O.AdjointRequest,
-            delayed: bool = False) -> dict:
-    """The reference's CUDA adjoint: a dict of gradient arrays like oracle.adjoint's."""
+def adjoint(scene: O.Scene, color: np.ndarray, term: np.ndarray, adj_color: np.ndarray,
+            req: O.AdjointRequest) -> dict:
+    """The reference's CUDA adjoint (TF gradients by immediate atomics): a
+    dict of gradient arrays like oracle.adjoint's."""
     import torch
-    c = Call(scene, adjoint=req, delayed=delayed, color=color, term=term, adj_color=adj_color)
+    c = Call(scene, adjoint=req, color=color, term=term, adj_color=adj_color)
     c.run_adjoint()
     torch.cuda.synchronize()
     return {k: v.cpu().numpy() for k, v in c.grads.items()}
 
 
-def time_tf_reconstruction(steps: int = 5, warmup: int = 3, delayed: bool = True, w=None) -> dict:
-    """The reference's CUDA forward + TF adjoint on the TF-reconstruction
-    workload (256^3 FP32 volume of blobs + noise, 64-entry texture TF, 8 views
-    at 256^2, step 0.25 voxel, Beer-Lambert; the reference stores volumes in
-    FP32 only), timed with CUDA events on the launching stream after `warmup`
-    steps; a 256 MB buffer is written before every step so the volume (64 MB)
-    is not left in L2.  delayed: the reference's default per-thread
-    shared-memory TF accumulation, else immediate atomics.  w: the workload,
-    if already generated."""
+# The adjoints the timing below launches, per workload: (TF mode, camera,
+# TF, delayed TF accumulation, volume derivatives), all with trilinear
+# filtering, per-pixel rays and Beer-Lambert blending, no step-size
+# derivatives: the reference's kernel for exactly the gradients each
+# workload asks for, TF gradients by immediate atomics.
+# oracle/ref_device.cu instantiates each one.
+TIMED_ADJOINTS = {
+    "tf_reconstruction_256": (1, False, True, False, False),
+    "absorption_recon_128": (0, False, False, False, True),
+    "large_mixed_512": (2, True, True, False, True),
+    "plain_cpu_64": (2, False, True, False, True),
+}
+
+
+def timed_adjoint_name(tf_mode: int, camera: bool, tf: bool, delayed: bool, volume: bool) -> str:
+    sc = O.Scene(width=1, height=1, volume=None, tf=None, step_size=None, box_min=None, box_size=None,
+                 filter_mode=1, camera_mode=0, tf_mode=tf_mode, blend_mode=0)
+    return adjoint_kernel_name(sc, False, camera, tf, delayed, volume)
+
+
+def time_workload(w, volume: Optional[np.ndarray] = None, steps: int = 5, warmup: int = 3) -> dict:
+    """The reference's CUDA forward + adjoint on a workload of
+    ``diffdvr_gb300.scenes`` (a Workload with per-pixel rays), with the
+    gradients the workload asks for (``TIMED_ADJOINTS``), timed with CUDA
+    events on the launching stream after `warmup` steps; a 256 MB buffer is
+    written before every step so the volume is not left in L2.  volume: the
+    FP32 volume each step renders (the workload's own when None; the
+    reference stores volumes in FP32 only)."""
     import torch
-    from diffdvr_gb300 import scenes
-    w = w or scenes.tf_reconstruction_256()
-    vol = w.volume if w.volume.ndim == 4 else w.volume[None]
+    tf_mode, cam, tfg, dl, volg = TIMED_ADJOINTS[w.name]
+    assert tf_mode == w.tf_mode and w.filter_mode == 1 and w.blend_mode == 0, w.name
+    vol = np.asarray(w.volume if volume is None else volume, dtype=np.float32)
+    vol = vol if vol.ndim == 4 else vol[None]
     sc = O.Scene(width=w.width, height=w.height, volume=vol, tf=w.tf,
                  step_size=np.full((1, 1, 1), w.step_size, np.float32),
                  box_min=np.asarray([w.box_min], np.float32), box_size=np.asarray([w.box_size], np.float32),
@@ -301,13 +310,15 @@ def time_tf_reconstruction(steps: int = 5, warmup: int = 3, delayed: bool = True
                  ray_start=w.ray_start, ray_dir=w.ray_dir)
     B = sc.batch()
     adj = np.random.default_rng(0).normal(size=(B, w.height, w.width, 4)).astype(np.float32)
-    call = Call(sc, adjoint=O.AdjointRequest(tf=True), delayed=delayed, adj_color=adj)
+    call = Call(sc, adjoint=O.AdjointRequest(tf=tfg, volume=volg, camera=cam), adj_color=adj)
+    assert call.adjoint_name == timed_adjoint_name(tf_mode, cam, tfg, dl, volg)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
     t_fwd, t_adj = [], []
     for i in range(warmup + steps):
         flush.zero_()
-        call.grads["adj_tf"].zero_()
+        for g in call.grads.values():
+            g.zero_()
         torch.cuda.synchronize()
         ev[0].record()
         call.run_forward()
@@ -320,15 +331,22 @@ def time_tf_reconstruction(steps: int = 5, warmup: int = 3, delayed: bool = True
             t_adj.append(ev[1].elapsed_time(ev[2]))
     samples = int(call.term.sum().item())
     f, a = float(np.median(t_fwd)), float(np.median(t_adj))
-    return {"workload": w.name, "volume_dtype": "f32", "tf_accumulation": "delayed" if delayed else "immediate",
+    return {"workload": w.name, "volume_dtype": "f32", "gradients": sorted(call.grads),
+            "tf_accumulation": ("delayed" if dl else "immediate") if tfg else None,
             "samples_per_step": samples, "forward_ms": f, "adjoint_ms": a,
-            "samples_per_s": samples / ((f + a) * 1e-3),
+            "samples_per_s": samples / ((f + a) * 1e-3), "kernels": [forward_kernel_name(sc), call.adjoint_name],
             "launch": {"forward": list(call.fwd_cfg), "adjoint": list(call.adj_cfg)}}
+
+
+def time_tf_reconstruction(steps: int = 5, warmup: int = 3, w=None) -> dict:
+    """The reference's CUDA forward + TF adjoint on the TF-reconstruction
+    workload (256^3 FP32 volume of blobs + noise, 64-entry texture TF, 8 views
+    at 256^2, step 0.25 voxel, Beer-Lambert): ``time_workload``."""
+    from diffdvr_gb300 import scenes
+    return time_workload(w or scenes.tf_reconstruction_256(), steps=steps, warmup=warmup)
 
 
 if __name__ == "__main__":
     import json
     from diffdvr_gb300 import scenes
-    workload = scenes.tf_reconstruction_256()
-    for d in (True, False):
-        print(json.dumps(time_tf_reconstruction(delayed=d, w=workload)), flush=True)
+    print(json.dumps(time_tf_reconstruction(w=scenes.tf_reconstruction_256())), flush=True)

@@ -95,9 +95,7 @@ extern "C" __global__ void ref_build_params(const OracleInputs in, const OracleT
 // Forward: every filter x camera x TF x blend combination.  Adjoint: step
 // size, TF and volume derivatives (plus camera derivatives for per-pixel
 // rays, the only camera mode whose rays have gradients) with immediate TF
-// atomics; for the TF-reconstruction modes also the TF-only kernels with and
-// without the delayed (per-thread shared memory) TF accumulation, the
-// reference's default in pytests/diffdvr/renderer.py:270.
+// atomics; for the TF-reconstruction modes also the TF-only kernel.
 #define DVR_REF_MODE(F, C, T, B) DVR_REF_FWD(F, C, T, B)
 #define DVR_REF_BLENDS(F, C, T)                 \
   DVR_REF_MODE(F, C, T, BlendBeerLambert)       \
@@ -121,4 +119,21 @@ DVR_REF_CAMS(FilterNearest)
 DVR_REF_CAMS(FilterTrilinear)
 
 DVR_REF_ADJ(FilterTrilinear, CameraRayStartDir, TFTexture, BlendBeerLambert, 0, 0, 1, 0, 0)
-DVR_REF_ADJ(FilterTrilinear, CameraRayStartDir, TFTexture, BlendBeerLambert, 0, 0, 1, 1, 0)
+
+// The adjoints that time the reference's CUDA path on the other workloads
+// (oracle/ref_cuda.py, TIMED_ADJOINTS), each with exactly the derivatives its
+// workload asks for: the volume only (identity TF, absorption
+// reconstruction); rays, TF and volume (linear TF, large mixed
+// configuration); TF and volume (linear TF, the small CPU-sized
+// configuration).
+//
+// No kernel here uses the reference's delayed TF accumulation (its
+// per-thread shared-memory TF gradient, the default of
+// pytests/diffdvr/renderer.py:270): its warp reduction
+// (renderer/cooperative_groups.cuh:161-212) passes the shuffle's value where
+// the member mask belongs (:206) whenever the active threads of a warp are
+// not a power of two in number, and kernels built with it raised "an
+// illegal instruction was encountered" on the GB300.
+DVR_REF_ADJ(FilterTrilinear, CameraRayStartDir, TFIdentity, BlendBeerLambert, 0, 0, 0, 0, 1)
+DVR_REF_ADJ(FilterTrilinear, CameraRayStartDir, TFLinear, BlendBeerLambert, 0, 1, 1, 0, 1)
+DVR_REF_ADJ(FilterTrilinear, CameraRayStartDir, TFLinear, BlendBeerLambert, 0, 0, 1, 0, 1)

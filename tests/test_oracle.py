@@ -208,8 +208,8 @@ def test_reference_cuda_kernel_names(oracle_built, tmp_path):
         want.add(R.forward_kernel_name(sc))
         want.add(R.adjoint_kernel_name(sc, True, cam == 0, True, False, True))
     sc = O.Scene(width=1, height=1, volume=None, tf=None, step_size=None, box_min=None, box_size=None)
-    for delayed in (False, True):
-        want.add(R.adjoint_kernel_name(sc, False, False, True, delayed, False))
+    want.add(R.adjoint_kernel_name(sc, False, False, True, False, False))
+    want.update(R.timed_adjoint_name(*v) for v in R.TIMED_ADJOINTS.values())
     assert want == defined, (sorted(want - defined), sorted(defined - want))
     adj = list(re.finditer(r"void (ref_adj_\w+)\s*\(.*?DvrKernelAdjointImpl<[^>]*?,\s*(\d),\s*(\d),\s*(\d),"
                            r"\s*(\d),\s*(\d)\s*>", src, re.S))
