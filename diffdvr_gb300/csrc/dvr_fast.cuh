@@ -707,6 +707,9 @@ template <int FILTER, bool VOLGRAD>
 struct VolGradCell {
   int cx = -1, cy = -1, cz = -1;
   float g[8];
+  // the cell-corner gradient of this ray's volume batch entry
+  // (AdjointParams::cell_grad), or nullptr
+  float* cg = nullptr;
   __device__ __forceinline__ void reset() {
 #pragma unroll
     for (int q = 0; q < 8; ++q) g[q] = 0.f;
@@ -717,6 +720,13 @@ struct VolGradCell {
       const int64_t sx = o.s[1], sy = o.s[2], sz = o.s[3];
       if constexpr (FILTER == kNearest) {
         if (g[0] != 0.f) atomicAdd(adjv + cx * sx + cy * sy + cz * sz, g[0]);
+      } else if (cg) {
+        // the cell's eight sums as two aligned 16-byte reductions; a cell
+        // index above size - 1 (a sample within rounding of the far face)
+        // has the same clamped corners as cell size - 1, which stands for it
+        float* e = cg + ((size_t(clampi(cx, 0, X1)) * (Y1 + 1) + clampi(cy, 0, Y1)) * (Z1 + 1) + clampi(cz, 0, Z1)) * 8;
+        atomicAdd(reinterpret_cast<float4*>(e), make_float4(g[0], g[1], g[2], g[3]));
+        atomicAdd(reinterpret_cast<float4*>(e + 4), make_float4(g[4], g[5], g[6], g[7]));
       } else {
         const int lx = clampi(cx, 0, X1), hx = clampi(cx + 1, 0, X1);
         const int ly = clampi(cy, 0, Y1), hy = clampi(cy + 1, 0, Y1);

@@ -94,6 +94,11 @@ static int persistent_grid(K kernel, size_t smem, int64_t rays, const LaunchInfo
   return int(need < cap ? (need > 0 ? need : 1) : cap);
 }
 
+// Largest cell-corner volume gradient (8 floats per cell and volume batch
+// entry) the general adjoint accumulates into: it must stay in L2 beside the
+// volume and the sample record's stream.
+constexpr size_t kCellGradMaxBytes = size_t(80) << 20;
+
 // Volume batch entries of a call (1 for a broadcast volume).
 static inline int volume_entries(const RenderParams& p) { return p.volume.s[0] != 0 ? p.B : 1; }
 
@@ -364,10 +369,22 @@ static cudaError_t fast_adjoint_go(const RenderParams& p, const AdjointParams& a
       if (e == cudaErrorNotSupported) tg = TexGather{};
       else if (e != cudaSuccess) return e;
     }
-    kernel<<<grid, kFastThreads, smem, s>>>(p, a, order, counter, tfgrad ? reinterpret_cast<float*>(scratch + list_bytes)
-                                                                       : nullptr,
+    // volume gradient through the cell-corner buffer where it stays in L2
+    AdjointParams ac = a;
+    const int vb = a.adj_volume.s[0] != 0 ? p.B : 1;
+    const size_t cell_bytes = size_t(p.X) * p.Y * p.Z * vb * 8 * sizeof(float);
+    if (FILTER == kTrilinear && volgrad && cell_bytes <= kCellGradMaxBytes) {
+      ac.cell_grad = static_cast<float*>(acquire_scratch(li.device, s, cell_bytes, e, 2));
+      if (!ac.cell_grad) return e;
+      e = cudaMemsetAsync(ac.cell_grad, 0, cell_bytes, s);
+      if (e != cudaSuccess) return e;
+    }
+    kernel<<<grid, kFastThreads, smem, s>>>(p, ac, order, counter, tfgrad ? reinterpret_cast<float*>(scratch + list_bytes)
+                                                                        : nullptr,
                                             order_ints + work_order_list_offset, nullptr, tg);
-    return cudaGetLastError();
+    e = cudaGetLastError();
+    if (e != cudaSuccess || !ac.cell_grad) return e;
+    return fold_cell_grad(ac.cell_grad, a.adj_volume, p.X, p.Y, p.Z, vb, li, s);
   };
   if constexpr (TF == kTfTexture) {
     // TF gradient only, from the sample-density record

@@ -67,6 +67,11 @@ size_t work_order_ints(const RenderParams& p);
 cudaError_t order_rays_by_work(const RenderParams& p, const AdjointParams* a, int* scratch, const LaunchInfo& li,
                                cudaStream_t s);
 
+// Adds the cell-corner volume gradient cell_grad (AdjointParams::cell_grad,
+// vb volume batch entries of X*Y*Z cells) to adj_volume (dvr_cellgrad.cu).
+cudaError_t fold_cell_grad(const float* cell_grad, const OutView& adj_volume, int X, int Y, int Z, int vb,
+                           const LaunchInfo& li, cudaStream_t s);
+
 // Plain family (reference semantics).
 template <int TF>
 cudaError_t launch_plain_forward(const RenderParams& p, int filter, int blend, const LaunchInfo& li, cudaStream_t s);

@@ -67,6 +67,12 @@ struct AdjointParams {
   OutView adj_tf;               // [b][r][c]
   int32_t has_viewport, pad2_;
   OutView adj_viewport;         // [b][row][c], reference-frame camera (broadcast strides allowed)
+  // Optional cell-corner volume gradient (general adjoint, trilinear): for
+  // every volume batch entry of adj_volume and every cell (x, y, z), the
+  // eight corner sums of the cell in the corner order of the trilinear
+  // fetch, 8 floats per cell, z fastest; folded into adj_volume after the
+  // launch.  nullptr: cells flush straight into adj_volume.
+  float* cell_grad;
 };
 
 // Forward-mode derivatives (renderForwardGradients): derivative indices

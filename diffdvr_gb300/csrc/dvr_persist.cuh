@@ -182,6 +182,8 @@ __global__ void __launch_bounds__(kFastThreads) fast_adjoint_persistent_kernel(c
           vol.t.s0 = p.volume.s[0] != 0 ? b * p.X : 0;
           tf = TfShared<C>(s_tf + (copies > 1 ? b : 0) * p.R * C, p.R);
           adjv = VOLGRAD ? static_cast<float*>(a.adj_volume.p) + b * a.adj_volume.s[0] : nullptr;
+          if (VOLGRAD && a.cell_grad)
+            vg.cg = a.cell_grad + (a.adj_volume.s[0] != 0 ? size_t(b) : 0) * 8 * size_t(p.X) * p.Y * p.Z;
           ckpt_ray = p.ckpt.p != nullptr && n <= (p.ckpt_slots + 1) * K;
           drow = nullptr;
           if (ckpt_ray) {
