@@ -184,10 +184,12 @@ typedef struct DvrAdjointOutputs {
  * Replaces renderer::Renderer::renderForward (renderer/renderer.h:159-161,
  * renderer/renderer.cpp:393-417).
  * Library scratch: the optimized family takes work counters and, per
- * stream, a ray-order buffer (and the cell-corner volume for trilinear
- * filtering) from pools that it grows with cudaMalloc when a call needs more
- * than they hold; dvr_render_adjoint does the same for its ray order and
- * TF-gradient slices.  cudaMalloc is not allowed while a stream is being
+ * stream, a ray-order buffer (and, for trilinear filtering, the cell-corner
+ * volume or the slab gather texture with its staging image) from pools that
+ * it grows with cudaMalloc when a call needs more than they hold;
+ * dvr_render_adjoint does the same for its ray order, TF-gradient slices,
+ * the gather texture of the rays it marches again and the cell-corner
+ * volume-gradient buffer.  cudaMalloc is not allowed while a stream is being
  * captured into a CUDA graph, so make one call of the same sizes on the same
  * stream before capturing it; later calls reuse the pools and allocate
  * nothing. */
