@@ -40,6 +40,84 @@ __device__ __forceinline__ float over(float a, float b) { return a + (1.f - a) *
 // How a trilinear sample reads its eight corners.
 enum { kGatherDirect = 0, kGatherCells = 1, kGatherTexture = 2 };
 
+// Marches ray (b, x, y) with the 32 lanes of the calling warp, 32
+// consecutive samples per step: writes its colour and termination index,
+// and per sample the (density, incoming opacity) pair to rec (when not
+// nullptr) or the opacity before every K-th sample to the checkpoints ck
+// (when not nullptr).  sample(float3 q) returns the density at volume
+// position q.  Every lane of the warp calls it with the same ray.
+template <int TF, int BLEND, class Sample>
+__device__ __forceinline__ void warp_march_ray(const RenderParams& p, int b, int x, int y, const FastRay& q,
+                                               int kmax, const TfShared<TfChannels<TF>::C>& tf, float* rec,
+                                               float* ck, Sample sample) {
+  const int lane = threadIdx.x & 31;
+  const int K = p.ckpt_interval;
+  const int kshift = (K & (K - 1)) == 0 ? __ffs(K) - 1 : -1;  // log2 K for a power-of-two interval
+  float alpha = 0.f;  // accumulated opacity before the chunk
+  float cr = 0.f, cg = 0.f, cb = 0.f;  // this lane's samples' colour contributions
+  int n = 0;
+  for (int k0 = 0;; k0 += 32) {
+    const int k = k0 + lane;
+    const float t = q.tmin + k * q.step;
+    const bool in_ray = k < kmax && !(t > q.tmax);
+    float density = 0.f, a = 0.f;
+    f4 c = mk4(0, 0, 0, 0);
+    if (in_ray) {
+      density = sample(fast_pos(q, t));
+      c = tf_eval<TF>(tf, density);
+      a = blend_alpha<BLEND>(c.w, q.step);
+    }
+    // incoming opacity of each sample: exclusive "over" scan
+    float incl = a;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const float v = __shfl_up_sync(kFullMask, incl, o);
+      if (lane >= o) incl = over(v, incl);
+    }
+    float excl = __shfl_up_sync(kFullMask, incl, 1);
+    if (lane == 0) excl = 0.f;
+    const float a_in = over(alpha, excl);
+    const bool go = in_ray && !(a_in > p.early_out);
+    const unsigned gm = __ballot_sync(kFullMask, go);
+    const int f = gm == kFullMask ? 32 : __ffs(~gm) - 1;  // first sample not taken
+    const bool used = lane < f;
+    if (used) {
+      if (rec) __stcs(reinterpret_cast<float2*>(rec) + k, make_float2(density, a_in));
+      if (ck && k > 0) {
+        // opacity before sample (slot + 1) * K
+        const bool at = kshift >= 0 ? (k & (K - 1)) == 0 : k % K == 0;
+        const int slot = (kshift >= 0 ? k >> kshift : k / K) - 1;
+        if (at && slot < p.ckpt_slots) ck[slot * p.ckpt.s[3]] = a_in;
+      }
+      const float w = (1.f - a_in) * a;
+      const float2 rg = __ffma2_rn(make_float2(w, w), make_float2(c.x, c.y), make_float2(cr, cg));
+      cr = rg.x;
+      cg = rg.y;
+      cb = fmaf(w, c.z, cb);
+    }
+    if (f < 32) {
+      alpha = __shfl_sync(kFullMask, a_in, f);
+      n = k0 + f;
+      break;
+    }
+    alpha = over(alpha, __shfl_sync(kFullMask, incl, 31));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    cr += __shfl_xor_sync(kFullMask, cr, o);
+    cg += __shfl_xor_sync(kFullMask, cg, o);
+    cb += __shfl_xor_sync(kFullMask, cb, o);
+  }
+  if (lane == 0) {
+    float* col = static_cast<float*>(p.color.p) + b * p.color.s[0] + y * p.color.s[1] + x * p.color.s[2];
+    col[0] = cr;
+    col[p.color.s[3]] = cg;
+    col[2 * p.color.s[3]] = cb;
+    col[3 * p.color.s[3]] = alpha;
+    static_cast<int*>(p.term.p)[b * p.term.s[0] + y * p.term.s[1] + x * p.term.s[2]] = n;
+  }
+}
+
 // ray_list[0 .. *ray_count): the rays with samples (longest first); the
 // ordering pass has already finished the others.  GATHER: trilinear samples
 // load the corners directly from the volume, read the cell-corner volume
@@ -59,8 +137,6 @@ __global__ void __launch_bounds__(kFastThreads) fast_forward_warp_kernel(const R
 
   const int lane = threadIdx.x & 31;
   const int total = *ray_count;
-  const int K = p.ckpt_interval;
-  const int kshift = (K & (K - 1)) == 0 ? __ffs(K) - 1 : -1;  // log2 K for a power-of-two interval
   unsigned long long* const bump = reinterpret_cast<unsigned long long*>(counter + 2);
 
   while (true) {
@@ -98,71 +174,11 @@ __global__ void __launch_bounds__(kFastThreads) fast_forward_warp_kernel(const R
                     ? static_cast<float*>(p.ckpt.p) + b * p.ckpt.s[0] + y * p.ckpt.s[1] + x * p.ckpt.s[2]
                     : nullptr;
 
-    float alpha = 0.f;  // accumulated opacity before the chunk
-    float cr = 0.f, cg = 0.f, cb = 0.f;  // this lane's samples' colour contributions
-    int n = 0;
-    for (int k0 = 0;; k0 += 32) {
-      const int k = k0 + lane;
-      const float t = q.tmin + k * q.step;
-      const bool in_ray = k < kmax && !(t > q.tmax);
-      float density = 0.f, a = 0.f;
-      f4 c = mk4(0, 0, 0, 0);
-      if (in_ray) {
-        if constexpr (GATHER == kGatherCells) density = cv.sample(fast_pos(q, t));
-        else if constexpr (GATHER == kGatherTexture) density = tv.sample(fast_pos(q, t));
-        else density = sample_density<FILTER, VT>(vol, fast_pos(q, t));
-        c = tf_eval<TF>(tf, density);
-        a = blend_alpha<BLEND>(c.w, q.step);
-      }
-      // incoming opacity of each sample: exclusive "over" scan
-      float incl = a;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const float v = __shfl_up_sync(kFullMask, incl, o);
-        if (lane >= o) incl = over(v, incl);
-      }
-      float excl = __shfl_up_sync(kFullMask, incl, 1);
-      if (lane == 0) excl = 0.f;
-      const float a_in = over(alpha, excl);
-      const bool go = in_ray && !(a_in > p.early_out);
-      const unsigned gm = __ballot_sync(kFullMask, go);
-      const int f = gm == kFullMask ? 32 : __ffs(~gm) - 1;  // first sample not taken
-      const bool used = lane < f;
-      if (used) {
-        if (rec) __stcs(reinterpret_cast<float2*>(rec) + k, make_float2(density, a_in));
-        if (ck && k > 0) {
-          // opacity before sample (slot + 1) * K
-          const bool at = kshift >= 0 ? (k & (K - 1)) == 0 : k % K == 0;
-          const int slot = (kshift >= 0 ? k >> kshift : k / K) - 1;
-          if (at && slot < p.ckpt_slots) ck[slot * p.ckpt.s[3]] = a_in;
-        }
-        const float w = (1.f - a_in) * a;
-        const float2 rg = __ffma2_rn(make_float2(w, w), make_float2(c.x, c.y), make_float2(cr, cg));
-        cr = rg.x;
-        cg = rg.y;
-        cb = fmaf(w, c.z, cb);
-      }
-      if (f < 32) {
-        alpha = __shfl_sync(kFullMask, a_in, f);
-        n = k0 + f;
-        break;
-      }
-      alpha = over(alpha, __shfl_sync(kFullMask, incl, 31));
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      cr += __shfl_xor_sync(kFullMask, cr, o);
-      cg += __shfl_xor_sync(kFullMask, cg, o);
-      cb += __shfl_xor_sync(kFullMask, cb, o);
-    }
-    if (lane == 0) {
-      float* col = static_cast<float*>(p.color.p) + b * p.color.s[0] + y * p.color.s[1] + x * p.color.s[2];
-      col[0] = cr;
-      col[p.color.s[3]] = cg;
-      col[2 * p.color.s[3]] = cb;
-      col[3 * p.color.s[3]] = alpha;
-      static_cast<int*>(p.term.p)[b * p.term.s[0] + y * p.term.s[1] + x * p.term.s[2]] = n;
-    }
+    warp_march_ray<TF, BLEND>(p, b, x, y, q, kmax, tf, rec, ck, [&](float3 pos) {
+      if constexpr (GATHER == kGatherCells) return cv.sample(pos);
+      else if constexpr (GATHER == kGatherTexture) return tv.sample(pos);
+      else return sample_density<FILTER, VT>(vol, pos);
+    });
   }
 }
 
