@@ -14,11 +14,13 @@ configuration's accuracy report.
   position derivative is one-sided and picks its cell by rounding, so ray
   gradients would otherwise compare two different one-sided derivatives.
 * The large mixed-precision configuration's accuracy report: the 512^3
-  scene stored in BF16, its volume, TF and ray gradients against the FP64
-  oracle on a 64^3 crop (same TF and rays of one view, the box shrunk to the
-  sub-volume; the oracle gets the BF16-rounded voxels, so the comparison
-  measures the arithmetic, not the storage).
+  scene stored in BF16 and, separately, in FP16, its volume, TF and ray
+  gradients against the FP64 oracle on a 64^3 crop (same TF and rays of one
+  view, the box shrunk to the sub-volume; the oracle gets the rounded
+  voxels, so the comparison measures the arithmetic, not the storage).
 """
+import functools
+
 import numpy as np
 import pytest
 import torch
@@ -83,20 +85,27 @@ def test_degenerate_inputs(family, filter_mode, oracle_built, cuda_device):
     assert not failures, failures
 
 
-def test_large_mixed_crop_accuracy(oracle_built, cuda_device):
+@functools.lru_cache(maxsize=1)
+def _large_mixed_crop():
+    """The 64^3 crop at voxel 224 of the 512^3 scene, one view (built once:
+    the full scene takes a while)."""
     from diffdvr_gb300 import scenes
+    return scenes.crop(scenes.large_mixed_512(seed=4, views=1), (224, 224, 224), 64)
+
+
+@pytest.mark.parametrize("storage", [torch.bfloat16, torch.float16], ids=["bf16", "f16"])
+def test_large_mixed_crop_accuracy(storage, oracle_built, cuda_device):
     O = oracle_built
-    w = scenes.large_mixed_512(seed=4, views=1)
-    c = scenes.crop(w, (224, 224, 224), 64)
-    vol_bf16 = torch.from_numpy(c.volume).to(torch.bfloat16).to(torch.float32).numpy()
-    case = Case(width=c.width, height=c.height, volume=vol_bf16, tf=c.tf, tf_mode=c.tf_mode,
+    c = _large_mixed_crop()
+    vol_rounded = torch.from_numpy(c.volume).to(storage).to(torch.float32).numpy()
+    case = Case(width=c.width, height=c.height, volume=vol_rounded, tf=c.tf, tf_mode=c.tf_mode,
                 filter_mode=c.filter_mode, blend_mode=c.blend_mode, camera_mode=0, step=c.step_size,
                 box_min=c.box_min, box_size=c.box_size)
     case.ray_start, case.ray_dir = c.ray_start, c.ray_dir
     sc = case.oracle_scene()
     c64, t64 = O.forward(sc, "port", "f64")
     assert (t64 > 0).sum() > 500  # the view's rays cross the crop
-    inp, out = gpu_forward(case, "optimized", volume_dtype=torch.bfloat16, checkpoints=True)
+    inp, out = gpu_forward(case, "optimized", volume_dtype=storage, checkpoints=True)
     term = out.terminationIndex.cpu().numpy()
     same = term == t64
     assert np.mean(~same) <= 0.02
