@@ -649,16 +649,26 @@ def run_gpu(args):
     inp_e2e = inputs(vol_d, tf_d, cam_d)
     loss_d = torch.empty(1, device=dev)
 
+    # the target image is needed only by the loss: its copy runs on a side
+    # stream beside the forward, after the previous step's loss has read it
+    copy_stream = torch.cuda.Stream(device=dev)
+    target_in = torch.cuda.Event()
+
     def e2e_step():
+        cur = torch.cuda.current_stream()
+        copy_stream.wait_stream(cur)
+        with torch.cuda.stream(copy_stream):
+            tgt_d.copy_(target_host, non_blocking=True)
+            target_in.record(copy_stream)
         vol_d.copy_(vol_host, non_blocking=True)
         tf_d.copy_(tf_host, non_blocking=True)
         for d, h in zip(cam_d, cam_host):
             d.copy_(h, non_blocking=True)
-        tgt_d.copy_(target_host, non_blocking=True)
         if forward_method:
             pr.Renderer.render_forward_gradients(inp_e2e, fs, out_fg, J)
         else:
             pr.Renderer.render_forward(inp_e2e, out)
+        cur.wait_event(target_in)
         torch.sub(color, tgt_d, out=adj_color)
         loss_d.copy_((adj_color * adj_color).sum().view(1))
         adj_color.mul_(2 * inv_n)
