@@ -89,7 +89,7 @@ std::vector<ScratchSlot> g_scratch;
 struct GatherTextureSlot {
   int device = -1;
   cudaStream_t stream = nullptr;
-  int W = 0, H = 0, bits = 0;
+  int W = 0, H = 0, format = -1;
   cudaArray_t array = nullptr;
   cudaTextureObject_t tex = 0;
 };
@@ -125,7 +125,7 @@ void* acquire_scratch(int device, cudaStream_t s, size_t bytes, cudaError_t& err
   return slot->ptr;
 }
 
-cudaError_t acquire_gather_texture(int device, cudaStream_t s, int W, int H, int bits, cudaArray_t& array,
+cudaError_t acquire_gather_texture(int device, cudaStream_t s, int W, int H, int format, cudaArray_t& array,
                                    cudaTextureObject_t& tex) {
   std::lock_guard<std::mutex> lock(g_texture_mutex);
   GatherTextureSlot* slot = nullptr;
@@ -135,7 +135,7 @@ cudaError_t acquire_gather_texture(int device, cudaStream_t s, int W, int H, int
     g_textures.push_back(GatherTextureSlot{device, s});
     slot = &g_textures.back();
   }
-  if (slot->array && (slot->W != W || slot->H != H || slot->bits != bits)) {
+  if (slot->array && (slot->W != W || slot->H != H || slot->format != format)) {
     // earlier launches on this stream may still read the old texture
     const cudaError_t err = cudaStreamSynchronize(s);
     if (err != cudaSuccess) return err;
@@ -145,8 +145,10 @@ cudaError_t acquire_gather_texture(int device, cudaStream_t s, int W, int H, int
     slot->tex = 0;
   }
   if (!slot->array) {
-    const cudaChannelFormatDesc desc = bits == 32 ? cudaCreateChannelDesc<float>()
-                                                  : cudaCreateChannelDesc<unsigned short>();
+    // texel formats of TexelFormat (dvr_cells.cuh): 0 float, 1 half, 2 raw 16-bit
+    const cudaChannelFormatDesc desc = format == 0   ? cudaCreateChannelDesc<float>()
+                                       : format == 1 ? cudaCreateChannelDescHalf()
+                                                     : cudaCreateChannelDesc<unsigned short>();
     cudaError_t err = cudaMallocArray(&slot->array, &desc, size_t(W), size_t(H), cudaArrayTextureGather);
     if (err != cudaSuccess) {
       slot->array = nullptr;
@@ -169,7 +171,7 @@ cudaError_t acquire_gather_texture(int device, cudaStream_t s, int W, int H, int
     }
     slot->W = W;
     slot->H = H;
-    slot->bits = bits;
+    slot->format = format;
   }
   array = slot->array;
   tex = slot->tex;

@@ -126,24 +126,38 @@ __global__ void build_cells_kernel(const RenderParams p, int bv, CellWords<VT>* 
 // [-1, size-1] (the apron), the texels read are exactly the clamped corners of
 // VolumeFast::corners for every cell index (renderer/renderer_interpolation.cuh:193-207).
 // Texture fetches clamp their coordinates to the array, so no index reads
-// outside it.  Raw storage bits are kept: BF16 and FP16 as 16-bit unsigned
-// texels, FP32 as 32-bit float texels.
+// outside it.  Texels hold the stored values exactly (TexelFormat).
 struct TexGather {
   cudaTextureObject_t tex;
   int tshift;  // tiles per texture row = 2^tshift
   int tw, th;  // tile size in texels: Z + 2, Y + 2
 };
 
-template <typename VT>
-__device__ __forceinline__ float texel_value(unsigned short raw);
-template <>
-__device__ __forceinline__ float texel_value<__nv_bfloat16>(unsigned short raw) {
-  return __uint_as_float(unsigned(raw) << 16);
-}
-template <>
-__device__ __forceinline__ float texel_value<__half>(unsigned short raw) {
-  return __half2float(__ushort_as_half(raw));
-}
+// How the gather texture holds a volume's values, exactly in every case:
+//  kTexelF32:  32-bit float texels: FP32 volumes (and BF16 volumes widened,
+//              a BF16 value being the upper half of its FP32 bits, when
+//              kWideBf16Texels);
+//  kTexelF16:  16-bit float texels, which the texture unit returns as FP32;
+//  kTexelRaw16: the BF16 bits as 16-bit unsigned texels, widened in
+//              registers.
+// Widening BF16 saves the eight conversions per sample but doubles the
+// texture's bytes, and measured slower (256^3 forward 0.69 -> 0.78 ms,
+// 512^3 24.6 -> 25.8 ms), so BF16 volumes keep 16-bit texels.
+enum { kTexelF32 = 0, kTexelF16 = 1, kTexelRaw16 = 2 };
+constexpr bool kWideBf16Texels = false;
+template <typename VT> struct TexelFormat;
+template <> struct TexelFormat<float> {
+  static constexpr int kind = kTexelF32;
+  using T = float;
+};
+template <> struct TexelFormat<__half> {
+  static constexpr int kind = kTexelF16;
+  using T = unsigned short;
+};
+template <> struct TexelFormat<__nv_bfloat16> {
+  static constexpr int kind = kWideBf16Texels ? kTexelF32 : kTexelRaw16;
+  using T = typename std::conditional<kWideBf16Texels, float, unsigned short>::type;
+};
 
 // The four corners (y, z) of one slab in the corner order of
 // VolumeFast::corners: (ly lz), (ly hz), (hy lz), (hy hz).  tex2Dgather
@@ -151,13 +165,13 @@ __device__ __forceinline__ float texel_value<__half>(unsigned short raw) {
 // x = (u0, v1), y = (u1, v1), z = (u1, v0), w = (u0, v0).
 template <typename VT>
 __device__ __forceinline__ void gather_slab(cudaTextureObject_t tex, float u, float v, float* d) {
-  if constexpr (sizeof(VT) == 4) {
+  if constexpr (TexelFormat<VT>::kind == kTexelRaw16) {
+    const ushort4 g = tex2Dgather<ushort4>(tex, u, v, 0);
+    d[0] = __uint_as_float(unsigned(g.w) << 16); d[1] = __uint_as_float(unsigned(g.z) << 16);
+    d[2] = __uint_as_float(unsigned(g.x) << 16); d[3] = __uint_as_float(unsigned(g.y) << 16);
+  } else {
     const float4 g = tex2Dgather<float4>(tex, u, v, 0);
     d[0] = g.w; d[1] = g.z; d[2] = g.x; d[3] = g.y;
-  } else {
-    const ushort4 g = tex2Dgather<ushort4>(tex, u, v, 0);
-    d[0] = texel_value<VT>(g.w); d[1] = texel_value<VT>(g.z);
-    d[2] = texel_value<VT>(g.x); d[3] = texel_value<VT>(g.y);
   }
 }
 
@@ -220,8 +234,8 @@ struct AdjVolume {
 // slab are zero.
 template <typename VT>
 __global__ void build_gather_image_kernel(const RenderParams p, int bv, int tshift, int W, int H,
-                                          typename std::conditional<sizeof(VT) == 4, float, unsigned short>::type* out) {
-  using Texel = typename std::conditional<sizeof(VT) == 4, float, unsigned short>::type;
+                                          typename TexelFormat<VT>::T* out) {
+  using Texel = typename TexelFormat<VT>::T;
   const int X = p.X, Y = p.Y, Z = p.Z, tw = Z + 2, th = Y + 2;
   const int lane = threadIdx.x & 31;
   const int tc = blockIdx.x;
@@ -240,7 +254,7 @@ __global__ void build_gather_image_kernel(const RenderParams p, int bv, int tshi
     const int64_t sz = p.volume.s[3];
     for (int u = lane; u < tw; u += 32) {
       const VT e = src[min(max(u - 1, 0), Z - 1) * sz];
-      if constexpr (sizeof(VT) == 4) row[u] = e;
+      if constexpr (TexelFormat<VT>::kind == kTexelF32) row[u] = float(e);
       else row[u] = raw16(e);
     }
   }

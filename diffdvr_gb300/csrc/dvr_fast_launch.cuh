@@ -130,11 +130,11 @@ static cudaError_t build_gather_texture(const RenderParams& p, int bv, const Lau
   const int64_t per_row = std::min<int64_t>(int64_t(1) << shift, slabs);
   const int64_t W = per_row * tw, H = ((slabs + (int64_t(1) << shift) - 1) >> shift) * th;
   if (W > max_w || H > max_h) return cudaErrorNotSupported;
-  constexpr int bytes = sizeof(VT) == 4 ? 4 : 2;
+  using Texel = typename TexelFormat<VT>::T;
+  constexpr int bytes = int(sizeof(Texel));
   cudaArray_t array = nullptr;
-  err = acquire_gather_texture(li.device, s, int(W), int(H), bytes * 8, array, tg.tex);
+  err = acquire_gather_texture(li.device, s, int(W), int(H), TexelFormat<VT>::kind, array, tg.tex);
   if (err != cudaSuccess) return err;
-  using Texel = typename std::conditional<sizeof(VT) == 4, float, unsigned short>::type;
   auto* image = static_cast<Texel*>(acquire_scratch(li.device, s, size_t(W) * H * bytes, err, 1));
   if (!image) return err;
   // a block per tile column and 8 texel rows (one per warp)

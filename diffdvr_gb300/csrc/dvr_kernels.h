@@ -34,15 +34,17 @@ int* acquire_counter(int device, cudaStream_t s, cudaError_t& err);
 // Scratch memory of at least `bytes` for launches on stream s, owned by the
 // library and reused by later launches on the same stream (grown on demand;
 // growing synchronises the stream).  Not zeroed.  Slots are independent
-// buffers (0: ray order and TF-gradient slices, 1: cell-corner volume).
+// buffers (0: ray order and TF-gradient slices, 1: cell-corner volume or the
+// gather texture's staging image, 2: the adjoint's cell-corner gradient).
 void* acquire_scratch(int device, cudaStream_t s, size_t bytes, cudaError_t& err, int slot = 0);
 
-// A 2D CUDA array of W x H texels (bits = 16: unsigned 16-bit, 32: float)
-// created with the gather flag, and its texture object (point filtering,
-// clamped unnormalised coordinates, element reads), owned by the library and
-// reused by later launches on stream s while the size stays the same
-// (replacing it synchronises the stream).
-cudaError_t acquire_gather_texture(int device, cudaStream_t s, int W, int H, int bits, cudaArray_t& array,
+// A 2D CUDA array of W x H texels (format, TexelFormat of dvr_cells.cuh:
+// 0 float, 1 half, 2 unsigned 16-bit) created with the gather flag, and its
+// texture object (point filtering, clamped unnormalised coordinates, element
+// reads: half texels arrive as float), owned by the library and reused by
+// later launches on stream s while size and format stay the same (replacing
+// it synchronises the stream).
+cudaError_t acquire_gather_texture(int device, cudaStream_t s, int W, int H, int format, cudaArray_t& array,
                                    cudaTextureObject_t& tex);
 
 // Scratch handed in by the caller instead of the library's pools: `counter`
