@@ -27,7 +27,15 @@ and returns the errors the metric's gates are stated in:
   failing pixel is unexplained.
 * gradients: relative L2 error of each gradient against the FP64 adjoint on
   the same output adjoint (renderer/renderer_kernels.cuh:315-444), beside
-  the FP32 arithmetic's own.
+  the FP32 arithmetic's own.  Per-pixel ray gradients are also reported
+  over the well-conditioned pixels: those on which the FP32 arithmetic
+  itself stays within 1e-3 of FP64 (relative to the pixel's gradient, plus
+  1e-6 of the largest one), with the number of pixels left out.  A ray
+  whose sample lies within rounding of a cell boundary takes the trilinear
+  position derivative of one cell or the other (the derivative jumps
+  there, and the first sample sits on a box face), so on those few rays any
+  two FP32 implementations may each differ from FP64 by a whole sample's
+  derivative.
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s checker leg
 use this module.
@@ -53,6 +61,19 @@ def rel_l2(a, b) -> float:
     b = np.asarray(b, np.float64).ravel()
     nb = np.linalg.norm(b)
     return float(np.linalg.norm(a - b) / nb) if nb > 0 else float(np.linalg.norm(a - b))
+
+
+def _well_conditioned(got, g32, g64) -> dict:
+    """Relative L2 error of a per-pixel vector gradient (..., 3) over the
+    pixels where the FP32 arithmetic stays within 1e-3 of FP64 (see the
+    module docstring), and the number of pixels left out."""
+    got, g32, g64 = (np.asarray(x, np.float64).reshape(-1, 3) for x in (got, g32, g64))
+    n64 = np.linalg.norm(g64, axis=1)
+    e32 = np.linalg.norm(g32 - g64, axis=1)
+    ok = e32 <= 1e-3 * n64 + 1e-6 * (n64.max() if n64.size else 0.0)
+    return {"rel_l2_well_conditioned": rel_l2(got[ok], g64[ok]),
+            "rel_l2_f32_well_conditioned": rel_l2(g32[ok], g64[ok]),
+            "pixels_ill_conditioned": int((~ok).sum()), "pixels": int(ok.size)}
 
 
 def exit_ambiguity(scene: O.Scene):
@@ -133,6 +154,9 @@ def render_errors(scene: O.Scene, color: np.ndarray, term: np.ndarray, adj_color
         g32 = O.adjoint(scene, c32, t32, adj_color, req, "port", "f32")
         res["grad"] = {k: {"rel_l2": rel_l2(v, g64[k]), "rel_l2_f32": rel_l2(g32[k], g64[k])}
                        for k, v in grads.items()}
+        for k in ("adj_ray_start", "adj_ray_dir"):
+            if k in grads:
+                res["grad"][k].update(_well_conditioned(grads[k], g32[k], g64[k]))
         res["grad_rel_err"] = max(e["rel_l2"] for e in res["grad"].values())
         res["grad_rel_err_f32"] = max(e["rel_l2_f32"] for e in res["grad"].values())
     return res

@@ -220,3 +220,22 @@ def test_workloads_follow_their_configurations():
 
     p = scenes.preshaded_256(seed=1, res=16, views=2, image=8)
     assert p.volume.shape == (4, 16, 16, 16) and (p.tf_mode, p.filter_mode) == (5, 3)
+
+
+def test_ray_gradient_report_leaves_out_ill_conditioned_pixels():
+    """oracle.check's ray-gradient report: pixels where the FP32 arithmetic
+    is off by more than 1e-3 (here 3 of 500, a whole sample's derivative
+    apart) are left out of the well-conditioned figure and counted; the raw
+    figure keeps them."""
+    from oracle import check
+    rng = np.random.default_rng(4)
+    g64 = rng.normal(size=(1, 20, 25, 3))
+    g32 = g64 * (1 + 1e-6 * rng.normal(size=g64.shape))
+    got = g64 * (1 + 2e-6 * rng.normal(size=g64.shape))
+    for idx in [(0, 3, 4), (0, 10, 11), (0, 19, 0)]:
+        g32[idx] += 5.0
+        got[idx] -= 5.0
+    r = check._well_conditioned(got, g32, g64)
+    assert r["pixels"] == 500 and r["pixels_ill_conditioned"] == 3
+    assert r["rel_l2_well_conditioned"] < 1e-5 and r["rel_l2_f32_well_conditioned"] < 1e-5
+    assert check.rel_l2(got, g64) > 1e-2
