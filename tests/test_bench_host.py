@@ -222,20 +222,27 @@ def test_workloads_follow_their_configurations():
     assert p.volume.shape == (4, 16, 16, 16) and (p.tf_mode, p.filter_mode) == (5, 3)
 
 
-def test_ray_gradient_report_leaves_out_ill_conditioned_pixels():
-    """oracle.check's ray-gradient report: pixels where the FP32 arithmetic
-    is off by more than 1e-3 (here 3 of 500, a whole sample's derivative
-    apart) are left out of the well-conditioned figure and counted; the raw
-    figure keeps them."""
-    from oracle import check
+def test_ray_gradient_report_leaves_out_rounding_decided_rays():
+    """oracle.check's ray-gradient report: rays whose first sample lies on
+    the box face at the upper end of an axis (the cell there is decided by
+    rounding) are left out of the unambiguous-ray figure and counted; a ray
+    entering through a lower face is kept; the raw figure keeps them all."""
+    from oracle import check, oracle as O
+    starts = np.array([[2.0, 0.01, 0.02], [-2.0, 0.01, 0.02], [0.03, 2.0, -0.01], [0.02, 0.01, -2.0]])
+    dirs = np.array([[-1.0, 0, 0], [1.0, 0, 0], [0, -1.0, 0], [0, 0, 1.0]])
+    sc = O.Scene(width=4, height=1, volume=np.zeros((1, 9, 9, 9), np.float32), tf=np.zeros((1, 2, 2), np.float32),
+                 step_size=np.full((1, 1, 1), 0.3, np.float32), box_min=np.array([[-0.5, -0.5, -0.5]], np.float32),
+                 box_size=np.ones((1, 3), np.float32), filter_mode=1, tf_mode=0, blend_mode=0, camera_mode=0)
+    sc.ray_start = starts.reshape(1, 1, 4, 3).astype(np.float32)
+    sc.ray_dir = dirs.reshape(1, 1, 4, 3).astype(np.float32)
+    decided = check.rounding_decided_rays(sc)
+    assert decided.tolist() == [[[True, False, True, False]]]
     rng = np.random.default_rng(4)
-    g64 = rng.normal(size=(1, 20, 25, 3))
+    g64 = rng.normal(size=(1, 1, 4, 3))
     g32 = g64 * (1 + 1e-6 * rng.normal(size=g64.shape))
-    got = g64 * (1 + 2e-6 * rng.normal(size=g64.shape))
-    for idx in [(0, 3, 4), (0, 10, 11), (0, 19, 0)]:
-        g32[idx] += 5.0
-        got[idx] -= 5.0
-    r = check._well_conditioned(got, g32, g64)
-    assert r["pixels"] == 500 and r["pixels_ill_conditioned"] == 3
-    assert r["rel_l2_well_conditioned"] < 1e-5 and r["rel_l2_f32_well_conditioned"] < 1e-5
-    assert check.rel_l2(got, g64) > 1e-2
+    got = g64.copy()
+    got[0, 0, 0] += 5.0  # a whole sample's derivative apart on a decided ray
+    r = check._well_conditioned(got, g32, g64, decided)
+    assert r["rays"] == 4 and r["rays_left_out"] == 2
+    assert r["rel_l2_unambiguous_rays"] == 0.0 and r["rel_l2_f32_unambiguous_rays"] < 1e-5
+    assert check.rel_l2(got, g64) > 1e-1
