@@ -15,6 +15,9 @@
  * Citations are to files of the reference project (shamanDevel/DiffDVR).
  */
 #include <math.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 #include <stddef.h>
 #include <stdlib.h>
 #include <string.h>
@@ -603,6 +606,21 @@ static v3 rgba_adjoint(RgbaSampler* s, v4 adj) {
 }
 
 int oracle_real_size(void) { return (int)sizeof(real_t); }
+
+/* Threads of the parallel loops started from the calling thread from now on
+ * (the OpenMP runtime is shared by every library of the process, the
+ * reference's templates included); returns the previous number.  One thread
+ * makes the atomic sums of the adjoint deterministic. */
+int oracle_set_threads(int n) {
+#ifdef _OPENMP
+  const int prev = omp_get_max_threads();
+  if (n > 0) omp_set_num_threads(n);
+  return prev;
+#else
+  (void)n;
+  return 1;
+#endif
+}
 
 /* ---- forward march (renderer/renderer_kernels.cuh:22-90) ---- */
 int oracle_forward(const OracleInputs* in, OracleTensor* color, OracleTensor* termination) {

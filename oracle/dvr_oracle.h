@@ -109,6 +109,7 @@ int oracle_preshade_volume_adjoint(const OracleTensor* density, const OracleTens
 void oracle_set_exact_preshaded(int exact);
 /* Size of real_t in this build (4 or 8). */
 int oracle_real_size(void);
+int oracle_set_threads(int n);
 
 #ifdef DVR_ORACLE_HAS_REAL_T
 /* Port only: one step of each part of the march, as the march computes it,

@@ -210,6 +210,16 @@ def _dtype(lib) -> type:
     return np.float64 if lib.oracle_real_size() == 8 else np.float32
 
 
+def set_threads(n: int) -> int:
+    """Threads of the oracle's (and the reference templates') parallel loops
+    from now on; returns the previous number.  One thread makes the adjoint's
+    atomic sums deterministic."""
+    lib = load("port", "f64")
+    lib.oracle_set_threads.argtypes = [ctypes.c_int]
+    lib.oracle_set_threads.restype = ctypes.c_int
+    return int(lib.oracle_set_threads(int(n)))
+
+
 def forward(scene: Scene, kind: str = "port", precision: str = "f64"):
     """Returns (color B*H*W*4, termination_index B*H*W int32)."""
     lib = load(kind, precision)
