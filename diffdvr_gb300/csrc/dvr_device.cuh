@@ -342,9 +342,17 @@ __device__ __forceinline__ int linear_interval(const TfShared<5>& tf, float dens
 __device__ __forceinline__ float gauss(float d, float mu, float sigma) {
   return expf(-(d - mu) * (d - mu) / (2 * sigma * sigma));
 }
+// The same with one fast reciprocal and the fast exponential instead of a
+// division and expf (a few ulp apart): the optimized forward kernels' TF
+// evaluation.  Every adjoint keeps gauss.
+__device__ __forceinline__ float gauss_fast(float d, float mu, float sigma) {
+  const float z = (d - mu) * __fdividef(1.f, sigma);
+  return __expf(-0.5f * z * z);
+}
 
-// renderer/renderer_tf.cuh:62-73, :160-171, :294-313, :507-519
-template <int TF, class A>
+// renderer/renderer_tf.cuh:62-73, :160-171, :294-313, :507-519.  FAST: the
+// Gaussians by gauss_fast (the optimized forward kernels).
+template <int TF, bool FAST = false, class A>
 __device__ __forceinline__ f4 tf_eval(const A& tf, float density) {
   if constexpr (TF == kTfIdentity) {
     const float d = clampf(density, 0.f, 1.f);
@@ -370,7 +378,7 @@ __device__ __forceinline__ f4 tf_eval(const A& tf, float density) {
     f4 acc = mk4(0, 0, 0, 0);
     for (int i = 0; i < tf.R; ++i) {
       const f4 ci = tf.rgba(i);
-      const float ni = gauss(density, tf.at(i, 4), tf.at(i, 5));
+      const float ni = FAST ? gauss_fast(density, tf.at(i, 4), tf.at(i, 5)) : gauss(density, tf.at(i, 4), tf.at(i, 5));
       acc.x += ci.x * ni;
       acc.y += ci.y * ni;
       acc.z += ci.z * ni;

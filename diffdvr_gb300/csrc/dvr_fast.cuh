@@ -225,7 +225,7 @@ __device__ __forceinline__ void fast_forward_tile(const RenderParams& p, int b, 
     }
     const float density = smp.sample(vol, fast_pos(r, t));
     if (rec) rec[k] = make_float2(density, acc.w);
-    acc = blend<BLEND>(acc, tf_eval<TF>(tf, density), r.step);
+    acc = blend<BLEND>(acc, tf_eval<TF, true>(tf, density), r.step);
   }
   float* col = static_cast<float*>(p.color.p) + b * p.color.s[0] + y * p.color.s[1] + x * p.color.s[2];
   col[0] = acc.x;

@@ -64,7 +64,7 @@ __device__ __forceinline__ void warp_march_ray(const RenderParams& p, int b, int
     f4 c = mk4(0, 0, 0, 0);
     if (in_ray) {
       density = sample(fast_pos(q, t));
-      c = tf_eval<TF>(tf, density);
+      c = tf_eval<TF, true>(tf, density);
       a = blend_alpha<BLEND>(c.w, q.step);
     }
     // incoming opacity of each sample: exclusive "over" scan
