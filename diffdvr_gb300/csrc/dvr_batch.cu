@@ -92,6 +92,7 @@ struct GatherTextureSlot {
   int W = 0, H = 0, format = -1;
   cudaArray_t array = nullptr;
   cudaTextureObject_t tex = 0;
+  cudaSurfaceObject_t surf = 0;  // 0 when the array could not take surface stores
 };
 std::mutex g_texture_mutex;
 std::vector<GatherTextureSlot> g_textures;
@@ -126,7 +127,7 @@ void* acquire_scratch(int device, cudaStream_t s, size_t bytes, cudaError_t& err
 }
 
 cudaError_t acquire_gather_texture(int device, cudaStream_t s, int W, int H, int format, cudaArray_t& array,
-                                   cudaTextureObject_t& tex) {
+                                   cudaTextureObject_t& tex, cudaSurfaceObject_t& surf) {
   std::lock_guard<std::mutex> lock(g_texture_mutex);
   GatherTextureSlot* slot = nullptr;
   for (auto& e : g_textures)
@@ -140,16 +141,28 @@ cudaError_t acquire_gather_texture(int device, cudaStream_t s, int W, int H, int
     const cudaError_t err = cudaStreamSynchronize(s);
     if (err != cudaSuccess) return err;
     cudaDestroyTextureObject(slot->tex);
+    if (slot->surf) cudaDestroySurfaceObject(slot->surf);
     cudaFreeArray(slot->array);
     slot->array = nullptr;
     slot->tex = 0;
+    slot->surf = 0;
   }
   if (!slot->array) {
     // texel formats of TexelFormat (dvr_cells.cuh): 0 float, 1 half, 2 raw 16-bit
     const cudaChannelFormatDesc desc = format == 0   ? cudaCreateChannelDesc<float>()
                                        : format == 1 ? cudaCreateChannelDescHalf()
                                                      : cudaCreateChannelDesc<unsigned short>();
-    cudaError_t err = cudaMallocArray(&slot->array, &desc, size_t(W), size_t(H), cudaArrayTextureGather);
+    // with surface stores the slab image is written into the array
+    // directly; where gather and surface flags do not combine, through a
+    // staging image and a copy
+    bool surface = true;
+    cudaError_t err = cudaMallocArray(&slot->array, &desc, size_t(W), size_t(H),
+                                      cudaArrayTextureGather | cudaArraySurfaceLoadStore);
+    if (err != cudaSuccess) {
+      (void)cudaGetLastError();  // the refused combination is not an error of the call
+      surface = false;
+      err = cudaMallocArray(&slot->array, &desc, size_t(W), size_t(H), cudaArrayTextureGather);
+    }
     if (err != cudaSuccess) {
       slot->array = nullptr;
       return err;
@@ -157,6 +170,10 @@ cudaError_t acquire_gather_texture(int device, cudaStream_t s, int W, int H, int
     cudaResourceDesc res{};
     res.resType = cudaResourceTypeArray;
     res.res.array.array = slot->array;
+    if (surface && cudaCreateSurfaceObject(&slot->surf, &res) != cudaSuccess) {
+      (void)cudaGetLastError();
+      slot->surf = 0;
+    }
     cudaTextureDesc td{};
     td.addressMode[0] = td.addressMode[1] = cudaAddressModeClamp;
     td.filterMode = cudaFilterModePoint;
@@ -164,9 +181,11 @@ cudaError_t acquire_gather_texture(int device, cudaStream_t s, int W, int H, int
     td.normalizedCoords = 0;
     err = cudaCreateTextureObject(&slot->tex, &res, &td, nullptr);
     if (err != cudaSuccess) {
+      if (slot->surf) cudaDestroySurfaceObject(slot->surf);
       cudaFreeArray(slot->array);
       slot->array = nullptr;
       slot->tex = 0;
+      slot->surf = 0;
       return err;
     }
     slot->W = W;
@@ -175,6 +194,7 @@ cudaError_t acquire_gather_texture(int device, cudaStream_t s, int W, int H, int
   }
   array = slot->array;
   tex = slot->tex;
+  surf = slot->surf;
   return cudaSuccess;
 }
 

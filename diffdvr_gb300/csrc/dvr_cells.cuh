@@ -226,15 +226,13 @@ struct AdjVolume {
   }
 };
 
-// Writes the tiled, aproned slab image (W x H texels, row-major, pitch W)
-// that is then copied into the gather texture's array: one warp per texel row
+// The texel (u, v) of the tiled, aproned slab image: one warp per texel row
 // of one tile (blockIdx.x = tile column, warps over texel rows), lanes along
 // z, so the row's index arithmetic is done once per warp and the volume reads
-// and image writes of a warp are contiguous.  Texels of tiles past the last
-// slab are zero.
-template <typename VT>
-__global__ void build_gather_image_kernel(const RenderParams p, int bv, int tshift, int W, int H,
-                                          typename TexelFormat<VT>::T* out) {
+// and texel writes of a warp are contiguous.  Texels of tiles past the last
+// slab are zero.  put(u, v, texel) stores one texel.
+template <typename VT, class Put>
+__device__ __forceinline__ void gather_image_rows(const RenderParams& p, int bv, int tshift, int H, Put put) {
   using Texel = typename TexelFormat<VT>::T;
   const int X = p.X, Y = p.Y, Z = p.Z, tw = Z + 2, th = Y + 2;
   const int lane = threadIdx.x & 31;
@@ -243,9 +241,9 @@ __global__ void build_gather_image_kernel(const RenderParams p, int bv, int tshi
   for (int v = blockIdx.y * (blockDim.x >> 5) + (threadIdx.x >> 5); v < H; v += gridDim.y * (blockDim.x >> 5)) {
     const int tr = v / th;
     const int64_t s = (int64_t(tr) << tshift) + tc;
-    Texel* row = out + int64_t(v) * W + int64_t(tc) * tw;
+    const int u0 = tc * tw;
     if (s >= slabs) {
-      for (int u = lane; u < tw; u += 32) row[u] = 0;
+      for (int u = lane; u < tw; u += 32) put(u0 + u, v, Texel(0));
       continue;
     }
     const int b = int(s / X), x = int(s - int64_t(b) * X);
@@ -254,10 +252,30 @@ __global__ void build_gather_image_kernel(const RenderParams p, int bv, int tshi
     const int64_t sz = p.volume.s[3];
     for (int u = lane; u < tw; u += 32) {
       const VT e = src[min(max(u - 1, 0), Z - 1) * sz];
-      if constexpr (TexelFormat<VT>::kind == kTexelF32) row[u] = float(e);
-      else row[u] = raw16(e);
+      if constexpr (TexelFormat<VT>::kind == kTexelF32) put(u0 + u, v, Texel(float(e)));
+      else put(u0 + u, v, Texel(raw16(e)));
     }
   }
+}
+
+// The slab image written to memory (W x H texels, row-major, pitch W), then
+// copied into the texture's array.
+template <typename VT>
+__global__ void build_gather_image_kernel(const RenderParams p, int bv, int tshift, int W, int H,
+                                          typename TexelFormat<VT>::T* out) {
+  using Texel = typename TexelFormat<VT>::T;
+  gather_image_rows<VT>(p, bv, tshift, H, [&](int u, int v, Texel t) { out[int64_t(v) * W + u] = t; });
+}
+
+// The slab image written straight into the texture's array by surface
+// stores (u < W and v < H by construction; stores outside would be dropped).
+template <typename VT>
+__global__ void build_gather_surface_kernel(const RenderParams p, int bv, int tshift, int H,
+                                            cudaSurfaceObject_t surf) {
+  using Texel = typename TexelFormat<VT>::T;
+  gather_image_rows<VT>(p, bv, tshift, H, [&](int u, int v, Texel t) {
+    surf2Dwrite<Texel>(t, surf, u * int(sizeof(Texel)), v, cudaBoundaryModeZero);
+  });
 }
 
 }  // namespace dvr

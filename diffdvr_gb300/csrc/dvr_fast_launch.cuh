@@ -133,18 +133,25 @@ static cudaError_t build_gather_texture(const RenderParams& p, int bv, const Lau
   using Texel = typename TexelFormat<VT>::T;
   constexpr int bytes = int(sizeof(Texel));
   cudaArray_t array = nullptr;
-  err = acquire_gather_texture(li.device, s, int(W), int(H), TexelFormat<VT>::kind, array, tg.tex);
+  cudaSurfaceObject_t surf = 0;
+  err = acquire_gather_texture(li.device, s, int(W), int(H), TexelFormat<VT>::kind, array, tg.tex, surf);
   if (err != cudaSuccess) return err;
-  auto* image = static_cast<Texel*>(acquire_scratch(li.device, s, size_t(W) * H * bytes, err, 1));
-  if (!image) return err;
   // a block per tile column and 8 texel rows (one per warp)
   const dim3 grid(unsigned(per_row), unsigned(std::min<int64_t>((H + 7) / 8, 65535)));
-  build_gather_image_kernel<VT><<<grid, 256, 0, s>>>(p, bv, shift, int(W), int(H), image);
-  err = cudaGetLastError();
-  if (err != cudaSuccess) return err;
-  err = cudaMemcpy2DToArrayAsync(array, 0, 0, image, size_t(W) * bytes, size_t(W) * bytes, size_t(H),
-                                 cudaMemcpyDeviceToDevice, s);
-  if (err != cudaSuccess) return err;
+  if (surf) {
+    build_gather_surface_kernel<VT><<<grid, 256, 0, s>>>(p, bv, shift, int(H), surf);
+    err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+  } else {
+    auto* image = static_cast<Texel*>(acquire_scratch(li.device, s, size_t(W) * H * bytes, err, 1));
+    if (!image) return err;
+    build_gather_image_kernel<VT><<<grid, 256, 0, s>>>(p, bv, shift, int(W), int(H), image);
+    err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+    err = cudaMemcpy2DToArrayAsync(array, 0, 0, image, size_t(W) * bytes, size_t(W) * bytes, size_t(H),
+                                   cudaMemcpyDeviceToDevice, s);
+    if (err != cudaSuccess) return err;
+  }
   tg.tshift = shift;
   tg.tw = int(tw);
   tg.th = int(th);

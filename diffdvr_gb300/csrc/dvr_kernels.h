@@ -41,11 +41,12 @@ void* acquire_scratch(int device, cudaStream_t s, size_t bytes, cudaError_t& err
 // A 2D CUDA array of W x H texels (format, TexelFormat of dvr_cells.cuh:
 // 0 float, 1 half, 2 unsigned 16-bit) created with the gather flag, and its
 // texture object (point filtering, clamped unnormalised coordinates, element
-// reads: half texels arrive as float), owned by the library and reused by
-// later launches on stream s while size and format stay the same (replacing
-// it synchronises the stream).
+// reads: half texels arrive as float) and, where the array takes surface
+// stores as well, its surface object (else surf = 0), owned by the library
+// and reused by later launches on stream s while size and format stay the
+// same (replacing it synchronises the stream).
 cudaError_t acquire_gather_texture(int device, cudaStream_t s, int W, int H, int format, cudaArray_t& array,
-                                   cudaTextureObject_t& tex);
+                                   cudaTextureObject_t& tex, cudaSurfaceObject_t& surf);
 
 // Scratch handed in by the caller instead of the library's pools: `counter`
 // (one int, zeroed here on the stream before each launch) and `tf` (TF-gradient
