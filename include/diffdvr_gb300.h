@@ -185,7 +185,7 @@ typedef struct DvrAdjointOutputs {
  * renderer/renderer.cpp:393-417).
  * Library scratch: the optimized family takes work counters and, per
  * stream, a ray-order buffer (and, for trilinear filtering, the cell-corner
- * volume or the slab gather texture with its staging image) from pools that
+ * volume or the slab gather texture) from pools that
  * it grows with cudaMalloc when a call needs more than they hold;
  * dvr_render_adjoint does the same for its ray order, TF-gradient slices,
  * the gather texture of the rays it marches again and the cell-corner
