@@ -212,6 +212,36 @@ def make_workload(args):
     return scenes.tf_reconstruction_256(seed=1, res=args.res, views=args.views, image=args.image)
 
 
+def l2_copy_peak(dev) -> dict:
+    """Copy bandwidth inside L2, measured live: a 12 MB float buffer copied
+    into another (24 MB of L2-resident traffic per copy, read + write), 200
+    copies after 20 warm-up ones, CUDA events on the current stream.  The
+    denominator of the gather model (per-sample corner bytes served from the
+    caches)."""
+    import torch
+    n = 3 * 1024 * 1024
+    a = torch.rand(n, device=dev)
+    b = torch.empty_like(a)
+    for _ in range(20):
+        b.copy_(a)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(200):
+        b.copy_(a)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / 200
+    return {"GBps": 2 * n * 4 / (ms * 1e-3) / 1e9, "how": "torch copy of a 12 MB float buffer, 200 times, CUDA events"}
+
+
+def gather_model(gather_bytes: float, ms: float, l2: dict) -> dict:
+    """The gather model's bytes per second (every sample's corners, no
+    reuse assumed) against the measured L2 copy bandwidth."""
+    achieved = gather_bytes / (ms / 1e3) / 1e9
+    return {"achieved_GBps": achieved, "l2_peak_GBps": l2["GBps"], "frac": achieved / l2["GBps"],
+            "l2_peak_how": l2["how"], "bytes_per_step": int(gather_bytes)}
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -842,6 +872,7 @@ def run_gpu(args):
                      "with_record": {"bytes_per_launch": int(dominant[1]), "achieved": achieved_rec,
                                      "frac": achieved_rec / peak},
                      "gather_model_GBps": gather_bytes / ((fwd_ms + adj_ms) / 1e3) / 1e9,
+                     "gather_model": gather_model(gather_bytes, fwd_ms + adj_ms, l2_copy_peak(dev)),
                      "issue": issue_bound(args.workload, dominant[0], samples, dominant[2])},
         "plain_fp32": plain,
         "speedup_vs_plain_fp32": (value / plain["samples_per_s"]) if plain else None,
@@ -1139,7 +1170,8 @@ def run_gpu_batched(args):
         "roofline": {"bound": "hbm", "kernel": dominant[0], "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_launch": int(dominant[1]),
-                     "gather_model_GBps": samples * 8 * s_v * 2 / ((fwd_ms + adj_ms) / 1e3) / 1e9},
+                     "gather_model_GBps": samples * 8 * s_v * 2 / ((fwd_ms + adj_ms) / 1e3) / 1e9,
+                     "gather_model": gather_model(samples * 8 * s_v * 2, fwd_ms + adj_ms, l2_copy_peak(dev))},
         "clocks": clock_summary,
     }
     if rank == 0:

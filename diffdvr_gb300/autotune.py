@@ -17,7 +17,9 @@ searches the shapes of every class of a batch in the batched call itself:
 starting from 16x8 everywhere, it tries each other shape for one class at a
 time in the full forward and the full adjoint launch (CUDA events on the
 current stream, warm-up, median of repeats, on scratch outputs so the
-caller's outputs and gradients are untouched) and keeps a shape only when it
+caller's outputs and gradients are untouched; the scratch outputs carry
+checkpoints and a sample record where the caller's do, so the adjoint is
+timed on the path the caller's call takes) and keeps a shape only when it
 beats the current choice by more than the noise margin.  Choices are cached
 per device name and class in a JSON file, so later batches and later
 processes reuse them without timing.
@@ -163,9 +165,13 @@ class TileTuner:
                                    (int(inp.volume_filter_mode), int(inp.tf_mode), int(inp.blend_mode)), storage,
                                    grads))
         classes = sorted(set(keys))
+        # scratch outputs of the same kind as the caller's: with a sample
+        # record of their own where the caller's carry one, so the adjoint is
+        # timed on the path (record or re-march) that the caller's call takes
+        like = lambda o, name: None if getattr(o, name, None) is None else torch.empty_like(getattr(o, name))
         scratch_out = [pr.RendererOutputs(torch.empty_like(o.color), torch.empty_like(o.terminationIndex),
-                                          None if o.checkpoints is None else torch.empty_like(o.checkpoints),
-                                          o.checkpoint_interval) for o in outputs]
+                                          like(o, "checkpoints"), o.checkpoint_interval,
+                                          like(o, "sample_density"), like(o, "sample_offset")) for o in outputs]
         scratch_adj = []
         for a in adj_outputs:
             sa = pr.AdjointOutputs()

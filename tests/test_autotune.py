@@ -81,7 +81,8 @@ def test_unreadable_cache_is_ignored(tmp_path):
 
 
 @pytest.mark.gpu
-def test_tuned_batched_calls_match_default_tiles(cuda_device, tmp_path):
+@pytest.mark.parametrize("record", [False, True])
+def test_tuned_batched_calls_match_default_tiles(cuda_device, tmp_path, record):
     import torch
     from diffdvr_gb300 import pyrenderer as pr
     from dvr_cases import make_case, rel_l2
@@ -96,6 +97,9 @@ def test_tuned_batched_calls_match_default_tiles(cuda_device, tmp_path):
         ins.append(inp)
         outs.append(pr.RendererOutputs(torch.empty(1, c.height, c.width, 4, device="cuda"),
                                        torch.empty(1, c.height, c.width, dtype=torch.int32, device="cuda"), ck, 16))
+        if record:  # the forward's sample record: the adjoint reads it instead of re-marching
+            outs[-1].sample_density = torch.empty(pr.Renderer.sample_density_size(inp, 1), device="cuda")
+            outs[-1].sample_offset = torch.empty(1, c.height, c.width, dtype=torch.int32, device="cuda")
         adjs.append(torch.from_numpy(rng.normal(size=(1, c.height, c.width, 4)).astype(np.float32)).cuda())
         a = pr.AdjointOutputs()
         a.has_tf_derivatives = True
@@ -104,8 +108,11 @@ def test_tuned_batched_calls_match_default_tiles(cuda_device, tmp_path):
         a.adj_volume = torch.zeros(c.volume.shape, device="cuda")
         aos.append(a)
     pr.Renderer.render_forward_batched(ins, outs)
+    kept = [o.sample_offset.clone() for o in outs] if record else []
     tuner = T.TileTuner(cache_path=str(tmp_path / "tiles.json"), warmup=1, repeats=3)
     fs, as_ = tuner.tune(ins, outs, adjs, aos, storage="f32")
+    # the tuner ran on scratch outputs (with a record of their own) and left the caller's record alone
+    assert all(torch.equal(k, o.sample_offset) for k, o in zip(kept, outs))
     assert tuner.timed and len(fs) == len(as_) == 3 and all(s in T.SHAPES for s in fs + as_)
     assert fs[0] == fs[2] and as_[0] == as_[2]  # one size class
     # the tuner's runs did not touch the caller's gradients

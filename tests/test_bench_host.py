@@ -246,3 +246,11 @@ def test_ray_gradient_report_leaves_out_rounding_decided_rays():
     assert r["rays"] == 4 and r["rays_left_out"] == 2
     assert r["rel_l2_unambiguous_rays"] == 0.0 and r["rel_l2_f32_unambiguous_rays"] < 1e-5
     assert check.rel_l2(got, g64) > 1e-1
+
+
+def test_gather_model_against_the_l2_peak():
+    """The gather model's bytes per second and its fraction of the measured
+    L2 copy bandwidth."""
+    g = bench.gather_model(1e9, 1.0, {"GBps": 2000.0, "how": "test"})
+    assert g["achieved_GBps"] == pytest.approx(1000.0) and g["frac"] == pytest.approx(0.5)
+    assert g["bytes_per_step"] == 10**9 and g["l2_peak_GBps"] == 2000.0
