@@ -1,18 +1,20 @@
 // Forward march with one warp per ray.
 //
-// The 32 lanes of a warp take 32 consecutive samples of the same ray at once:
-// each lane gathers its sample's density and evaluates the TF, then the warp
-// composites the 32 samples front to back.  Compositing is associative (the
-// "over" operator: opacity a then b gives a + (1 - a) b, colour likewise), so
-// a 5-step warp scan gives every sample's incoming opacity, from which follow
-// the early-termination point (the first sample whose incoming opacity
-// exceeds blendingEarlyOut, renderer/renderer_kernels.cuh:55-58), each
-// sample's colour contribution (1 - incoming opacity) a c (summed per lane,
-// then over the warp at the end of the ray) and the transmittance checkpoints.  The per-sample arithmetic is the
-// reference's (renderer/renderer_blending.cuh:30-49); only the order of the
-// compositing sums differs, by rounding.
+// The 32 lanes of a warp take 64 consecutive samples of the same ray at once,
+// two adjacent ones per lane: each lane gathers its samples' densities and
+// evaluates the TF, then the warp composites the 64 samples front to back.
+// Compositing is associative (the "over" operator: opacity a then b gives
+// a + (1 - a) b, colour likewise), so a 5-step warp scan over the lanes'
+// pairs gives every sample's incoming opacity, from which follow the
+// early-termination point (the first sample whose incoming opacity exceeds
+// blendingEarlyOut, renderer/renderer_kernels.cuh:55-58), each sample's
+// colour contribution (1 - incoming opacity) a c (summed per lane, then over
+// the warp at the end of the ray) and the transmittance checkpoints.  The
+// per-sample arithmetic is the reference's
+// (renderer/renderer_blending.cuh:30-49); only the order of the compositing
+// sums differs, by rounding.
 //
-// All 32 gathers of a step are independent and issued together, lanes never
+// All 64 gathers of a step are independent and issued together, lanes never
 // diverge on cell or termination events, and a lane keeps no per-ray state,
 // so registers are few and many warps fit per SM.  Warps fetch one ray at a
 // time from the longest-first order of the rays with samples.
@@ -40,12 +42,19 @@ __device__ __forceinline__ float over(float a, float b) { return a + (1.f - a) *
 // How a trilinear sample reads its eight corners.
 enum { kGatherDirect = 0, kGatherCells = 1, kGatherTexture = 2 };
 
-// Marches ray (b, x, y) with the 32 lanes of the calling warp, 32
-// consecutive samples per step: writes its colour and termination index,
-// and per sample the (density, incoming opacity) pair to rec (when not
+// Marches ray (b, x, y) with the 32 lanes of the calling warp, 64
+// consecutive samples per step, two adjacent ones per lane (lane l takes
+// samples 2l and 2l + 1 of the step): writes its colour and termination
+// index, and per sample the (density, incoming opacity) pair to rec (when not
 // nullptr) or the opacity before every K-th sample to the checkpoints ck
 // (when not nullptr).  sample(float3 q) returns the density at volume
 // position q.  Every lane of the warp calls it with the same ray.
+//
+// Two samples per lane halve the scan, ballot and loop work per sample, put
+// four independent texture gathers (or sixteen corner loads) of a lane in
+// flight at once, and store a lane's two record entries as one 16-byte
+// store.  A ray that terminates early computes at most 63 samples past its
+// end, against 31 with one sample per lane.
 template <int TF, int BLEND, class Sample>
 __device__ __forceinline__ void warp_march_ray(const RenderParams& p, int b, int x, int y, const FastRay& q,
                                                int kmax, const TfShared<TfChannels<TF>::C>& tf, float* rec,
@@ -53,22 +62,35 @@ __device__ __forceinline__ void warp_march_ray(const RenderParams& p, int b, int
   const int lane = threadIdx.x & 31;
   const int K = p.ckpt_interval;
   const int kshift = (K & (K - 1)) == 0 ? __ffs(K) - 1 : -1;  // log2 K for a power-of-two interval
-  float alpha = 0.f;  // accumulated opacity before the chunk
+  // sample 0 lies in the volume whenever the ray has samples: lanes whose
+  // samples are past the ray's end gather there, so every lane issues its
+  // gathers unconditionally and the result is discarded
+  const bool has = kmax > 0 && !(q.tmin > q.tmax);
+  float alpha = 0.f;  // accumulated opacity before the step
   float cr = 0.f, cg = 0.f, cb = 0.f;  // this lane's samples' colour contributions
   int n = 0;
-  for (int k0 = 0;; k0 += 32) {
-    const int k = k0 + lane;
-    const float t = q.tmin + k * q.step;
-    const bool in_ray = k < kmax && !(t > q.tmax);
-    float density = 0.f, a = 0.f;
-    f4 c = mk4(0, 0, 0, 0);
-    if (in_ray) {
-      density = sample(fast_pos(q, t));
-      c = tf_eval<TF, true>(tf, density);
-      a = blend_alpha<BLEND>(c.w, q.step);
+  for (int k0 = 0;; k0 += 64) {
+    const int k = k0 + 2 * lane;  // the lane's samples k and k + 1
+    float density[2] = {0.f, 0.f}, a[2] = {0.f, 0.f};
+    f4 c[2] = {mk4(0, 0, 0, 0), mk4(0, 0, 0, 0)};
+    bool in_ray[2];
+#pragma unroll
+    for (int i = 0; i < 2; ++i) in_ray[i] = k + i < kmax && !(q.tmin + (k + i) * q.step > q.tmax);
+    if (has) {
+      float d[2];
+#pragma unroll
+      for (int i = 0; i < 2; ++i) d[i] = sample(fast_pos(q, q.tmin + (in_ray[i] ? k + i : 0) * q.step));
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        if (in_ray[i]) {
+          density[i] = d[i];
+          c[i] = tf_eval<TF, true>(tf, d[i]);
+          a[i] = blend_alpha<BLEND>(c[i].w, q.step);
+        }
+      }
     }
-    // incoming opacity of each sample: exclusive "over" scan
-    float incl = a;
+    // incoming opacity of each pair: exclusive "over" scan of the lanes' pairs
+    float incl = over(a[0], a[1]);
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const float v = __shfl_up_sync(kFullMask, incl, o);
@@ -76,27 +98,43 @@ __device__ __forceinline__ void warp_march_ray(const RenderParams& p, int b, int
     }
     float excl = __shfl_up_sync(kFullMask, incl, 1);
     if (lane == 0) excl = 0.f;
-    const float a_in = over(alpha, excl);
-    const bool go = in_ray && !(a_in > p.early_out);
-    const unsigned gm = __ballot_sync(kFullMask, go);
-    const int f = gm == kFullMask ? 32 : __ffs(~gm) - 1;  // first sample not taken
-    const bool used = lane < f;
-    if (used) {
-      if (rec) __stcs(reinterpret_cast<float2*>(rec) + k, make_float2(density, a_in));
-      if (ck && k > 0) {
-        // opacity before sample (slot + 1) * K
-        const bool at = kshift >= 0 ? (k & (K - 1)) == 0 : k % K == 0;
-        const int slot = (kshift >= 0 ? k >> kshift : k / K) - 1;
-        if (at && slot < p.ckpt_slots) ck[slot * p.ckpt.s[3]] = a_in;
-      }
-      const float w = (1.f - a_in) * a;
-      const float2 rg = __ffma2_rn(make_float2(w, w), make_float2(c.x, c.y), make_float2(cr, cg));
-      cr = rg.x;
-      cg = rg.y;
-      cb = fmaf(w, c.z, cb);
+    float a_in[2];
+    a_in[0] = over(alpha, excl);
+    a_in[1] = over(a_in[0], a[0]);
+    // first sample of the step not taken: past the ray's end or behind the
+    // early-termination opacity
+    const unsigned m0 = __ballot_sync(kFullMask, in_ray[0] && !(a_in[0] > p.early_out));
+    const unsigned m1 = __ballot_sync(kFullMask, in_ray[1] && !(a_in[1] > p.early_out));
+    const int f = min(m0 == kFullMask ? 64 : 2 * (__ffs(~m0) - 1), m1 == kFullMask ? 64 : 2 * __ffs(~m1) - 1);
+    const bool used0 = 2 * lane < f, used1 = 2 * lane + 1 < f;
+    if (rec) {
+      if (used1) __stcs(reinterpret_cast<float4*>(rec + 2 * k), make_float4(density[0], a_in[0], density[1], a_in[1]));
+      else if (used0) __stcs(reinterpret_cast<float2*>(rec) + k, make_float2(density[0], a_in[0]));
     }
-    if (f < 32) {
-      alpha = __shfl_sync(kFullMask, a_in, f);
+    if (ck) {
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const int ki = k + i;
+        if ((i == 0 ? used0 : used1) && ki > 0) {
+          // opacity before sample (slot + 1) * K
+          const bool at = kshift >= 0 ? (ki & (K - 1)) == 0 : ki % K == 0;
+          const int slot = (kshift >= 0 ? ki >> kshift : ki / K) - 1;
+          if (at && slot < p.ckpt_slots) ck[slot * p.ckpt.s[3]] = a_in[i];
+        }
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      if (i == 0 ? used0 : used1) {
+        const float w = (1.f - a_in[i]) * a[i];
+        const float2 rg = __ffma2_rn(make_float2(w, w), make_float2(c[i].x, c[i].y), make_float2(cr, cg));
+        cr = rg.x;
+        cg = rg.y;
+        cb = fmaf(w, c[i].z, cb);
+      }
+    }
+    if (f < 64) {
+      alpha = __shfl_sync(kFullMask, (f & 1) ? a_in[1] : a_in[0], f >> 1);
       n = k0 + f;
       break;
     }
