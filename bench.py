@@ -779,12 +779,15 @@ def run_gpu(args):
                 flush.zero_()
                 ck_step(record=True)
             torch.cuda.synchronize()
+            ck_path = pr.last_adjoint_path()
         checkpoint_only = {
             "samples_per_s": samples / (ms_ck / 1e3), "ms_per_step": ms_ck,
             "forward_ms": float(np.mean([a_.elapsed_time(b_) for a_, b_ in fwd_ev])),
             "adjoint_ms": float(np.mean([a_.elapsed_time(b_) for a_, b_ in adj_ev])),
             "checkpoint_interval": K, "checkpoint_MB": round(ckpt.numel() * 4 / 1e6, 1),
-            "path": "no sample record; the general adjoint re-marches each K-sample segment from its checkpoint"}
+            "adjoint_path": ck_path,
+            "path": "no sample record; the adjoint re-marches from the checkpoints (remarch: each warp re-marches its "
+                    "ray in chunks of up to 512 samples into shared memory; general: per-ray K-sample segments)"}
 
     # ---- aggregate over ranks (max time)
     ms_graph, ms_e2e = max_over_ranks([ms_graph, ms_e2e], world, dev)

@@ -154,7 +154,7 @@ SIGNATURES = {
 
 # DvrAdjointPath
 FORWARD_GATHERS = {"auto": 0, "direct": 1, "cells": 2, "texture": 3}
-ADJOINT_PATHS = {0: "none", 1: "plain", 2: "general", 3: "record", 4: "window", 5: "preshaded"}
+ADJOINT_PATHS = {0: "none", 1: "plain", 2: "general", 3: "record", 4: "window", 5: "preshaded", 6: "remarch"}
 
 _LIB = None
 ABI_VERSION = 6

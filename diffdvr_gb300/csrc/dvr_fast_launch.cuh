@@ -273,6 +273,63 @@ static cudaError_t fast_adjoint_record_go(const RenderParams& p, const AdjointPa
   return cudaGetLastError();
 }
 
+// TF-gradient-only adjoint of a texture TF from the checkpoints alone (no
+// sample record): longest-first order, the re-march kernel (chunks
+// re-marched from their checkpoints into shared memory, through the slab
+// gather texture where the forward would use it), then the general kernel
+// over the rays the checkpoints do not cover.
+template <int FILTER, int BLEND, typename VT>
+static cudaError_t fast_adjoint_remarch_go(const RenderParams& p, const AdjointParams& a, const RayOrder& order,
+                                           int* counter, int chunk, size_t rsmem, size_t gsmem, const LaunchInfo& li,
+                                           cudaStream_t s) {
+  constexpr int C = 4;
+  const int64_t total = order.total();
+  TexGather tg{};
+  if (FILTER == kTrilinear && texture_gather_wanted<VT>(p)) {
+    cudaError_t e = build_gather_texture<VT>(p, volume_entries(p), li, s, tg);
+    if (e == cudaErrorNotSupported) tg = TexGather{};
+    else if (e != cudaSuccess) return e;
+  }
+  auto go = [&](auto rem) {
+    auto gen = fast_adjoint_persistent_kernel<FILTER, kTfTexture, BLEND, false, true, VT>;
+    cudaError_t e = set_smem(rem, rsmem);
+    if (e != cudaSuccess) return e;
+    e = set_smem(gen, gsmem);
+    if (e != cudaSuccess) return e;
+    const int rgrid = persistent_grid(rem, rsmem, total * 32, li);  // one warp per ray
+    const int ggrid = li.num_sms;
+    // scratch: order ints, leftover list, the general kernel's TF-gradient slices, the
+    // re-march kernel's per-warp slices
+    const size_t order_bytes = (work_order_ints(p) * sizeof(int) + 255) & ~size_t(255);
+    const size_t left_bytes = (size_t(total) * sizeof(int) + 255) & ~size_t(255);
+    const size_t tf_bytes = (size_t(ggrid) * p.R * C * sizeof(float) + 255) & ~size_t(255);
+    const size_t slice_bytes = size_t(rgrid) * (kFastThreads / 32) * p.R * C * sizeof(float);
+    char* scratch =
+        static_cast<char*>(acquire_scratch(li.device, s, order_bytes + left_bytes + tf_bytes + slice_bytes, e));
+    if (!scratch) return e;
+    int* order_ints = reinterpret_cast<int*>(scratch);
+    int* leftover = reinterpret_cast<int*>(scratch + order_bytes);
+    e = order_rays_by_work(p, &a, order_ints, li, s);
+    if (e != cudaSuccess) return e;
+    rem<<<rgrid, kFastThreads, rsmem, s>>>(p, a, order, counter, order_ints + work_order_list_offset,
+                                           order_ints + work_order_count_offset, leftover,
+                                           reinterpret_cast<float*>(scratch + order_bytes + left_bytes + tf_bytes),
+                                           tg, chunk);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    int* counter2 = acquire_counter(li.device, s, e);
+    if (!counter2) return e;
+    gen<<<ggrid, kFastThreads, gsmem, s>>>(p, a, order, counter2,
+                                           reinterpret_cast<float*>(scratch + order_bytes + left_bytes), leftover,
+                                           counter + 1, TexGather{});
+    return cudaGetLastError();
+  };
+  if constexpr (FILTER == kTrilinear) {
+    if (tg.tex) return go(fast_adjoint_remarch_kernel<FILTER, BLEND, VT, kGatherTexture>);
+  }
+  return go(fast_adjoint_remarch_kernel<FILTER, BLEND, VT, kGatherDirect>);
+}
+
 // The window kernel (dvr_window.cuh) adds its gradient window to global
 // memory in 16-byte groups and stages the volume in 16-byte rows: both
 // tensors must be z-contiguous with 16-byte aligned rows.
@@ -402,6 +459,16 @@ static cudaError_t fast_adjoint_go(const RenderParams& p, const AdjointParams& a
       if (rsmem <= size_t(li.max_smem_optin)) {
         last_adjoint_path() = DVR_PATH_RECORD;
         return fast_adjoint_record_go<FILTER, BLEND, VT>(p, a, order, counter, rsmem, smem, li, s);
+      }
+    }
+    // TF gradient only, from the checkpoints alone: the re-march kernel
+    const int chunk = p.ckpt.p ? remarch_chunk(p.ckpt_interval) : 0;
+    if (tfgrad && !volgrad && !a.has_camera && !a.has_stepsize && !a.has_viewport && !p.dens && chunk > 0) {
+      const size_t rsmem =
+          size_t(remarch_smem_floats(p.R, C, copies, kFastThreads / 32, chunk)) * sizeof(float);
+      if (rsmem <= size_t(li.max_smem_optin)) {
+        last_adjoint_path() = DVR_PATH_REMARCH;
+        return fast_adjoint_remarch_go<FILTER, BLEND, VT>(p, a, order, counter, chunk, rsmem, smem, li, s);
       }
     }
   }

@@ -129,15 +129,76 @@ __device__ __forceinline__ void record_sample_map(const TfShared<4>& tf, float s
   B = -a_k * (cur.x * adj_rgb.x + cur.y * adj_rgb.y + cur.z * adj_rgb.z);
 }
 
+// The TF-only reverse pass over a run of recorded samples [0, len) of one
+// ray, split over the 32 lanes of the calling warp: lane j takes the j-th of
+// 32 consecutive segments of L = ceil(len / 32) samples.  Each lane composes
+// the affine maps of its segment, a warp suffix scan gives the opacity
+// adjoint at the end of every segment, and each lane then walks its segment
+// back to front with the full reverse step.  The serial depth is 2 L samples
+// instead of len.  adj: the accumulator adjoint behind the run (the colour
+// adjoint, constant along the ray, and the opacity adjoint at the run's
+// end).  rec(k) returns sample k's (density, incoming opacity).  Returns, in
+// every lane, the opacity adjoint in front of the run.
+template <int BLEND, class Rec>
+__device__ __forceinline__ float record_run_adjoint(const TfShared<4>& tf, float step, int len, const f4 adj, Rec rec,
+                                                    TexelPairAtomic& acc_tf) {
+  const int lane = threadIdx.x & 31;
+  const int L = (len + 31) >> 5;
+  const int s0 = min(len, lane * L), s1 = min(len, s0 + L);
+
+  // 1. affine map of the segment: G = f_s0 o f_s0+1 o ... o f_s1-1
+  float A = 1.f, B = 0.f;
+  {
+    int k = s0;
+    for (; k + 1 < s1; k += 2) {
+      const float2 v0 = rec(k), v1 = rec(k + 1);
+      float A0, B0, A1, B1;
+      record_sample_map<BLEND>(tf, step, v0.x, adj, A0, B0);
+      record_sample_map<BLEND>(tf, step, v1.x, adj, A1, B1);
+      compose(A0, B0, A1, B1);
+      compose(A, B, A0, B0);
+    }
+    if (k < s1) {
+      float A0, B0;
+      record_sample_map<BLEND>(tf, step, rec(k).x, adj, A0, B0);
+      compose(A, B, A0, B0);
+    }
+  }
+  // 2. opacity adjoint behind each segment: suffix composition over the lanes
+  float SA = A, SB = B;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const float Ao = __shfl_down_sync(kFullMask, SA, o), Bo = __shfl_down_sync(kFullMask, SB, o);
+    if (lane + o < 32) compose(SA, SB, Ao, Bo);
+  }
+  const float NA = __shfl_down_sync(kFullMask, SA, 1), NB = __shfl_down_sync(kFullMask, SB, 1);
+  f4 adj_acc = adj;
+  if (lane < 31) adj_acc.w = fmaf(NA, adj.w, NB);
+
+  // 3. reverse walk over the segment
+  {
+    int k = s1 - 1;
+    float2 v0 = k >= s0 ? rec(k) : make_float2(0.f, 0.f);
+    float2 v1 = k - 1 >= s0 ? rec(k - 1) : make_float2(0.f, 0.f);
+    for (; k - 1 >= s0; k -= 2) {
+      const float2 u0 = k - 2 >= s0 ? rec(k - 2) : make_float2(0.f, 0.f);  // next pair, in flight
+      const float2 u1 = k - 3 >= s0 ? rec(k - 3) : make_float2(0.f, 0.f);
+      record_reverse_step<BLEND>(tf, step, v0.x, v0.y, adj_acc, acc_tf);
+      record_reverse_step<BLEND>(tf, step, v1.x, v1.y, adj_acc, acc_tf);
+      v0 = u0;
+      v1 = u1;
+    }
+    if (k >= s0) record_reverse_step<BLEND>(tf, step, v0.x, v0.y, adj_acc, acc_tf);
+  }
+  // lane 0's segment starts the run
+  return __shfl_sync(kFullMask, adj_acc.w, 0);
+}
+
 // ray_list[0 .. *ray_count): the rays with samples; leftover[0 .. counter[1]):
 // the rays left to the general kernel.  tf_slices: (blocks x warps) slices of
 // R*C floats, one per warp (TF gradient of a broadcast TF), zeroed here.
 //
-// One warp per ray: lane j takes the j-th of 32 consecutive segments of
-// L = ceil(n / 32) samples.  Each lane composes the affine maps of its
-// segment, a warp suffix scan gives the opacity adjoint at the end of every
-// segment, and each lane then walks its segment back to front with the full
-// reverse step.  The serial depth of a ray is 2 L samples instead of n.
+// One warp per ray: record_run_adjoint over the ray's n recorded samples.
 template <int BLEND>
 __global__ void __launch_bounds__(kFastThreads) fast_adjoint_record_kernel(const RenderParams p, const AdjointParams a,
                                                                             const RayOrder order, int* counter,
@@ -195,53 +256,159 @@ __global__ void __launch_bounds__(kFastThreads) fast_adjoint_record_kernel(const
       acc_tf.sc = a.adj_tf.s[2];
     }
 
-    // this lane's segment [s0, s1)
-    const int L = (n + 31) >> 5;
-    const int s0 = min(n, lane * L), s1 = min(n, s0 + L);
+    record_run_adjoint<BLEND>(tf, step, n, adj_col, [rec](int k) { return __ldg(rec + k); }, acc_tf);
+  }
 
-    // 1. affine map of the segment: G = f_s0 o f_s0+1 o ... o f_s1-1
-    float A = 1.f, B = 0.f;
-    {
-      int k = s0;
-      for (; k + 1 < s1; k += 2) {
-        const float2 v0 = __ldg(rec + k), v1 = __ldg(rec + k + 1);
-        float A0, B0, A1, B1;
-        record_sample_map<BLEND>(tf, step, v0.x, adj_col, A0, B0);
-        record_sample_map<BLEND>(tf, step, v1.x, adj_col, A1, B1);
-        compose(A0, B0, A1, B1);
-        compose(A, B, A0, B0);
-      }
-      if (k < s1) {
-        float A0, B0;
-        record_sample_map<BLEND>(tf, step, __ldg(rec + k).x, adj_col, A0, B0);
-        compose(A, B, A0, B0);
-      }
+  // TF gradient of the block
+  acc_tf.flush();
+  if (!per_batch) {
+    __syncthreads();
+    float* out = static_cast<float*>(a.adj_tf.p);
+    for (int e = threadIdx.x; e < n_tf; e += blockDim.x) {
+      float v = 0.f;
+      for (int w = 0; w < warps; ++w) v += __ldcg(block_slices + w * n_tf + e);
+      const int t = e / C, c = e - t * C;
+      if (v != 0.f) atomicAdd(out + t * a.adj_tf.s[1] + c * a.adj_tf.s[2], v);
     }
-    // 2. opacity adjoint behind each segment: suffix composition over the lanes
-    float SA = A, SB = B;
+  }
+}
+
+// Samples of one re-marched chunk: each warp's shared-memory run of
+// (density, incoming opacity) pairs holds this many.
+constexpr int kRemarchCap = 512;
+
+// The chunk length of the re-march adjoint for checkpoint interval K: a
+// multiple of K (every chunk starts at a checkpoint) and of 2 (a lane's two
+// samples are one 16-byte store), at most kRemarchCap; 0 when no such length
+// fits (never for the intervals the entry points accept, 1 to 64).
+__host__ __device__ inline int remarch_chunk(int K) {
+  const int unit = K % 2 == 0 ? K : 2 * K;
+  return K > 0 && unit <= kRemarchCap ? unit * (kRemarchCap / unit) : 0;
+}
+
+// Shared memory of the re-march adjoint (floats): the TF copies, then each
+// warp's run of `chunk` (density, opacity) pairs.
+__host__ __device__ inline int remarch_smem_floats(int R, int C, int tf_copies, int warps, int chunk) {
+  return record_smem_floats(R, C, tf_copies) + warps * chunk * 2;
+}
+
+// TF-gradient-only adjoint of a texture TF from the transmittance
+// checkpoints alone (no sample record): the memory-lean path.  One warp per
+// ray takes the ray's n samples in chunks of `chunk` samples from the back.
+// A chunk is re-marched from the checkpoint at its start (the opacity in
+// front of sample c0, written by the forward) with the forward's warp scan,
+// 64 samples per step and two per lane, into the warp's shared-memory run,
+// and that run is reversed by record_run_adjoint with the opacity adjoint
+// carried from the chunk behind it.  The adjoint needs O(warps) memory
+// instead of the record's O(samples), and each sample is gathered once more
+// than with the record.  Rays the checkpoints do not cover (n above
+// (slots + 1) K) go to leftover for the general kernel.  ray_list, leftover
+// and tf_slices as fast_adjoint_record_kernel; GATHER as the forward's
+// (direct loads or the slab texture tg).
+template <int FILTER, int BLEND, typename VT, int GATHER>
+__global__ void __launch_bounds__(kFastThreads) fast_adjoint_remarch_kernel(const RenderParams p, const AdjointParams a,
+                                                                             const RayOrder order, int* counter,
+                                                                             const int* ray_list, const int* ray_count,
+                                                                             int* leftover, float* tf_slices,
+                                                                             const TexGather tg, int chunk) {
+  extern __shared__ float4 fast_smem4[];
+  constexpr int C = 4;
+  float* s_tf = reinterpret_cast<float*>(fast_smem4);
+  const int copies = tf_copies(p);
+  for (int bb = 0; bb < copies; ++bb) stage_tf(p, bb, s_tf + bb * p.R * C);
+  const int n_tf = p.R * C;
+  const int warps = int(blockDim.x) / 32;
+  // the warp's run: 16-byte aligned (the TF part is a multiple of 4 floats,
+  // chunk is even)
+  float2* run = reinterpret_cast<float2*>(s_tf + record_smem_floats(p.R, C, copies)) +
+                size_t(threadIdx.x >> 5) * chunk;
+  const bool per_batch = a.adj_tf.s[0] != 0;
+  float* block_slices = tf_slices + size_t(blockIdx.x) * warps * n_tf;
+  if (!per_batch)
+    for (int e = threadIdx.x; e < warps * n_tf; e += blockDim.x) block_slices[e] = 0.f;
+  __syncthreads();
+
+  const int lane = threadIdx.x & 31;
+  const int total = *ray_count;
+  const int K = p.ckpt_interval;
+  TexelPairAtomic acc_tf;
+  acc_tf.R = p.R;
+  if (!per_batch) acc_tf.dst = block_slices + (threadIdx.x >> 5) * n_tf;
+  int cur_b = -1;
+
+  while (true) {
+    int pos = 0;
+    if (lane == 0) pos = atomicAdd(counter, 1);
+    pos = __shfl_sync(kFullMask, pos, 0);
+    if (pos >= total) break;
+    const int id = ray_list[pos];
+    int b, x, y;
+    if (!order.pixel(id, b, x, y)) continue;
+    FastRay q;
+    fast_setup(p, x, y, b, q);
+    const int n = min(static_cast<const int*>(a.fwd_term.p)[b * a.fwd_term.s[0] + y * a.fwd_term.s[1] +
+                                                             x * a.fwd_term.s[2]],
+                      max_samples(q.tmin, q.tmax, q.step));
+    if (n <= 0) continue;
+    // every chunk start c0 < n is a multiple of K with c0 / K - 1 < slots
+    if (n > (p.ckpt_slots + 1) * K) {
+      if (lane == 0) leftover[atomicAdd(counter + 1, 1)] = id;
+      continue;
+    }
+    const float* ck = static_cast<const float*>(p.ckpt.p) + b * p.ckpt.s[0] + y * p.ckpt.s[1] + x * p.ckpt.s[2];
+    const float* ac = static_cast<const float*>(a.adj_color.p) + b * a.adj_color.s[0] + y * a.adj_color.s[1] +
+                      x * a.adj_color.s[2];
+    f4 adj = mk4(ac[0], ac[a.adj_color.s[3]], ac[2 * a.adj_color.s[3]], ac[3 * a.adj_color.s[3]]);
+    const TfShared<C> tf{s_tf + (copies > 1 ? b : 0) * n_tf, p.R};
+    if (per_batch && b != cur_b) {
+      acc_tf.flush();
+      cur_b = b;
+      acc_tf.dst = static_cast<float*>(a.adj_tf.p) + b * a.adj_tf.s[0];
+      acc_tf.sr = a.adj_tf.s[1];
+      acc_tf.sc = a.adj_tf.s[2];
+    }
+    const VolumeFast<VT> vol{static_cast<const VT*>(p.volume.p) + b * p.volume.s[0], int(p.volume.s[1]),
+                             int(p.volume.s[2]), int(p.volume.s[3]), p.X - 1, p.Y - 1, p.Z - 1};
+    const TexVolume<VT> tv{tg, p.volume.s[0] != 0 ? b * p.X : 0, p.X - 1, p.Y - 1, p.Z - 1};
+
+    for (int c0 = ((n - 1) / chunk) * chunk; c0 >= 0; c0 -= chunk) {
+      const int len = min(n - c0, chunk);
+      // 1. re-march [c0, c0 + len) from the opacity in front of sample c0
+      float alpha = c0 > 0 ? ck[(c0 / K - 1) * p.ckpt.s[3]] : 0.f;
+      for (int s0 = 0; s0 < len; s0 += 64) {
+        const int i0 = s0 + 2 * lane;  // the lane's samples: run entries i0 and i0 + 1
+        const bool in0 = i0 < len, in1 = i0 + 1 < len;
+        float d[2], a_s[2] = {0.f, 0.f};
+        // lanes past the chunk's end gather at its first sample (inside the
+        // ray) and discard the value
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const float Ao = __shfl_down_sync(kFullMask, SA, o), Bo = __shfl_down_sync(kFullMask, SB, o);
-      if (lane + o < 32) compose(SA, SB, Ao, Bo);
-    }
-    const float NA = __shfl_down_sync(kFullMask, SA, 1), NB = __shfl_down_sync(kFullMask, SB, 1);
-    f4 adj_acc = adj_col;
-    if (lane < 31) adj_acc.w = fmaf(NA, adj_col.w, NB);
-
-    // 3. reverse walk over the segment
-    {
-      int k = s1 - 1;
-      float2 v0 = k >= s0 ? __ldg(rec + k) : make_float2(0.f, 0.f);
-      float2 v1 = k - 1 >= s0 ? __ldg(rec + k - 1) : make_float2(0.f, 0.f);
-      for (; k - 1 >= s0; k -= 2) {
-        const float2 u0 = k - 2 >= s0 ? __ldg(rec + k - 2) : make_float2(0.f, 0.f);  // next pair, in flight
-        const float2 u1 = k - 3 >= s0 ? __ldg(rec + k - 3) : make_float2(0.f, 0.f);
-        record_reverse_step<BLEND>(tf, step, v0.x, v0.y, adj_acc, acc_tf);
-        record_reverse_step<BLEND>(tf, step, v1.x, v1.y, adj_acc, acc_tf);
-        v0 = u0;
-        v1 = u1;
+        for (int i = 0; i < 2; ++i) {
+          const int k = c0 + ((i == 0 ? in0 : in1) ? i0 + i : 0);
+          const float3 q3 = fast_pos(q, q.tmin + k * q.step);
+          if constexpr (GATHER == kGatherTexture) d[i] = tv.sample(q3);
+          else d[i] = sample_density<FILTER, VT>(vol, q3);
+        }
+        if (in0) a_s[0] = blend_alpha<BLEND>(tf_eval<kTfTexture>(tf, d[0]).w, q.step);
+        if (in1) a_s[1] = blend_alpha<BLEND>(tf_eval<kTfTexture>(tf, d[1]).w, q.step);
+        // incoming opacity of each sample: exclusive "over" scan of the pairs
+        float incl = over(a_s[0], a_s[1]);
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const float v = __shfl_up_sync(kFullMask, incl, o);
+          if (lane >= o) incl = over(v, incl);
+        }
+        float excl = __shfl_up_sync(kFullMask, incl, 1);
+        if (lane == 0) excl = 0.f;
+        const float a_in0 = over(alpha, excl), a_in1 = over(a_in0, a_s[0]);
+        if (in1) *reinterpret_cast<float4*>(run + i0) = make_float4(d[0], a_in0, d[1], a_in1);
+        else if (in0) run[i0] = make_float2(d[0], a_in0);
+        alpha = over(alpha, __shfl_sync(kFullMask, incl, 31));
       }
-      if (k >= s0) record_reverse_step<BLEND>(tf, step, v0.x, v0.y, adj_acc, acc_tf);
+      __syncwarp();
+      // 2. reverse the chunk; the opacity adjoint in front of it goes on to
+      // the chunk before
+      adj.w = record_run_adjoint<BLEND>(tf, q.step, len, adj, [run](int k) { return run[k]; }, acc_tf);
+      __syncwarp();
     }
   }
 

@@ -352,7 +352,9 @@ enum DvrAdjointPath {
   DVR_PATH_GENERAL = 2,  /* general per-ray kernel (checkpoints or blend inversion) */
   DVR_PATH_RECORD = 3,   /* record kernel (TF gradient of a texture TF from the sample record) */
   DVR_PATH_WINDOW = 4,   /* window kernel (volume gradient from the sample record) */
-  DVR_PATH_PRESHADED = 5 /* pre-shaded kernels */
+  DVR_PATH_PRESHADED = 5, /* pre-shaded kernels */
+  DVR_PATH_REMARCH = 6   /* re-march kernel (TF gradient of a texture TF from the
+                            checkpoints alone: chunks re-marched into shared memory) */
 };
 int dvr_last_adjoint_path(void);
 
