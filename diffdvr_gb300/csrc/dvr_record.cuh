@@ -278,18 +278,21 @@ __global__ void __launch_bounds__(kFastThreads) fast_adjoint_record_kernel(const
 constexpr int kRemarchCap = 512;
 
 // The chunk length of the re-march adjoint for checkpoint interval K: a
-// multiple of K (every chunk starts at a checkpoint) and of 2 (a lane's two
-// samples are one 16-byte store), at most kRemarchCap; 0 when no such length
-// fits (never for the intervals the entry points accept, 1 to 64).
+// multiple of K (every chunk starts at a checkpoint) and of 2, at most
+// kRemarchCap; 0 when no such length fits (never for the intervals the entry
+// points accept, 1 to 64).
 __host__ __device__ inline int remarch_chunk(int K) {
   const int unit = K % 2 == 0 ? K : 2 * K;
   return K > 0 && unit <= kRemarchCap ? unit * (kRemarchCap / unit) : 0;
 }
 
+// Entries of a warp's run: the chunk's pairs and up to 32 pad entries.
+__host__ __device__ inline int remarch_run_entries(int chunk) { return chunk + 32; }
+
 // Shared memory of the re-march adjoint (floats): the TF copies, then each
-// warp's run of `chunk` (density, opacity) pairs.
+// warp's run of (density, opacity) pairs.
 __host__ __device__ inline int remarch_smem_floats(int R, int C, int tf_copies, int warps, int chunk) {
-  return record_smem_floats(R, C, tf_copies) + warps * chunk * 2;
+  return record_smem_floats(R, C, tf_copies) + warps * remarch_run_entries(chunk) * 2;
 }
 
 // TF-gradient-only adjoint of a texture TF from the transmittance
@@ -306,7 +309,7 @@ __host__ __device__ inline int remarch_smem_floats(int R, int C, int tf_copies, 
 // and tf_slices as fast_adjoint_record_kernel; GATHER as the forward's
 // (direct loads or the slab texture tg).
 template <int FILTER, int BLEND, typename VT, int GATHER>
-__global__ void __launch_bounds__(kFastThreads) fast_adjoint_remarch_kernel(const RenderParams p, const AdjointParams a,
+__global__ void __launch_bounds__(kFastThreads, 6) fast_adjoint_remarch_kernel(const RenderParams p, const AdjointParams a,
                                                                              const RayOrder order, int* counter,
                                                                              const int* ray_list, const int* ray_count,
                                                                              int* leftover, float* tf_slices,
@@ -318,10 +321,9 @@ __global__ void __launch_bounds__(kFastThreads) fast_adjoint_remarch_kernel(cons
   for (int bb = 0; bb < copies; ++bb) stage_tf(p, bb, s_tf + bb * p.R * C);
   const int n_tf = p.R * C;
   const int warps = int(blockDim.x) / 32;
-  // the warp's run: 16-byte aligned (the TF part is a multiple of 4 floats,
-  // chunk is even)
+  // the warp's run of remarch_run_entries(chunk) pairs
   float2* run = reinterpret_cast<float2*>(s_tf + record_smem_floats(p.R, C, copies)) +
-                size_t(threadIdx.x >> 5) * chunk;
+                size_t(threadIdx.x >> 5) * remarch_run_entries(chunk);
   const bool per_batch = a.adj_tf.s[0] != 0;
   float* block_slices = tf_slices + size_t(blockIdx.x) * warps * n_tf;
   if (!per_batch)
@@ -373,6 +375,14 @@ __global__ void __launch_bounds__(kFastThreads) fast_adjoint_remarch_kernel(cons
 
     for (int c0 = ((n - 1) / chunk) * chunk; c0 >= 0; c0 -= chunk) {
       const int len = min(n - c0, chunk);
+      // The reverse pass reads lane j's segment [j L, j L + L) of the run
+      // (L = ceil(len / 32)) one entry per lane at a time.  Sample i is stored
+      // at i + pad floor(i / L), one pad entry after every segment when L is
+      // even, so the lanes' entries lie an odd number L + pad of pairs apart
+      // and a half-warp's reads fall in distinct banks.  At most 31 pads.
+      const int L = (len + 31) >> 5;
+      const int pad = (L & 1) ^ 1;
+      const float inv_L = 1.f / float(L);
       // 1. re-march [c0, c0 + len) from the opacity in front of sample c0
       float alpha = c0 > 0 ? ck[(c0 / K - 1) * p.ckpt.s[3]] : 0.f;
       for (int s0 = 0; s0 < len; s0 += 64) {
@@ -400,14 +410,23 @@ __global__ void __launch_bounds__(kFastThreads) fast_adjoint_remarch_kernel(cons
         float excl = __shfl_up_sync(kFullMask, incl, 1);
         if (lane == 0) excl = 0.f;
         const float a_in0 = over(alpha, excl), a_in1 = over(a_in0, a_s[0]);
-        if (in1) *reinterpret_cast<float4*>(run + i0) = make_float4(d[0], a_in0, d[1], a_in1);
-        else if (in0) run[i0] = make_float2(d[0], a_in0);
+        // floor(i / L) for i < 512, L <= 16: (i + 1/2) / L is at least 1/32
+        // from an integer, far above the rounding of one multiplication
+        if (pad) {
+          if (in0) run[i0 + __float2int_rz((float(i0) + 0.5f) * inv_L)] = make_float2(d[0], a_in0);
+          if (in1) run[i0 + 1 + __float2int_rz((float(i0) + 1.5f) * inv_L)] = make_float2(d[1], a_in1);
+        } else {
+          if (in0) run[i0] = make_float2(d[0], a_in0);
+          if (in1) run[i0 + 1] = make_float2(d[1], a_in1);
+        }
         alpha = over(alpha, __shfl_sync(kFullMask, incl, 31));
       }
       __syncwarp();
       // 2. reverse the chunk; the opacity adjoint in front of it goes on to
       // the chunk before
-      adj.w = record_run_adjoint<BLEND>(tf, q.step, len, adj, [run](int k) { return run[k]; }, acc_tf);
+      // lane j reads only its own segment: entry k sits at k + j pad
+      const float2* seg = run + lane * pad;
+      adj.w = record_run_adjoint<BLEND>(tf, q.step, len, adj, [seg](int k) { return seg[k]; }, acc_tf);
       __syncwarp();
     }
   }
