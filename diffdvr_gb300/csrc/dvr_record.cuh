@@ -137,8 +137,9 @@ __device__ __forceinline__ void record_sample_map(const TfShared<4>& tf, float s
 // back to front with the full reverse step.  The serial depth is 2 L samples
 // instead of len.  adj: the accumulator adjoint behind the run (the colour
 // adjoint, constant along the ray, and the opacity adjoint at the run's
-// end).  rec(k) returns sample k's (density, incoming opacity).  Returns, in
-// every lane, the opacity adjoint in front of the run.
+// end).  rec(k) returns sample k's (density, incoming opacity).  Returns the
+// opacity adjoint in front of the lane's segment: lane 0's value is the one
+// in front of the run.
 template <int BLEND, class Rec>
 __device__ __forceinline__ float record_run_adjoint(const TfShared<4>& tf, float step, int len, const f4 adj, Rec rec,
                                                     TexelPairAtomic& acc_tf) {
@@ -190,8 +191,7 @@ __device__ __forceinline__ float record_run_adjoint(const TfShared<4>& tf, float
     }
     if (k >= s0) record_reverse_step<BLEND>(tf, step, v0.x, v0.y, adj_acc, acc_tf);
   }
-  // lane 0's segment starts the run
-  return __shfl_sync(kFullMask, adj_acc.w, 0);
+  return adj_acc.w;
 }
 
 // ray_list[0 .. *ray_count): the rays with samples; leftover[0 .. counter[1]):
@@ -426,7 +426,8 @@ __global__ void __launch_bounds__(kFastThreads, 6) fast_adjoint_remarch_kernel(c
       // the chunk before
       // lane j reads only its own segment: entry k sits at k + j pad
       const float2* seg = run + lane * pad;
-      adj.w = record_run_adjoint<BLEND>(tf, q.step, len, adj, [seg](int k) { return seg[k]; }, acc_tf);
+      adj.w = __shfl_sync(kFullMask,
+                          record_run_adjoint<BLEND>(tf, q.step, len, adj, [seg](int k) { return seg[k]; }, acc_tf), 0);
       __syncwarp();
     }
   }
