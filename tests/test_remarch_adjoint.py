@@ -118,3 +118,22 @@ def test_remarch_adjoint_leaves_uncovered_rays_to_the_general_kernel(oracle_buil
     got, path = _adjoint(case, inp, out, adj, "direct")
     assert path == "remarch"
     assert rel_l2(got, ref) <= max(1e-3, 3 * r32), (rel_l2(got, ref), r32)
+
+
+@pytest.mark.parametrize("gather", ["direct", "texture"])
+def test_remarch_adjoint_with_a_broadcast_tf(gather, oracle_built, cuda_device):
+    """One TF for both batch entries: the TF gradient sums the entries' rays
+    through the per-warp slices, as the headline's eight views do."""
+    O = oracle_built
+    case = _case(941, 1, 0)
+    case.tf = np.ascontiguousarray(case.tf[:1])
+    inp, out, term, adj = _tf_grad(case, 16, torch.float32, gather)
+    assert int(term.max()) > 512
+    ref, r32, adj = _oracle(case, O, term, adj)
+    got, path = _adjoint(case, inp, out, adj, gather)
+    assert path == "remarch" and got.shape == case.tf.shape
+    assert rel_l2(got, ref) <= max(1e-3, 3 * r32), (rel_l2(got, ref), r32)
+    inp2, out2, term2, _ = _tf_grad(case, 16, torch.float32, gather, record="full")
+    got2, path2 = _adjoint(case, inp2, out2, adj, gather)
+    assert path2 == "record" and np.array_equal(term2, term)
+    assert rel_l2(got, got2) <= 2e-5, rel_l2(got, got2)
