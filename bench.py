@@ -786,6 +786,9 @@ def run_gpu(args):
             "adjoint_ms": float(np.mean([a_.elapsed_time(b_) for a_, b_ in adj_ev])),
             "checkpoint_interval": K, "checkpoint_MB": round(ckpt.numel() * 4 / 1e6, 1),
             "adjoint_path": ck_path,
+            "issue": issue_bound(args.workload, "adjoint_remarch", samples,
+                                 float(np.mean([a_.elapsed_time(b_) for a_, b_ in adj_ev])))
+            if ck_path == "remarch" else None,
             "path": "no sample record; the adjoint re-marches from the checkpoints (remarch: each warp re-marches its "
                     "ray in chunks of up to 512 samples into shared memory; general: per-ray K-sample segments)"}
 
