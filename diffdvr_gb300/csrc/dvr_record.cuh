@@ -309,11 +309,10 @@ __host__ __device__ inline int remarch_smem_floats(int R, int C, int tf_copies, 
 // and tf_slices as fast_adjoint_record_kernel; GATHER as the forward's
 // (direct loads or the slab texture tg).
 template <int FILTER, int BLEND, typename VT, int GATHER>
-__global__ void __launch_bounds__(kFastThreads, 6) fast_adjoint_remarch_kernel(const RenderParams p, const AdjointParams a,
-                                                                             const RayOrder order, int* counter,
-                                                                             const int* ray_list, const int* ray_count,
-                                                                             int* leftover, float* tf_slices,
-                                                                             const TexGather tg, int chunk) {
+__global__ void __launch_bounds__(kFastThreads, 6)
+    fast_adjoint_remarch_kernel(const RenderParams p, const AdjointParams a, const RayOrder order, int* counter,
+                                const int* ray_list, const int* ray_count, int* leftover, float* tf_slices,
+                                const TexGather tg, int chunk) {
   extern __shared__ float4 fast_smem4[];
   constexpr int C = 4;
   float* s_tf = reinterpret_cast<float*>(fast_smem4);
