@@ -79,6 +79,10 @@ def test_issue_bound_from_the_committed_profile(monkeypatch, tmp_path):
     assert d["achieved"] == pytest.approx(per * 90e6 / 0.8e-3 / 1e12)
     assert d["peak"] == pytest.approx(152 * 4 * 2070e6 / 1e12)
     assert 0 < d["frac"] < 1.2
+    # every kernel the bench line asks for has its committed figure: the
+    # record arm's forward and adjoint, the memory-lean arm's re-march adjoint
+    for kernel in ("forward", "adjoint", "adjoint_remarch"):
+        assert bench.issue_bound("tf_reconstruction_256", kernel, 90_000_000, 1.0) is not None, kernel
     assert bench.issue_bound("no_such_workload", "forward", 1, 1.0) is None
     monkeypatch.setattr(bench, "ROOT", str(tmp_path))
     assert bench.issue_bound("tf_reconstruction_256", "forward", 1, 1.0) is None
